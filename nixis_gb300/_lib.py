@@ -1,0 +1,69 @@
+"""ctypes binding of libnixis_gb300.so (the C ABI in include/nixis_gb300.h).
+
+The library is the only compute path: if it cannot be built or loaded, every
+entry point raises.  There is no CPU fallback.
+"""
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_p = ctypes.c_void_p
+_i32 = ctypes.c_int
+_i64 = ctypes.c_int64
+_d = ctypes.c_double
+_u64 = ctypes.c_ulonglong
+
+# name -> (restype, argtypes); every symbol declared in include/nixis_gb300.h
+SIGNATURES = {
+    "nx_last_error": (ctypes.c_char_p, []),
+    "nx_version": (_i32, []),
+    "nx_launch_count": (_u64, []),
+    "nx_perm_init": (_i32, [_i64, _p, _p]),
+    "nx_fbm": (_i32, [_p, _i64, _p, _p, _i32, _p, _p, _d, _p, _p, _i32, _p, _p]),
+    "nx_sample_octaves": (_i32, [_p, _i64, _p, _p, _i32, _d, _d, _d, _d, _d, _p, _p, _i32, _p]),
+    "nx_noise3d_trace": (_i32, [_p, _i64, _p, _p, _d, _p, _p, _p, _p, _p]),
+}
+
+_lock = threading.Lock()
+_LIB = None
+
+
+class NxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"nixis_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Load (building first if needed) the CUDA library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _lock:
+        if _LIB is None:
+            if os.environ.get("NIXIS_GB300_NO_BUILD") != "1":
+                _build.build()
+            if not os.path.exists(_build.LIB):
+                raise RuntimeError(f"{_build.LIB} is missing; build it with python -m nixis_gb300.build")
+            L = ctypes.CDLL(_build.LIB)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _LIB = L
+    return _LIB
+
+
+def check(rc):
+    if rc != 0:
+        raise NxError(rc, lib().nx_last_error().decode(errors="replace"))
+
+
+def call(name, *args):
+    check(getattr(lib(), name)(*args))
+
+
+def launch_count():
+    return int(lib().nx_launch_count())

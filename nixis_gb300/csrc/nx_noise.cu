@@ -1,0 +1,563 @@
+// nx_noise.cu -- fused fractal OpenSimplex-3D noise (fBm) for sm_103a.
+//
+// Replaces terrain.sample_octaves / terrain.sample_noise (terrain.py:12-59)
+// over opensimplex.noise3d (opensimplex.py:266-759).
+//
+// Design
+//  * One thread per vertex, all octaves in registers; persistent grid of
+//    (#SM x resident CTAs) walking the vertex range.
+//  * The seeded tables live in shared memory as one packed word per entry
+//    [bits 0-6: gz+16 | bits 7-14: perm | bits 16-23: gx+16 | 24-31: gy+16],
+//    replicated 32 times (entry k of lane l at word 32*k + l) so the three
+//    dependent hash loads of a warp never conflict on a bank.
+//  * Arithmetic is binary32.  The lattice cell, the region and the two extra
+//    lattice points must equal what binary64 decides.  The large-magnitude
+//    part of the skew is removed exactly: x*scale is formed as a float pair,
+//    split into an integer A and a fraction a in [-1/2, 1/2], and with
+//    T = Ax+Ay+Az = 6q + r the skewed coordinate becomes
+//    xs = (Ax - q) + (a_x - (r + a_x + a_y + a_z)/6), whose second term is
+//    O(1) and carries an absolute error below 3e-7 (derivation in the design
+//    notes).  Every comparison that decides the cell or region records its
+//    margin; when the smallest margin is below TAU (>= 4x the error bound),
+//    or |x*scale| >= 2^16, that lane recomputes the decisions in binary64
+//    with the reference's operation order (decide_f64), so the decisions
+//    always equal the reference's.
+//  * The 6 or 8 contributions are evaluated branch-free as 9 slots: the
+//    corner (0,0,0)|(1,1,1), the six mixed corners, and the two extra points,
+//    with masks per region; hash prefixes of the fixed slots are shared.
+#include "nx_common.cuh"
+
+#include <cmath>
+
+namespace {
+
+constexpr float MAGIC = 12582912.0f;   // 1.5 * 2^23: v + MAGIC rounds v to an integer, |v| < 2^22
+constexpr int MAGIC_BITS = 0x4B400000;
+constexpr float TAU = 4.0e-6f;         // decision margin below which binary64 decides
+constexpr float PMAX = 65536.0f;       // |x*scale| bound of the binary32 decision path
+constexpr float THIRD = 1.0f / 3.0f;
+constexpr float SIXTH = 1.0f / 6.0f;
+constexpr float GBIAS = 8388624.0f;    // 2^23 + 16: removes the byte bias of a packed gradient
+
+// opensimplex.py:51-60 (GRADIENTS_3D), used only to build the packed table.
+__constant__ int c_grad3[72] = {
+    -11, 4, 4, -4, 11, 4, -4, 4, 11,
+    11, 4, 4, 4, 11, 4, 4, 4, 11,
+    -11, -4, 4, -4, -11, 4, -4, -4, 11,
+    11, -4, 4, 4, -11, 4, 4, -4, 11,
+    -11, 4, -4, -4, 11, -4, -4, 4, -11,
+    11, 4, -4, 4, 11, -4, 4, 4, -11,
+    -11, -4, -4, -4, -11, -4, -4, -4, -11,
+    11, -4, -4, 4, -11, -4, 4, -4, -11,
+};
+
+struct FbmParams {
+    int n_oct;
+    float s_hi[NX_MAX_OCTAVES];   // scale[o] as a binary32 pair
+    float s_lo[NX_MAX_OCTAVES];
+    float amp[NX_MAX_OCTAVES];    // 0.5 * strength[o] * radius
+    double s[NX_MAX_OCTAVES];     // scale[o] (binary64 decision path)
+};
+
+constexpr int TABLE_WORDS = 256 * 32;
+constexpr int TABLE_BYTES = TABLE_WORDS * 4;
+
+__device__ __forceinline__ void build_table(uint32_t *T, const int32_t *__restrict__ perm,
+                                            const int32_t *__restrict__ pgi)
+{
+    for (int i = threadIdx.x; i < TABLE_WORDS; i += blockDim.x) {
+        int k = i >> 5;
+        uint32_t p = (uint32_t)perm[k] & 255u;
+        int g = pgi[k];
+        g = g < 0 ? 0 : (g > 69 ? 69 : g);
+        uint32_t w = ((uint32_t)(c_grad3[g + 2] + 16) & 0x7Fu) | (p << 7) |
+                     ((uint32_t)(c_grad3[g] + 16) << 16) | ((uint32_t)(c_grad3[g + 1] + 16) << 24);
+        T[i] = w;
+    }
+}
+
+// Hash table load: bits 7-14 of a select the entry; lb = this lane's byte
+// offset of replica 0 in shared memory.
+__device__ __forceinline__ uint32_t lk(uint32_t lb, int a)
+{
+    uint32_t v;
+    uint32_t addr = lb + ((uint32_t)a & 0x7F80u);
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
+}
+
+// Split a binary64 into hi + lo binary32 with integer operations (no FP64
+// unit): hi = value truncated to 24 significant bits, lo = the next 23 bits.
+// |x - (hi+lo)| <= 2^-47 |x|.  Magnitudes outside [2^-74, 2^127] give lo = 0
+// (and hi = +-0 or +-inf); such lanes take the binary64 path anyway.
+__device__ __forceinline__ void split_f64(double v, float &hi, float &lo)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
+    int e = (int)((hw >> 20) & 0x7FF) - 1023;
+    uint32_t sign = hw & 0x80000000u;
+    if (e < -126) { hi = __uint_as_float(sign); lo = 0.0f; return; }
+    if (e > 127) { hi = __uint_as_float(sign | 0x7F800000u); lo = 0.0f; return; }
+    uint32_t top = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
+    hi = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | top);
+    if (e < -74 + 6) { lo = 0.0f; return; }
+    // remainder bits 28..6 of the low word, as 23-bit integer times 2^(e-46)
+    uint32_t rem = (lw & 0x1FFFFFFFu) >> 6;
+    float r = __uint_as_float(0x4B000000u | rem) - 8388608.0f;    // exact
+    float sc = __uint_as_float((uint32_t)(e - 46 + 127) << 23);
+    lo = __uint_as_float(__float_as_uint(r * sc) | sign);
+}
+
+// Decisions of noise3d (opensimplex.py:302-700) in either precision.  For
+// float, `m` tracks the smallest |a-b| over the comparisons on the taken
+// path; for double it is unused.  Extra-point offsets are relative to the
+// cell origin (components in {-1,0,1,2}).
+struct Decision {
+    int region;
+    float e0x, e0y, e0z, e1x, e1y, e1z;
+};
+
+template <typename T, bool TRACK>
+struct Cmp {
+    float m;
+    __device__ __forceinline__ void note(T a, T b)
+    {
+        if (TRACK) m = fminf(m, fabsf((float)(a - b)));
+    }
+    __device__ __forceinline__ bool gt(T a, T b) { note(a, b); return a > b; }
+    __device__ __forceinline__ bool ge(T a, T b) { note(a, b); return a >= b; }
+    __device__ __forceinline__ bool lt(T a, T b) { note(a, b); return a < b; }
+    __device__ __forceinline__ bool le(T a, T b) { note(a, b); return a <= b; }
+};
+
+template <typename T, bool TRACK>
+__device__ __forceinline__ void decide(T xins, T yins, T zins, T in_sum, Cmp<T, TRACK> &C,
+                                       Decision &D)
+{
+    const T one = (T)1, two = (T)2, three = (T)3;
+    if (C.le(in_sum, one)) {
+        // tetrahedron at (0,0,0): closest two of (1,0,0), (0,1,0), (0,0,1)
+        D.region = 0;
+        int ap = 1, bp = 2;
+        T as = xins, bs = yins;
+        if (C.ge(as, bs)) {
+            if (C.gt(zins, bs)) { bs = zins; bp = 4; }
+        } else {
+            if (C.gt(zins, as)) { as = zins; ap = 4; }
+        }
+        T wins = one - in_sum;
+        bool near0 = C.gt(wins, as);
+        if (!near0) near0 = C.gt(wins, bs);
+        if (near0) {
+            int c = C.gt(bs, as) ? bp : ap;
+            if ((c & 1) == 0) { D.e0x = -1.f; D.e1x = 0.f; } else { D.e0x = 1.f; D.e1x = 1.f; }
+            if ((c & 2) == 0) {
+                D.e0y = 0.f; D.e1y = 0.f;
+                if ((c & 1) == 0) D.e1y = -1.f; else D.e0y = -1.f;
+            } else { D.e0y = 1.f; D.e1y = 1.f; }
+            if ((c & 4) == 0) { D.e0z = 0.f; D.e1z = -1.f; } else { D.e0z = 1.f; D.e1z = 1.f; }
+        } else {
+            int c = ap | bp;
+            if ((c & 1) == 0) { D.e0x = 0.f; D.e1x = -1.f; } else { D.e0x = 1.f; D.e1x = 1.f; }
+            if ((c & 2) == 0) { D.e0y = 0.f; D.e1y = -1.f; } else { D.e0y = 1.f; D.e1y = 1.f; }
+            if ((c & 4) == 0) { D.e0z = 0.f; D.e1z = -1.f; } else { D.e0z = 1.f; D.e1z = 1.f; }
+        }
+    } else if (C.ge(in_sum, two)) {
+        // tetrahedron at (1,1,1): closest two of (1,1,0), (1,0,1), (0,1,1)
+        D.region = 1;
+        int ap = 6, bp = 5;
+        T as = xins, bs = yins;
+        if (C.le(as, bs)) {
+            if (C.lt(zins, bs)) { bs = zins; bp = 3; }
+        } else {
+            if (C.lt(zins, as)) { as = zins; ap = 3; }
+        }
+        T wins = three - in_sum;
+        bool near1 = C.lt(wins, as);
+        if (!near1) near1 = C.lt(wins, bs);
+        if (near1) {
+            int c = C.lt(bs, as) ? bp : ap;
+            if ((c & 1) != 0) { D.e0x = 2.f; D.e1x = 1.f; } else { D.e0x = 0.f; D.e1x = 0.f; }
+            if ((c & 2) != 0) {
+                D.e0y = 1.f; D.e1y = 1.f;
+                if ((c & 1) != 0) D.e1y = 2.f; else D.e0y = 2.f;
+            } else { D.e0y = 0.f; D.e1y = 0.f; }
+            if ((c & 4) != 0) { D.e0z = 1.f; D.e1z = 2.f; } else { D.e0z = 0.f; D.e1z = 0.f; }
+        } else {
+            int c = ap & bp;
+            if ((c & 1) != 0) { D.e0x = 1.f; D.e1x = 2.f; } else { D.e0x = 0.f; D.e1x = 0.f; }
+            if ((c & 2) != 0) { D.e0y = 1.f; D.e1y = 2.f; } else { D.e0y = 0.f; D.e1y = 0.f; }
+            if ((c & 4) != 0) { D.e0z = 1.f; D.e1z = 2.f; } else { D.e0z = 0.f; D.e1z = 0.f; }
+        }
+    } else {
+        // octahedron between them
+        D.region = 2;
+        T as, bs, score;
+        int ap, bp;
+        bool af, bf;
+        T p1 = xins + yins;
+        if (C.gt(p1, one)) { as = p1 - one; ap = 3; af = true; }
+        else { as = one - p1; ap = 4; af = false; }
+        T p2 = xins + zins;
+        if (C.gt(p2, one)) { bs = p2 - one; bp = 5; bf = true; }
+        else { bs = one - p2; bp = 2; bf = false; }
+        T p3 = yins + zins;
+        bool t3 = C.gt(p3, one);
+        score = t3 ? p3 - one : one - p3;
+        if (C.le(as, bs)) {
+            if (C.lt(as, score)) { ap = t3 ? 6 : 1; af = t3; }
+        } else {
+            if (C.lt(bs, score)) { bp = t3 ? 6 : 1; bf = t3; }
+        }
+        if (af == bf) {
+            if (af) {
+                D.e0x = 1.f; D.e0y = 1.f; D.e0z = 1.f;
+                int c = ap & bp;
+                if (c & 1) { D.e1x = 2.f; D.e1y = 0.f; D.e1z = 0.f; }
+                else if (c & 2) { D.e1x = 0.f; D.e1y = 2.f; D.e1z = 0.f; }
+                else { D.e1x = 0.f; D.e1y = 0.f; D.e1z = 2.f; }
+            } else {
+                D.e0x = 0.f; D.e0y = 0.f; D.e0z = 0.f;
+                int c = ap | bp;
+                if ((c & 1) == 0) { D.e1x = -1.f; D.e1y = 1.f; D.e1z = 1.f; }
+                else if ((c & 2) == 0) { D.e1x = 1.f; D.e1y = -1.f; D.e1z = 1.f; }
+                else { D.e1x = 1.f; D.e1y = 1.f; D.e1z = -1.f; }
+            }
+        } else {
+            int c1 = af ? ap : bp;
+            int c2 = af ? bp : ap;
+            if ((c1 & 1) == 0) { D.e0x = -1.f; D.e0y = 1.f; D.e0z = 1.f; }
+            else if ((c1 & 2) == 0) { D.e0x = 1.f; D.e0y = -1.f; D.e0z = 1.f; }
+            else { D.e0x = 1.f; D.e0y = 1.f; D.e0z = -1.f; }
+            D.e1x = 0.f; D.e1y = 0.f; D.e1z = 0.f;
+            if (c2 & 1) D.e1x = 2.f;
+            else if (c2 & 2) D.e1y = 2.f;
+            else D.e1z = 2.f;
+        }
+    }
+}
+
+// opensimplex.py:18-21 in binary64
+__device__ __forceinline__ long long fastfloor64(double x)
+{
+    long long xi = __double2ll_rz(x);
+    return x < (double)xi ? xi - 1 : xi;
+}
+
+// The cell state the contributions need.
+struct Cell {
+    float dx0, dy0, dz0;
+    int xb7, yb7, zb7;       // cell origin << 7 (hash base)
+    int xsb, ysb, zsb;       // cell origin (trace only)
+    Decision D;
+};
+
+// Binary64 decisions with the reference's operation order (opensimplex.py:
+// 270-300 and the region code).  No FMA contraction: explicit _rn ops.
+__device__ __noinline__ void decide_f64(double X, double Y, double Z, double s, Cell &c)
+{
+    double x = __dmul_rn(X, s), y = __dmul_rn(Y, s), z = __dmul_rn(Z, s);
+    double so = __dmul_rn(__dadd_rn(__dadd_rn(x, y), z), -1.0 / 6);
+    double xs = __dadd_rn(x, so), ys = __dadd_rn(y, so), zs = __dadd_rn(z, so);
+    long long xsb = fastfloor64(xs), ysb = fastfloor64(ys), zsb = fastfloor64(zs);
+    double sq = __dmul_rn((double)(xsb + ysb + zsb), 1.0 / 3);
+    double xb = __dadd_rn((double)xsb, sq), yb = __dadd_rn((double)ysb, sq), zb = __dadd_rn((double)zsb, sq);
+    double xins = __dsub_rn(xs, (double)xsb), yins = __dsub_rn(ys, (double)ysb), zins = __dsub_rn(zs, (double)zsb);
+    double in_sum = __dadd_rn(__dadd_rn(xins, yins), zins);
+    Cmp<double, false> C;
+    C.m = 0.f;
+    decide<double, false>(xins, yins, zins, in_sum, C, c.D);
+    c.dx0 = (float)__dsub_rn(x, xb);
+    c.dy0 = (float)__dsub_rn(y, yb);
+    c.dz0 = (float)__dsub_rn(z, zb);
+    c.xsb = (int)xsb; c.ysb = (int)ysb; c.zsb = (int)zsb;
+    c.xb7 = (int)((unsigned)xsb << 7);
+    c.yb7 = (int)((unsigned)ysb << 7);
+    c.zb7 = (int)((unsigned)zsb << 7);
+}
+
+// Binary32 path.  Returns false when binary64 must decide.
+__device__ __forceinline__ bool decide_f32(float xh, float xl, float yh, float yl, float zh, float zl,
+                                           float sh, float sl, Cell &c)
+{
+    float px = xh * sh, py = yh * sh, pz = zh * sh;
+    float ex = fmaf(xh, sh, -px), ey = fmaf(yh, sh, -py), ez = fmaf(zh, sh, -pz);
+    ex = fmaf(xh, sl, ex); ey = fmaf(yh, sl, ey); ez = fmaf(zh, sl, ez);
+    ex = fmaf(xl, sh, ex); ey = fmaf(yl, sh, ey); ez = fmaf(zl, sh, ez);
+    float big = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
+    float Ax = (px + MAGIC) - MAGIC, Ay = (py + MAGIC) - MAGIC, Az = (pz + MAGIC) - MAGIC;
+    float ax = (px - Ax) + ex, ay = (py - Ay) + ey, az = (pz - Az) + ez;
+    float T = (Ax + Ay) + Az;
+    float q = floorf(fmaf(T, SIXTH, 1.0f / 12.0f));
+    float r = fmaf(-6.0f, q, T);
+    float u = r + ((ax + ay) + az);
+    float bx = fmaf(-u, SIXTH, ax), by = fmaf(-u, SIXTH, ay), bz = fmaf(-u, SIXTH, az);
+    float fx = floorf(bx), fy = floorf(by), fz = floorf(bz);
+    float xins = bx - fx, yins = by - fy, zins = bz - fz;
+    float xsbf = (Ax - q) + fx, ysbf = (Ay - q) + fy, zsbf = (Az - q) + fz;
+    int xi = __float_as_int(xsbf + MAGIC), yi = __float_as_int(ysbf + MAGIC), zi = __float_as_int(zsbf + MAGIC);
+    c.xsb = xi - MAGIC_BITS; c.ysb = yi - MAGIC_BITS; c.zsb = zi - MAGIC_BITS;
+    c.xb7 = xi << 7; c.yb7 = yi << 7; c.zb7 = zi << 7;
+    float g = (r + ((fx + fy) + fz)) * THIRD;
+    c.dx0 = (ax - fx) - g; c.dy0 = (ay - fy) - g; c.dz0 = (az - fz) - g;
+    Cmp<float, true> C;
+    C.m = fminf(fminf(fminf(xins, 1.0f - xins), fminf(yins, 1.0f - yins)), fminf(zins, 1.0f - zins));
+    float in_sum = (xins + yins) + zins;
+    decide<float, true>(xins, yins, zins, in_sum, C, c.D);
+    return C.m >= TAU && big < PMAX;
+}
+
+// One lattice contribution: attn^4 * (grad . d) if attn > 0.
+__device__ __forceinline__ float contrib(uint32_t w, float dx, float dy, float dz, bool on)
+{
+    float attn = fmaf(-dx, dx, fmaf(-dy, dy, fmaf(-dz, dz, 2.0f)));
+    attn = on ? fmaxf(attn, 0.0f) : 0.0f;
+    float a2 = attn * attn;
+    float gx = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7442)) - GBIAS;
+    float gy = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7443)) - GBIAS;
+    float gz = __uint_as_float((w & 0x7Fu) | 0x4B000000u) - GBIAS;
+    float dot = fmaf(gx, dx, fmaf(gy, dy, gz * dz));
+    return (a2 * a2) * dot;
+}
+
+struct SlotTrace {
+    int32_t *p;   // 9 slots x [x, y, z, packed gradient, used]
+};
+
+// noise3d(x*s) * 103 for one vertex and octave.
+template <bool TRACE>
+__device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float yl, float zh, float zl,
+                                           float sh, float sl, double X, double Y, double Z, double s,
+                                           uint32_t lb, unsigned &nfb, int32_t *tr, int32_t *sl9)
+{
+    Cell c;
+    if (!decide_f32(xh, xl, yh, yl, zh, zl, sh, sl, c)) {
+        decide_f64(X, Y, Z, s, c);
+        ++nfb;
+    }
+    const int r = c.D.region;
+    const bool on0 = r != 2, onA = r != 1, onB = r != 0;
+    // hash prefixes of the fixed slots
+    uint32_t h0 = lk(lb, c.xb7), h1 = lk(lb, c.xb7 + 128);
+    uint32_t h00 = lk(lb, (int)h0 + c.yb7), h01 = lk(lb, (int)h0 + c.yb7 + 128);
+    uint32_t h10 = lk(lb, (int)h1 + c.yb7), h11 = lk(lb, (int)h1 + c.yb7 + 128);
+    const int z0 = c.zb7, z1 = c.zb7 + 128;
+    const float dx0 = c.dx0, dy0 = c.dy0, dz0 = c.dz0;
+    // slot 0: (0,0,0) in region 0, (1,1,1) in region 1
+    uint32_t w0 = lk(lb, r == 1 ? (int)h11 + z1 : (int)h00 + z0);
+    float k0 = r == 1 ? 1.0f + 1.0f : 0.0f;   // o + sum(o)/3 with o = (1,1,1): 1 + 1
+    float v = contrib(w0, dx0 - k0, dy0 - k0, dz0 - k0, on0);
+    // mixed corners
+    const float c1 = 1.0f + THIRD, c2 = 2.0f * THIRD, c3 = 1.0f + 2.0f * THIRD;
+    uint32_t w100 = lk(lb, (int)h10 + z0), w010 = lk(lb, (int)h01 + z0), w001 = lk(lb, (int)h00 + z1);
+    uint32_t w110 = lk(lb, (int)h11 + z0), w101 = lk(lb, (int)h10 + z1), w011 = lk(lb, (int)h01 + z1);
+    v += contrib(w100, dx0 - c1, dy0 - THIRD, dz0 - THIRD, onA);
+    v += contrib(w010, dx0 - THIRD, dy0 - c1, dz0 - THIRD, onA);
+    v += contrib(w001, dx0 - THIRD, dy0 - THIRD, dz0 - c1, onA);
+    v += contrib(w110, dx0 - c3, dy0 - c3, dz0 - c2, onB);
+    v += contrib(w101, dx0 - c3, dy0 - c2, dz0 - c3, onB);
+    v += contrib(w011, dx0 - c2, dy0 - c3, dz0 - c3, onB);
+    // extra points: d = d0 - o - sum(o)/3
+    const Decision &D = c.D;
+    float s0 = ((D.e0x + D.e0y) + D.e0z) * THIRD, s1 = ((D.e1x + D.e1y) + D.e1z) * THIRD;
+    int ox0 = __float_as_int(D.e0x + MAGIC) << 7, oy0 = __float_as_int(D.e0y + MAGIC) << 7,
+        oz0 = __float_as_int(D.e0z + MAGIC) << 7;
+    int ox1 = __float_as_int(D.e1x + MAGIC) << 7, oy1 = __float_as_int(D.e1y + MAGIC) << 7,
+        oz1 = __float_as_int(D.e1z + MAGIC) << 7;
+    uint32_t we0 = lk(lb, (int)lk(lb, (int)lk(lb, c.xb7 + ox0) + c.yb7 + oy0) + c.zb7 + oz0);
+    uint32_t we1 = lk(lb, (int)lk(lb, (int)lk(lb, c.xb7 + ox1) + c.yb7 + oy1) + c.zb7 + oz1);
+    v += contrib(we0, dx0 - (D.e0x + s0), dy0 - (D.e0y + s0), dz0 - (D.e0z + s0), true);
+    v += contrib(we1, dx0 - (D.e1x + s1), dy0 - (D.e1y + s1), dz0 - (D.e1z + s1), true);
+    if (TRACE) {
+        tr[0] = c.xsb; tr[1] = c.ysb; tr[2] = c.zsb; tr[3] = r;
+        tr[4] = c.xsb + (int)D.e0x; tr[5] = c.ysb + (int)D.e0y; tr[6] = c.zsb + (int)D.e0z;
+        tr[7] = c.xsb + (int)D.e1x; tr[8] = c.ysb + (int)D.e1y; tr[9] = c.zsb + (int)D.e1z;
+        const int o[9][3] = {{r == 1, r == 1, r == 1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0},
+                             {1, 0, 1}, {0, 1, 1}, {(int)D.e0x, (int)D.e0y, (int)D.e0z},
+                             {(int)D.e1x, (int)D.e1y, (int)D.e1z}};
+        const uint32_t w[9] = {w0, w100, w010, w001, w110, w101, w011, we0, we1};
+        const bool on[9] = {on0, onA, onA, onA, onB, onB, onB, true, true};
+        for (int k = 0; k < 9; ++k) {
+            int32_t *q = sl9 + 5 * k;
+            q[0] = c.xsb + o[k][0]; q[1] = c.ysb + o[k][1]; q[2] = c.zsb + o[k][2];
+            q[3] = (int32_t)(((w[k] >> 16) & 0xFF) | (((w[k] >> 24) & 0xFF) << 8) | ((w[k] & 0x7F) << 16));
+            q[4] = on[k] ? 1 : 0;
+        }
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint32_t lane_base(const uint32_t *T)
+{
+    return (uint32_t)__cvta_generic_to_shared(T) + ((threadIdx.x & 31u) << 2);
+}
+
+__global__ void __launch_bounds__(256) fbm_kernel(const double *__restrict__ xyz, int64_t n,
+                                                  const int32_t *__restrict__ perm,
+                                                  const int32_t *__restrict__ pgi, FbmParams P,
+                                                  double *__restrict__ out64, float *__restrict__ out32,
+                                                  int accumulate, unsigned long long *nfb_out)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    build_table(smem, perm, pgi);
+    __syncthreads();
+    const uint32_t lb = lane_base(smem);
+    unsigned nfb = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double X = xyz[3 * i], Y = xyz[3 * i + 1], Z = xyz[3 * i + 2];
+        float xh, xl, yh, yl, zh, zl;
+        split_f64(X, xh, xl);
+        split_f64(Y, yh, yl);
+        split_f64(Z, zh, zl);
+        float acc = 0.0f;
+        for (int o = 0; o < P.n_oct; ++o) {
+            float v = noise_raw<false>(xh, xl, yh, yl, zh, zl, P.s_hi[o], P.s_lo[o], X, Y, Z, P.s[o], lb,
+                                       nfb, nullptr, nullptr);
+            // (noise + 1) * 0.5 * strength * radius, noise = v / 103
+            acc += fmaf(v, P.amp[o] * (1.0f / 103.0f), P.amp[o]);
+        }
+        if (out64) out64[i] = accumulate ? out64[i] + (double)acc : (double)acc;
+        if (out32) out32[i] = accumulate ? out32[i] + acc : acc;
+    }
+    if (nfb_out) {
+        unsigned tot = __reduce_add_sync(0xFFFFFFFFu, nfb);
+        if ((threadIdx.x & 31) == 0 && tot) atomicAdd(nfb_out, (unsigned long long)tot);
+    }
+}
+
+__global__ void __launch_bounds__(256) trace_kernel(const double *__restrict__ xyz, int64_t n,
+                                                    const int32_t *__restrict__ perm,
+                                                    const int32_t *__restrict__ pgi, double s,
+                                                    float *__restrict__ value, int32_t *__restrict__ trace,
+                                                    int32_t *__restrict__ slots,
+                                                    unsigned long long *nfb_out)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    build_table(smem, perm, pgi);
+    __syncthreads();
+    const uint32_t lb = lane_base(smem);
+    float sh, sl;
+    split_f64(s, sh, sl);
+    unsigned nfb = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double X = xyz[3 * i], Y = xyz[3 * i + 1], Z = xyz[3 * i + 2];
+        float xh, xl, yh, yl, zh, zl;
+        split_f64(X, xh, xl);
+        split_f64(Y, yh, yl);
+        split_f64(Z, zh, zl);
+        int32_t tr[10], s9[45];
+        float v = noise_raw<true>(xh, xl, yh, yl, zh, zl, sh, sl, X, Y, Z, s, lb, nfb, tr, s9);
+        value[i] = v * (1.0f / 103.0f);
+        if (trace)
+            for (int k = 0; k < 10; ++k) trace[10 * i + k] = tr[k];
+        if (slots)
+            for (int k = 0; k < 45; ++k) slots[45 * i + k] = s9[k];
+    }
+    if (nfb_out) {
+        unsigned tot = __reduce_add_sync(0xFFFFFFFFu, nfb);
+        if ((threadIdx.x & 31) == 0 && tot) atomicAdd(nfb_out, (unsigned long long)tot);
+    }
+}
+
+int grid_for(int64_t n, int block, const void *kernel, int smem)
+{
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    if (per_sm < 1) per_sm = 1;
+    int64_t need = (n + block - 1) / block;
+    int64_t g = (int64_t)nx::sm_count() * per_sm;
+    if (need < g) g = need;
+    return (int)(g < 1 ? 1 : g);
+}
+
+bool smem_configured = false;
+
+int configure_smem()
+{
+    if (smem_configured) return NX_OK;
+    NX_CHECK_CUDA(cudaFuncSetAttribute(fbm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
+    NX_CHECK_CUDA(cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
+    smem_configured = true;
+    return NX_OK;
+}
+
+}  // namespace
+
+namespace nx {
+void note_launch(int k);
+}
+
+NX_EXPORT int nx_fbm(const double *xyz_dev, int64_t n, const int32_t *perm_dev, const int32_t *pgi_dev,
+                     int n_octaves, const double *scale, const double *strength, double radius,
+                     double *elev_f64_dev, float *elev_f32_dev, int accumulate,
+                     unsigned long long *n_fallback_dev, void *stream)
+{
+    if (n < 0) return nx::fail(NX_EINVAL, "nx_fbm: n < 0");
+    if (n_octaves < 0 || n_octaves > NX_MAX_OCTAVES)
+        return nx::fail(NX_EINVAL, "nx_fbm: n_octaves must be in [0, %d]", NX_MAX_OCTAVES);
+    if (n == 0) return NX_OK;
+    if (!xyz_dev || !perm_dev || !pgi_dev || (n_octaves > 0 && (!scale || !strength)))
+        return nx::fail(NX_EINVAL, "nx_fbm: null pointer");
+    if (!elev_f64_dev && !elev_f32_dev) return nx::fail(NX_EINVAL, "nx_fbm: no output");
+    FbmParams P;
+    P.n_oct = n_octaves;
+    for (int o = 0; o < n_octaves; ++o) {
+        double s = scale[o];
+        float hi = (float)s;
+        float lo = (float)(s - (double)hi);
+        P.s_hi[o] = hi;
+        P.s_lo[o] = lo;
+        P.s[o] = s;
+        P.amp[o] = (float)(0.5 * strength[o] * radius);
+    }
+    int rc = configure_smem();
+    if (rc) return rc;
+    int grid = grid_for(n, 256, (const void *)fbm_kernel, TABLE_BYTES);
+    fbm_kernel<<<grid, 256, TABLE_BYTES, (cudaStream_t)stream>>>(xyz_dev, n, perm_dev, pgi_dev, P, elev_f64_dev,
+                                                                 elev_f32_dev, accumulate, n_fallback_dev);
+    NX_CHECK_LAUNCH("fbm_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_sample_octaves(const double *xyz_dev, int64_t n, const int32_t *perm_dev,
+                                const int32_t *pgi_dev, int n_octaves, double n_init_roughness,
+                                double n_init_strength, double n_roughness, double n_persistence,
+                                double world_radius, double *elev_f64_dev, float *elev_f32_dev,
+                                int accumulate, void *stream)
+{
+    if (n_octaves < 0 || n_octaves > NX_MAX_OCTAVES)
+        return nx::fail(NX_EINVAL, "nx_sample_octaves: n_octaves must be in [0, %d]", NX_MAX_OCTAVES);
+    double scale[NX_MAX_OCTAVES], strength[NX_MAX_OCTAVES];
+    // terrain.py:35-46: the per-octave arguments, in binary64 as the reference
+    double f = n_init_roughness, a = n_init_strength;
+    for (int o = 0; o < n_octaves; ++o) {
+        scale[o] = f / world_radius;
+        strength[o] = a / world_radius;
+        f *= n_roughness;
+        a *= n_persistence;
+    }
+    return nx_fbm(xyz_dev, n, perm_dev, pgi_dev, n_octaves, scale, strength, world_radius, elev_f64_dev,
+                  elev_f32_dev, accumulate, nullptr, stream);
+}
+
+NX_EXPORT int nx_noise3d_trace(const double *xyz_dev, int64_t n, const int32_t *perm_dev,
+                               const int32_t *pgi_dev, double scale, float *value_dev, int32_t *trace_dev,
+                               int32_t *slots_dev, unsigned long long *n_fallback_dev, void *stream)
+{
+    if (n < 0) return nx::fail(NX_EINVAL, "nx_noise3d_trace: n < 0");
+    if (n == 0) return NX_OK;
+    if (!xyz_dev || !perm_dev || !pgi_dev || !value_dev)
+        return nx::fail(NX_EINVAL, "nx_noise3d_trace: null pointer");
+    int rc = configure_smem();
+    if (rc) return rc;
+    int grid = grid_for(n, 256, (const void *)trace_kernel, TABLE_BYTES);
+    trace_kernel<<<grid, 256, TABLE_BYTES, (cudaStream_t)stream>>>(xyz_dev, n, perm_dev, pgi_dev, scale,
+                                                                   value_dev, trace_dev, slots_dev,
+                                                                   n_fallback_dev);
+    NX_CHECK_LAUNCH("trace_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}

@@ -17,7 +17,7 @@ def _norm_rows(p):
     return np.stack([x / r, y / r, z / r], axis=1)
 
 
-def icosphere(k):
+def icosphere(k, with_tris=True):
     k = ico.check_divisions(k)
     C = ico.corners()
     E = ico.edges()
@@ -48,6 +48,8 @@ def icosphere(k):
         A, B, Cc = C[a], C[b], C[c]
         p = (w0[:, None] * A[None, :] + ii[:, None] * B[None, :]) + jj[:, None] * Cc[None, :]
         pts[base_int + f * npf: base_int + (f + 1) * npf] = _norm_rows(p)
+    if not with_tris:
+        return pts, None
 
     def vid(f, i, j):
         a, b, c = ico.FACES[f]
