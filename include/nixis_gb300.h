@@ -20,6 +20,7 @@
 #ifndef NIXIS_GB300_H
 #define NIXIS_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -93,6 +94,139 @@ int nx_sample_octaves(const double *xyz_dev, int64_t n, const int32_t *perm_dev,
 int nx_noise3d_trace(const double *xyz_dev, int64_t n, const int32_t *perm_dev,
                      const int32_t *pgi_dev, double scale, float *value_dev, int32_t *trace_dev,
                      int32_t *slots_dev, unsigned long long *n_fallback_dev, void *stream);
+
+
+/* ------------------------------------------------------------------ */
+/* Mesh: icosphere, adjacency, edge lengths                            */
+/* ------------------------------------------------------------------ */
+
+/* Upload the icosahedron tables (12 corners as float64[36], faces int32[60],
+ * per face side edge id and direction int32[120], edges int32[60]) for the
+ * current device; nixis_gb300/icosphere.py defines them.  Once per device. */
+int nx_icosphere_tables(const double *corners, const int32_t *faces, const int32_t *face_edges,
+                        const int32_t *edges);
+
+/* Icosphere with k divisions (replaces meshzoo.icosa_sphere at util.py:43):
+ * xyz_dev float64[(10k^2+2)*3] and/or tris_dev int32[20k^2*3] (either may be
+ * NULL).  Corners are vertices 0-11; layout in nixis_gb300/icosphere.py. */
+int nx_icosphere(int k, double *xyz_dev, int32_t *tris_dev, void *stream);
+
+/* Workspace bytes for nx_build_adjacency. */
+size_t nx_adjacency_workspace_size(int64_t nv);
+
+/* util.build_adjacency (util.py:591-613) for nv = (nt+4)/2 vertices:
+ * adj_dev int32[nv*6], row order = triangle order, -1 padding.  err_dev
+ * (device int, caller zeroes it) gets bit 0 for an out-of-range vertex id,
+ * bit 1 for a vertex with more than 6 neighbours. */
+int nx_build_adjacency(const int32_t *tris_dev, int64_t nt, int64_t nv, int32_t *adj_dev, void *workspace,
+                       size_t ws_bytes, int *err_dev, void *stream);
+
+/* util.sort_adjacency (util.py:638-662), out of place: rows of adj_in are
+ * walked into rings (vertices 0-11 have 5 neighbours) and written to adj_out. */
+int nx_sort_adjacency(const int32_t *adj_in_dev, int32_t *adj_out_dev, int64_t nv, void *stream);
+
+/* Per-slot neighbour distance |v_i - v_j| in binary64 (erosion.calc_distance,
+ * erosion.py:38-40) rounded to binary32: edge_dev float[nv*6], 0 for -1 slots.
+ * err_dev (optional) gets bit 0 for an out-of-range neighbour id. */
+int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, float *edge_dev, int *err_dev,
+                    void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Erosion (variant 3)                                                 */
+/* ------------------------------------------------------------------ */
+
+/* One planet's range in a packed batch.  vbeg must be a multiple of 256;
+ * planets are packed in order of non-increasing `iters`.  `rain` is added
+ * to every water value before each iteration (erode_terrain3 adds 0.3/320,
+ * erosion.py:182-183; 0 gives bare erosion_iteration3 steps).  Neighbour
+ * ids in a batch are global (packed) indices. */
+typedef struct nx_erosion_planet {
+    int64_t vbeg;
+    int64_t vend;
+    int32_t iters;
+    float rain;
+} nx_erosion_planet;
+
+/* Workspace bytes for erosion over n_padded_total packed vertices and
+ * nplanets planets (control words + per-block partial sums). */
+size_t nx_erosion_workspace_size(int64_t n_padded_total, int nplanets);
+
+/* Zero the per-planet control words (scale exponent 0) of a workspace. */
+int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream);
+
+/* Load binary64 fields (the reference's r_buff/heights, wat, sed; w/s may
+ * be NULL for zeros) into the binary32 state: hw_dev float[2n] interleaved
+ * (h, w), s_dev float[n], choosing a power-of-two scale so values fit. */
+int nx_erosion_load(const double *h64_dev, const double *w64_dev, const double *s64_dev, int64_t n, float *hw_dev,
+                    float *s_dev, void *workspace, size_t ws_bytes, void *stream);
+
+/* `iters` Jacobi iterations of erosion.erosion_iteration3 (erosion.py:
+ * 197-279) on one planet, result left in (hw_dev, s_dev).  hw_tmp/s_tmp:
+ * second buffer of the same sizes.  planet_dev: device scratch for one
+ * nx_erosion_planet.  mass_dev (optional): float64[iters*3] per-iteration
+ * (sum h, sum w, sum s), compensated, scaled back to true units.  flow_dev
+ * (optional): uint16[n], per slot k bits 2k..2k+1 = 1 if the neighbour is
+ * higher, 2 if lower (the reference's slope > 0 / < 0 choice), of the last
+ * iteration. */
+int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *hw_dev, float *s_dev,
+                     float *hw_tmp_dev, float *s_tmp_dev, int iters, float rain, const nx_erosion_planet *planet_dev,
+                     double *mass_dev, uint16_t *flow_dev, void *workspace, size_t ws_bytes, void *stream);
+
+/* Batched erosion: every planet runs its own iteration count in one
+ * launch per iteration over the planets still running.  Each planet's
+ * state starts in buffer (iters & 1) -- 0: (hw_dev, s_dev), 1: (hw_tmp,
+ * s_tmp) -- and ends in buffer 0.  mass_dev (optional): float64
+ * [max_iters][nplanets][3].  Call nx_erosion_ctl_init first. */
+int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
+                     const int32_t *nbr_dev, const float *edge_dev, float *hw_dev, float *s_dev, float *hw_tmp_dev,
+                     float *s_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes, void *stream);
+
+/* Write one planet's binary32 state back as binary64 true values (undoing
+ * its power-of-two scale, kept in the workspace's first control block).
+ * w64_dev / s64_dev may be NULL. */
+int nx_erosion_store(const float *hw_dev, const float *s_dev, int64_t n, const void *workspace, double *h64_dev,
+                     double *w64_dev, double *s64_dev, void *stream);
+
+/* Layout of a workspace's per-planet control block (32 bytes, planet p at
+ * byte 32*p): after a run, K[0] is the planet's scale exponent (stored
+ * value = true value * 2^-K[0]) and err != 0 flags a neighbour id outside
+ * the planet's range. */
+typedef struct nx_erosion_ctl {
+    uint32_t maxbits[3];
+    int32_t K[2];
+    uint32_t done;
+    int32_t err;
+    int32_t pad;
+} nx_erosion_ctl;
+
+/* erosion.find_lowest (erosion.py:398-406) for every vertex: pos_dev gets
+ * the position, among the neighbours that are not -1, of the first lowest
+ * one if it is strictly lower than the vertex, else -1; vid_dev (optional)
+ * that neighbour's id or -1. */
+int nx_steepest_descent(const int32_t *nbr_dev, const double *h_dev, int64_t n, int32_t *pos_dev, int32_t *vid_dev,
+                        void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Insolation                                                          */
+/* ------------------------------------------------------------------ */
+
+/* Host: the (cos, sin) table for a schedule of sun positions -- rotations
+ * in degrees (about z) and tilts in degrees (about y), the arguments of
+ * climate.sample_insolation (climate.py:415-444).  table_host must hold
+ * 2*(n_rot + n_tilt) floats.  If the rotations come in pairs h and
+ * h + n_rot/2 that differ by exactly 180 degrees, only the first half is
+ * tabulated (*pairs = 1).  *n_rot_entries gets the number of rotation
+ * entries written; tilt entries follow them. */
+int nx_insolation_plan(const double *rot_deg, int n_rot, const double *tilt_deg, int n_tilt, float *table_host,
+                       int *n_rot_entries, int *pairs);
+
+/* Sum over every (tilt, rotation) pair of sample_insolation's term
+ * max(cos|lat|,0)*max(cos lon,0) (climate.py:442, util.py:59-75):
+ * out_dev[v] = sum (accumulate=0) or out_dev[v] += sum.  table_dev: the
+ * plan's table on the device.  Binary32 terms; per-tilt partial sums with
+ * a compensated total. */
+int nx_insolation(const double *xyz_dev, int64_t n, double radius, const float *table_dev, int n_rot_entries,
+                  int pairs, int n_tilt, float *out_dev, int accumulate, void *stream);
 
 #ifdef __cplusplus
 }

@@ -24,7 +24,29 @@ SIGNATURES = {
     "nx_fbm": (_i32, [_p, _i64, _p, _p, _i32, _p, _p, _d, _p, _p, _i32, _p, _p]),
     "nx_sample_octaves": (_i32, [_p, _i64, _p, _p, _i32, _d, _d, _d, _d, _d, _p, _p, _i32, _p]),
     "nx_noise3d_trace": (_i32, [_p, _i64, _p, _p, _d, _p, _p, _p, _p, _p]),
+    "nx_icosphere_tables": (_i32, [_p, _p, _p, _p]),
+    "nx_icosphere": (_i32, [_i32, _p, _p, _p]),
+    "nx_adjacency_workspace_size": (ctypes.c_size_t, [_i64]),
+    "nx_build_adjacency": (_i32, [_p, _i64, _i64, _p, _p, ctypes.c_size_t, _p, _p]),
+    "nx_sort_adjacency": (_i32, [_p, _p, _i64, _p]),
+    "nx_edge_lengths": (_i32, [_p, _p, _i64, _p, _p, _p]),
+    "nx_erosion_workspace_size": (ctypes.c_size_t, [_i64, _i32]),
+    "nx_erosion_ctl_init": (_i32, [_p, ctypes.c_size_t, _i32, _p]),
+    "nx_erosion_load": (_i32, [_p, _p, _p, _i64, _p, _p, _p, ctypes.c_size_t, _p]),
+    "nx_erosion_steps": (_i32, [_p, _p, _i64, _p, _p, _p, _p, _i32, ctypes.c_float, _p, _p, _p, _p,
+                                ctypes.c_size_t, _p]),
+    "nx_erosion_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "nx_erosion_store": (_i32, [_p, _p, _i64, _p, _p, _p, _p, _p]),
+    "nx_steepest_descent": (_i32, [_p, _p, _i64, _p, _p, _p]),
+    "nx_insolation_plan": (_i32, [_p, _i32, _p, _i32, _p, _p, _p]),
+    "nx_insolation": (_i32, [_p, _i64, _d, _p, _i32, _i32, _i32, _p, _i32, _p]),
 }
+
+
+class ErosionPlanet(ctypes.Structure):
+    """nx_erosion_planet (include/nixis_gb300.h)."""
+    _fields_ = [("vbeg", ctypes.c_int64), ("vend", ctypes.c_int64), ("iters", ctypes.c_int32),
+                ("rain", ctypes.c_float)]
 
 _lock = threading.Lock()
 _LIB = None

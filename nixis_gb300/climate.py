@@ -1,0 +1,117 @@
+"""Drop-in for the insolation part of the reference's climate module
+(climate.py:167-201, 415-500) and the fused annual accumulation.
+
+``sample_insolation`` keeps the reference's in-place float32 ``arr +=``;
+``insolation_sum`` evaluates any (tilt x rotation) schedule in one kernel;
+``annual_insolation`` is the year of days x hourly sun positions.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _dev
+from ._lib import call
+
+SOLAR_CONSTANT = 1361.0  # W/m^2
+
+
+def day2deg(year_length, day):
+    """climate.day2deg (climate.py:167-171)."""
+    return (day / year_length) * 360.0
+
+
+def calculate_seasonal_tilt(axial_tilt, degrees):
+    """climate.calculate_seasonal_tilt (climate.py:192-201)."""
+    return math.sin(degrees * math.pi / 180) * axial_tilt
+
+
+def _plan(rot_deg, tilt_deg):
+    rot = np.ascontiguousarray(rot_deg, np.float64)
+    tilt = np.ascontiguousarray(tilt_deg, np.float64)
+    tab = np.zeros(2 * (len(rot) + len(tilt)), np.float32)
+    nre = ctypes.c_int(0)
+    pairs = ctypes.c_int(0)
+    vp = ctypes.c_void_p
+    call("nx_insolation_plan", rot.ctypes.data_as(vp), len(rot), tilt.ctypes.data_as(vp), len(tilt),
+         tab.ctypes.data_as(vp), ctypes.byref(nre), ctypes.byref(pairs))
+    used = 2 * (nre.value + len(tilt))
+    return tab[:used], nre.value, pairs.value
+
+
+def insolation_sum(verts, radius, rotations, tilts, out=None, accumulate=False, stream=None):
+    """Sum over every (tilt, rotation) of sample_insolation's term.
+
+    verts float64 (N,3) (CUDA tensor or numpy); rotations/tilts in degrees.
+    Returns a float32 CUDA tensor (N,) (or adds into `out`)."""
+    xyz = _dev.to_device(verts, np.float64, name="verts")
+    _dev.check_vertices(xyz)
+    n = xyz.shape[0]
+    tab, nre, pairs = _plan(rotations, tilts)
+    tdev = _dev.to_device(tab, np.float32, name="table")
+    if out is None:
+        out = torch.empty(n, dtype=torch.float32, device="cuda")
+        accumulate = False
+    if out.dtype != torch.float32 or out.shape != (n,) or not out.is_cuda:
+        raise ValueError("out must be a float32 CUDA tensor of shape (N,)")
+    call("nx_insolation", _dev.ptr(xyz), n, float(radius), _dev.ptr(tdev), nre, pairs, len(tilts), _dev.ptr(out),
+         1 if accumulate else 0, _dev.stream_handle(stream))
+    return out
+
+
+def sample_insolation(arr, verts, radius, rotation, tilt):
+    """climate.sample_insolation (climate.py:415-444): arr += the insolation
+    term for one sun position, in place (numpy float32 like the reference,
+    or a float32 CUDA tensor)."""
+    if _dev.is_host(arr):
+        if arr.dtype != np.float32 or not arr.flags.c_contiguous:
+            raise ValueError("arr must be a C-contiguous float32 array")
+        dev = _dev.to_device(arr, np.float32)
+        insolation_sum(verts, radius, [float(rotation)], [float(tilt)], out=dev, accumulate=True)
+        arr[...] = dev.cpu().numpy()
+        return
+    insolation_sum(verts, radius, [float(rotation)], [float(tilt)], out=arr, accumulate=True)
+
+
+def brute_daily_insolation(verts, altitudes, radius, tilt, snapshot=False):
+    """climate.brute_daily_insolation (climate.py:450-489): 360 rotations of
+    one degree from -180, one tilt; a new float32 array."""
+    if snapshot:
+        raise NotImplementedError("insolation snapshots (PNG export) are not provided by nixis_gb300")
+    host = _dev.is_host(verts)
+    rot = [-180.0 + i * 1.0 for i in range(360)]
+    out = insolation_sum(verts, radius, rot, [float(tilt)])
+    return out.cpu().numpy() if host else out
+
+
+def calc_instant_insolation(verts, altitudes, radius, rotation, tilt):
+    """climate.calc_instant_insolation (climate.py:492-500)."""
+    host = _dev.is_host(verts)
+    out = insolation_sum(verts, radius, [float(rotation)], [float(tilt)])
+    return out.cpu().numpy() if host else out
+
+
+def annual_schedule(axial_tilt=23.44, year_length=365, days=365, hours=24):
+    """Sun positions of a circular orbit: hourly rotations -180 + (360/hours) h
+    and daily tilts calculate_seasonal_tilt(axial_tilt, day2deg(year_length, d))."""
+    rot_amt = 360.0 / hours
+    rot = []
+    r = -180.0
+    for _ in range(hours):
+        rot.append(r)
+        r += rot_amt
+    tilts = [calculate_seasonal_tilt(axial_tilt, day2deg(year_length, d)) for d in range(days)]
+    return rot, tilts
+
+
+def annual_insolation(verts, radius, axial_tilt=23.44, year_length=365, days=365, hours=24, mean_wm2=False,
+                      out=None, stream=None):
+    """Sum of sample_insolation terms over `days` x `hours` sun positions
+    (float32 CUDA tensor).  With mean_wm2, converted to the mean top-of-
+    atmosphere flux: SOLAR_CONSTANT * sum / (days * hours)."""
+    rot, tilts = annual_schedule(axial_tilt, year_length, days, hours)
+    s = insolation_sum(verts, radius, rot, tilts, out=out, stream=stream)
+    if mean_wm2:
+        s.mul_(SOLAR_CONSTANT / (days * hours))
+    return s

@@ -1,0 +1,507 @@
+// nx_erosion.cu -- erosion variant 3 (erosion.py:172-279) for sm_103a.
+//
+// State per vertex: (h, w) as float2 and s as float, binary32, double
+// buffered (the reference reads old arrays and writes copies, erosion.py:
+// 199-201, 274-277).  Neighbour slots are the reference's (n,6) int32 table;
+// edge lengths are precomputed per slot in binary64 and rounded.
+//
+// Overflow: under the reference's update, water and sediment grow about 2x
+// per iteration, past binary32's range after ~140 iterations.  The update is
+// positively homogeneous (only signs of height differences and the
+// capacity test s > cap*w are decided, both scale invariant), and scaling by
+// a power of two commutes with binary32 rounding, so each planet carries an
+// exponent K: stored values are true values * 2^-K.  When the previous
+// iteration's max |value| exceeds 2^96, this iteration multiplies what it
+// reads by 2^-64 and K grows by 64.  The trajectory is then exactly the one
+// an overflow-free binary32 machine would compute.
+//
+// Batched: planets are packed back to back (each range starting at a
+// multiple of 256) and sorted by iteration count, descending, so the planets
+// still running at iteration t are a prefix; one launch per iteration covers
+// that prefix.  Each planet alternates its two buffers so that its last
+// iteration writes buffer 0.
+#include "nx_common.cuh"
+
+namespace nx {
+void note_launch(int k);
+}
+
+namespace {
+
+constexpr int BLOCK = 256;
+constexpr float RESCALE_ABOVE = 7.9228163e28f;   // 2^96
+constexpr int RESCALE_SHIFT = 64;
+
+// erosion.py:205-207, rounded to binary32
+__device__ __constant__ float c_sol = (float)(0.01 / 320);
+__device__ __constant__ float c_evap = (float)(0.1 / 320);
+__device__ __constant__ float c_cap = (float)(0.2 / 320);
+
+}  // namespace
+
+// nx_erosion_ctl (header): maxbits = max |h|,|w|,|s| of an iteration's
+// output as float bits in 3 rotating slots; K = scale exponent, ping-pong by
+// iteration parity; done = blocks finished in the current iteration (mass
+// sums); err = 1 for a neighbour id out of range.
+static_assert(sizeof(nx_erosion_ctl) == 32, "control block layout");
+
+namespace {
+
+struct StepArgs {
+    const nx_erosion_planet *planets;
+    int np;
+    int t;
+    const int32_t *nbr;
+    const float *el;
+    float2 *hw0;
+    float *s0;
+    float2 *hw1;
+    float *s1;
+    nx_erosion_ctl *ctl;
+    double *partials;      // [gridDim.x][3] (mass sums only)
+    double *mass;          // [iteration][planet][3] or null
+    int mass_np;           // planets per mass row
+    uint16_t *flow;        // optional: per vertex 2 bits per slot (1: neighbour higher, 2: lower)
+};
+
+__device__ __forceinline__ int find_planet(const nx_erosion_planet *P, int np, int64_t v)
+{
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (P[mid].vbeg <= v) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ float warp_max(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
+{
+    __shared__ int s_p;
+    __shared__ float s_lam, s_rain;
+    __shared__ int s_K;
+    __shared__ float s_wmax[BLOCK / 32];
+    __shared__ double s_wsum[BLOCK / 32][3];
+    __shared__ bool s_last;
+
+    const int64_t vblk = (int64_t)blockIdx.x * BLOCK;
+    if (threadIdx.x == 0) {
+        int p = find_planet(a.planets, a.np, vblk);
+        s_p = p;
+        nx_erosion_ctl *c = a.ctl + p;
+        float m = __uint_as_float(((volatile unsigned *)c->maxbits)[a.t % 3]);
+        int shift = m > RESCALE_ABOVE ? RESCALE_SHIFT : 0;
+        int K = ((volatile int *)c->K)[a.t & 1] + shift;
+        s_K = K;
+        s_lam = shift ? __int_as_float((127 - shift) << 23) : 1.0f;
+        s_rain = scalbnf(a.planets[p].rain, -K);
+        if (vblk == a.planets[p].vbeg) {
+            c->K[(a.t + 1) & 1] = K;
+            c->maxbits[(a.t + 2) % 3] = 0u;
+        }
+    }
+    __syncthreads();
+    const int p = s_p;
+    const nx_erosion_planet P = a.planets[p];
+    const float lam = s_lam, rain = s_rain;
+    // buffers: read B[(iters - t) & 1], write the other; B[0] = (hw0, s0)
+    const bool par = ((P.iters - a.t) & 1) != 0;
+    const float2 *__restrict__ ihw = par ? a.hw1 : a.hw0;
+    const float *__restrict__ is = par ? a.s1 : a.s0;
+    float2 *__restrict__ ohw = par ? a.hw0 : a.hw1;
+    float *__restrict__ os = par ? a.s0 : a.s1;
+
+    const int64_t i = vblk + threadIdx.x;
+    float vmax = 0.0f;
+    double sh = 0.0, sw = 0.0, ss = 0.0;
+    if (i < P.vend) {
+        const float sol = c_sol, evap = c_evap, cap = c_cap;
+        float2 hwi = ihw[i];
+        const float hi = __fmul_rn(hwi.x, lam);
+        const float wi = __fadd_rn(__fmul_rn(hwi.y, lam), rain);
+        const float si = __fmul_rn(is[i], lam);
+        float sed = si, wat = wi;
+        const int2 *nb2 = reinterpret_cast<const int2 *>(a.nbr + 6 * i);
+        const float2 *el2 = reinterpret_cast<const float2 *>(a.el + 6 * i);
+        int2 n01 = nb2[0], n23 = nb2[1], n45 = nb2[2];
+        float2 d01 = el2[0], d23 = el2[1], d45 = el2[2];
+        const int nbr[6] = {n01.x, n01.y, n23.x, n23.y, n45.x, n45.y};
+        const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
+        unsigned flow = 0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            int j = nbr[k];
+            if (j < 0) continue;
+            if ((int64_t)j < P.vbeg || (int64_t)j >= P.vend) {
+                a.ctl[p].err = 1;
+                continue;
+            }
+            float2 hwj = ihw[j];
+            float hj = __fmul_rn(hwj.x, lam);
+            float wj = __fadd_rn(__fmul_rn(hwj.y, lam), rain);
+            float diff = __fsub_rn(hj, hi);     // sign of the slope (erosion.py:230)
+            if (diff > 0.0f) {
+                sed = __fadd_rn(sed, __fmul_rn(sol, wj));
+                wat = __fadd_rn(wat, __fmul_rn(wj, dd[k]));
+                flow |= 1u << (2 * k);
+            } else if (diff < 0.0f) {
+                sed = __fsub_rn(sed, __fmul_rn(sol, wj));
+                wat = __fsub_rn(wat, __fmul_rn(wj, dd[k]));
+                flow |= 2u << (2 * k);
+            }
+        }
+        // erosion.py:262-267
+        float hn = __fsub_rn(hi, sed);
+        float sn = __fadd_rn(si, sed);
+        float wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, evap)));
+        float cw = __fmul_rn(cap, wn);
+        if (sn > cw) {
+            float ex = __fsub_rn(sn, cw);
+            hn = __fadd_rn(hn, ex);
+            sn = __fsub_rn(sn, ex);
+        }
+        ohw[i] = make_float2(hn, wn);
+        os[i] = sn;
+        if (a.flow) a.flow[i] = (uint16_t)flow;
+        vmax = fmaxf(fabsf(hn), fmaxf(fabsf(wn), fabsf(sn)));
+        if (a.mass) { sh = (double)hn; sw = (double)wn; ss = (double)sn; }
+    }
+    // block max -> planet max for the next iteration's rescale decision
+    vmax = warp_max(vmax);
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) s_wmax[wid] = vmax;
+    if (a.mass) {
+        sh = warp_sum(sh); sw = warp_sum(sw); ss = warp_sum(ss);
+        if (lane == 0) { s_wsum[wid][0] = sh; s_wsum[wid][1] = sw; s_wsum[wid][2] = ss; }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.0f;
+        for (int w = 0; w < BLOCK / 32; ++w) m = fmaxf(m, s_wmax[w]);
+        // NaN never wins fmaxf; an infinite value still triggers a rescale
+        atomicMax(&a.ctl[p].maxbits[(a.t + 1) % 3], __float_as_uint(m));
+        s_last = false;
+        if (a.mass) {
+            double t0 = 0, t1 = 0, t2 = 0;
+            for (int w = 0; w < BLOCK / 32; ++w) { t0 += s_wsum[w][0]; t1 += s_wsum[w][1]; t2 += s_wsum[w][2]; }
+            double *pp = a.partials + 3 * (int64_t)blockIdx.x;
+            pp[0] = t0; pp[1] = t1; pp[2] = t2;
+            __threadfence();
+            int64_t nblk = (P.vend - P.vbeg + BLOCK - 1) / BLOCK;
+            unsigned prev = atomicAdd(&a.ctl[p].done, 1u);
+            s_last = (int64_t)prev + 1 == nblk;
+        }
+    }
+    __syncthreads();
+    if (a.mass && s_last) {
+        // last block of this planet: compensated (Neumaier) sum of the
+        // planet's block partials in a fixed order, scaled by 2^K
+        __threadfence();
+        const int64_t b0 = P.vbeg / BLOCK, nblk = (P.vend - P.vbeg + BLOCK - 1) / BLOCK;
+        double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+        for (int64_t b = threadIdx.x; b < nblk; b += BLOCK) {
+            const volatile double *pp = a.partials + 3 * (b0 + b);
+            for (int c = 0; c < 3; ++c) {
+                double x = pp[c], tt = acc[c] + x;
+                cmp[c] += fabs(acc[c]) >= fabs(x) ? (acc[c] - tt) + x : (x - tt) + acc[c];
+                acc[c] = tt;
+            }
+        }
+        for (int c = 0; c < 3; ++c) {
+            double v = warp_sum(acc[c] + cmp[c]);
+            if (lane == 0) s_wsum[wid][c] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double out[3] = {0, 0, 0};
+            for (int c = 0; c < 3; ++c) {
+                double s = 0, e = 0;
+                for (int w = 0; w < BLOCK / 32; ++w) {
+                    double x = s_wsum[w][c], tt = s + x;
+                    e += fabs(s) >= fabs(x) ? (s - tt) + x : (x - tt) + s;
+                    s = tt;
+                }
+                out[c] = ldexp(s + e, s_K);
+            }
+            double *m = a.mass + 3 * ((int64_t)a.t * a.mass_np + p);
+            m[0] = out[0]; m[1] = out[1]; m[2] = out[2];
+            a.ctl[p].done = 0u;
+        }
+    }
+}
+
+// After a run: move each planet's final scale exponent and max into slot 0
+// so the state is self-describing (K[0]) and a later run starts at t = 0.
+__global__ void erosion_rebase_kernel(const nx_erosion_planet *__restrict__ P, int np, nx_erosion_ctl *__restrict__ ctl)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int it = P[p].iters;
+    if (it <= 0) return;
+    nx_erosion_ctl &c = ctl[p];
+    unsigned m = c.maxbits[it % 3];
+    int K = c.K[it & 1];
+    c.maxbits[0] = m;
+    c.maxbits[1] = 0u;
+    c.maxbits[2] = 0u;
+    c.K[0] = K;
+    c.K[1] = K;
+}
+
+// binary64 (h, w, s) -> scaled binary32 state in buffer B[iters & 1]; sets K
+// so the largest magnitude lands near 2^64 or below.
+__global__ void erosion_maxabs64_kernel(const double *__restrict__ h, const double *__restrict__ w,
+                                        const double *__restrict__ s, int64_t n, unsigned long long *__restrict__ mbits)
+{
+    double m = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a = fabs(h[i]);
+        if (w) a = fmax(a, fabs(w[i]));
+        if (s) a = fmax(a, fabs(s[i]));
+        m = fmax(m, a);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mbits, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void erosion_load64_kernel(const double *__restrict__ h, const double *__restrict__ w,
+                                      const double *__restrict__ s, int64_t n, const unsigned long long *__restrict__ mbits,
+                                      float2 *__restrict__ hw, float *__restrict__ so, nx_erosion_ctl *__restrict__ ctl)
+{
+    double m = __longlong_as_double((long long)*mbits);
+    int K = 0;
+    if (m > 0x1p64) K = ilogb(m) - 64;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float hv = (float)ldexp(h[i], -K);
+        float wv = w ? (float)ldexp(w[i], -K) : 0.0f;
+        float sv = s ? (float)ldexp(s[i], -K) : 0.0f;
+        hw[i] = make_float2(hv, wv);
+        so[i] = sv;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        float mf = (float)ldexp(m, -K);
+        ctl->maxbits[0] = __float_as_uint(mf);
+        ctl->maxbits[1] = 0u;
+        ctl->maxbits[2] = 0u;
+        ctl->K[0] = K;
+        ctl->K[1] = K;
+        ctl->done = 0u;
+        ctl->err = 0;
+    }
+}
+
+__global__ void erosion_store64_kernel(const float2 *__restrict__ hw, const float *__restrict__ s, int64_t n,
+                                       const nx_erosion_ctl *__restrict__ ctl, double *__restrict__ h,
+                                       double *__restrict__ w, double *__restrict__ so)
+{
+    const int K = ctl->K[0];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float2 v = hw[i];
+        h[i] = ldexp((double)v.x, K);
+        if (w) w[i] = ldexp((double)v.y, K);
+        if (so) so[i] = ldexp((double)s[i], K);
+    }
+}
+
+// find_lowest (erosion.py:398-406, util.py:580-587): position, within the
+// neighbours that are not -1, of the first lowest one if it is strictly
+// lower than the vertex, else -1; `vid` gets that neighbour's id (or -1).
+__global__ void steepest_kernel(const int32_t *__restrict__ nbr, const double *__restrict__ h, int64_t n,
+                                int32_t *__restrict__ pos, int32_t *__restrict__ vid)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int m = 0, best = -1, bestv = -1;
+        double low = 0.0;
+        for (int k = 0; k < 6; ++k) {
+            int j = nbr[6 * i + k];
+            if (j == -1) continue;
+            double hj = ((uint64_t)(uint32_t)j < (uint64_t)n) ? h[j] : __longlong_as_double(0x7FF8000000000000LL);
+            if (m == 0 || hj < low) { low = hj; best = m; bestv = j; }
+            ++m;
+        }
+        bool ok = m > 0 && low < h[i];
+        pos[i] = ok ? best : -1;
+        if (vid) vid[i] = ok ? bestv : -1;
+    }
+}
+
+int grid1d(int64_t n, int block = 256)
+{
+    int64_t g = (n + block - 1) / block;
+    int64_t cap = (int64_t)nx::sm_count() * 16;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+NX_EXPORT size_t nx_erosion_workspace_size(int64_t n_padded_total, int nplanets)
+{
+    int64_t nblk = (n_padded_total + BLOCK - 1) / BLOCK;
+    return sizeof(nx_erosion_ctl) * (size_t)(nplanets > 0 ? nplanets : 1) + 3 * sizeof(double) * (size_t)(nblk > 0 ? nblk : 1) + 64;
+}
+
+namespace {
+
+struct Workspace {
+    nx_erosion_ctl *ctl;
+    double *partials;
+};
+
+Workspace carve(void *ws, int np)
+{
+    Workspace w;
+    w.ctl = (nx_erosion_ctl *)ws;
+    uintptr_t p = (uintptr_t)(w.ctl + np);
+    p = (p + 15) & ~(uintptr_t)15;
+    w.partials = (double *)p;
+    return w;
+}
+
+}  // namespace
+
+NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, const double *s64_dev, int64_t n,
+                              float *hw_dev, float *s_dev, void *workspace, size_t ws_bytes, void *stream)
+{
+    if (n <= 0) return nx::fail(NX_EINVAL, "nx_erosion_load: n must be > 0");
+    if (!h64_dev || !hw_dev || !s_dev || !workspace) return nx::fail(NX_EINVAL, "nx_erosion_load: null pointer");
+    if (ws_bytes < nx_erosion_workspace_size(n, 1)) return nx::fail(NX_EINVAL, "nx_erosion_load: workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    Workspace w = carve(workspace, 1);
+    unsigned long long *mb = (unsigned long long *)w.partials;   // first partial slot as scratch
+    NX_CHECK_CUDA(cudaMemsetAsync(mb, 0, sizeof(unsigned long long), s));
+    erosion_maxabs64_kernel<<<grid1d(n), 256, 0, s>>>(h64_dev, w64_dev, s64_dev, n, mb);
+    NX_CHECK_LAUNCH("erosion_maxabs64_kernel");
+    erosion_load64_kernel<<<grid1d(n), 256, 0, s>>>(h64_dev, w64_dev, s64_dev, n, mb, (float2 *)hw_dev, s_dev, w.ctl);
+    NX_CHECK_LAUNCH("erosion_load64_kernel");
+    nx::note_launch(2);
+    return NX_OK;
+}
+
+static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
+                     const int32_t *nbr_dev, const float *edge_dev, float *hw_dev, float *s_dev, float *hw_tmp,
+                     float *s_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace, size_t ws_bytes,
+                     cudaStream_t s)
+{
+    if (np <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !nbr_dev || !edge_dev || !hw_dev || !s_dev || !hw_tmp || !s_tmp || !workspace)
+        return nx::fail(NX_EINVAL, "erosion: null pointer");
+    int max_it = 0;
+    int64_t total = 0;
+    for (int p = 0; p < np; ++p) {
+        const nx_erosion_planet &P = planets_host[p];
+        if (P.vbeg % BLOCK != 0 || P.vend < P.vbeg || P.iters < 0)
+            return nx::fail(NX_EINVAL, "erosion: planet %d range must start at a multiple of %d", p, BLOCK);
+        if (p > 0 && (P.vbeg < planets_host[p - 1].vend || P.iters > planets_host[p - 1].iters))
+            return nx::fail(NX_EINVAL, "erosion: planets must be packed in order of descending iterations");
+        if (P.iters > max_it) max_it = P.iters;
+        total = P.vend;
+    }
+    if (ws_bytes < nx_erosion_workspace_size(total, np)) return nx::fail(NX_EINVAL, "erosion: workspace too small");
+    Workspace w = carve(workspace, np);
+    StepArgs a;
+    a.planets = planets_dev;
+    a.np = np;
+    a.nbr = nbr_dev;
+    a.el = edge_dev;
+    a.hw0 = (float2 *)hw_dev;
+    a.s0 = s_dev;
+    a.hw1 = (float2 *)hw_tmp;
+    a.s1 = s_tmp;
+    a.ctl = w.ctl;
+    a.partials = w.partials;
+    a.mass = mass_dev;
+    a.mass_np = np;
+    a.flow = flow_dev;
+    int last = np - 1;
+    for (int t = 0; t < max_it; ++t) {
+        while (last >= 0 && planets_host[last].iters <= t) --last;
+        if (last < 0) break;
+        int64_t end = planets_host[last].vend;
+        int64_t nblk = (end + BLOCK - 1) / BLOCK;
+        a.t = t;
+        erosion_step_kernel<<<(unsigned)nblk, BLOCK, 0, s>>>(a);
+        NX_CHECK_LAUNCH("erosion_step_kernel");
+        nx::note_launch(1);
+    }
+    if (max_it > 0) {
+        erosion_rebase_kernel<<<(np + 127) / 128, 128, 0, s>>>(planets_dev, np, w.ctl);
+        NX_CHECK_LAUNCH("erosion_rebase_kernel");
+        nx::note_launch(1);
+    }
+    return NX_OK;
+}
+
+NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *hw_dev, float *s_dev,
+                               float *hw_tmp_dev, float *s_tmp_dev, int iters, float rain,
+                               const nx_erosion_planet *planet_dev, double *mass_dev, uint16_t *flow_dev,
+                               void *workspace, size_t ws_bytes, void *stream)
+{
+    if (n <= 0 || iters < 0) return nx::fail(NX_EINVAL, "nx_erosion_steps: bad n or iters");
+    if (!planet_dev) return nx::fail(NX_EINVAL, "nx_erosion_steps: planet descriptor (device) required");
+    nx_erosion_planet P;
+    P.vbeg = 0;
+    P.vend = n;
+    P.iters = iters;
+    P.rain = rain;
+    cudaStream_t s = (cudaStream_t)stream;
+    NX_CHECK_CUDA(cudaMemcpyAsync((void *)planet_dev, &P, sizeof(P), cudaMemcpyHostToDevice, s));
+    // state enters in buffer 0; with an odd count the first iteration must read buffer 1
+    if (iters & 1) {
+        NX_CHECK_CUDA(cudaMemcpyAsync(hw_tmp_dev, hw_dev, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        NX_CHECK_CUDA(cudaMemcpyAsync(s_tmp_dev, s_dev, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    }
+    return run_batch(planet_dev, &P, 1, nbr_dev, edge_dev, hw_dev, s_dev, hw_tmp_dev, s_tmp_dev, mass_dev, flow_dev,
+                     workspace, ws_bytes, s);
+}
+
+NX_EXPORT int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
+                               const int32_t *nbr_dev, const float *edge_dev, float *hw_dev, float *s_dev,
+                               float *hw_tmp_dev, float *s_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes,
+                               void *stream)
+{
+    return run_batch(planets_dev, planets_host, nplanets, nbr_dev, edge_dev, hw_dev, s_dev, hw_tmp_dev, s_tmp_dev,
+                     mass_dev, nullptr, workspace, ws_bytes, (cudaStream_t)stream);
+}
+
+NX_EXPORT int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream)
+{
+    if (!workspace || nplanets <= 0) return nx::fail(NX_EINVAL, "nx_erosion_ctl_init: bad arguments");
+    if (ws_bytes < sizeof(nx_erosion_ctl) * (size_t)nplanets) return nx::fail(NX_EINVAL, "nx_erosion_ctl_init: workspace too small");
+    NX_CHECK_CUDA(cudaMemsetAsync(workspace, 0, sizeof(nx_erosion_ctl) * (size_t)nplanets, (cudaStream_t)stream));
+    return NX_OK;
+}
+
+NX_EXPORT int nx_erosion_store(const float *hw_dev, const float *s_dev, int64_t n, const void *workspace,
+                               double *h64_dev, double *w64_dev, double *s64_dev, void *stream)
+{
+    if (n <= 0 || !hw_dev || !s_dev || !workspace || !h64_dev) return nx::fail(NX_EINVAL, "nx_erosion_store: bad arguments");
+    const nx_erosion_ctl *ctl = (const nx_erosion_ctl *)workspace;
+    erosion_store64_kernel<<<grid1d(n), 256, 0, (cudaStream_t)stream>>>((const float2 *)hw_dev, s_dev, n, ctl,
+                                                                         h64_dev, w64_dev, s64_dev);
+    NX_CHECK_LAUNCH("erosion_store64_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_steepest_descent(const int32_t *nbr_dev, const double *h_dev, int64_t n, int32_t *pos_dev,
+                                  int32_t *vid_dev, void *stream)
+{
+    if (n < 0 || (n > 0 && (!nbr_dev || !h_dev || !pos_dev))) return nx::fail(NX_EINVAL, "nx_steepest_descent: bad arguments");
+    if (n == 0) return NX_OK;
+    steepest_kernel<<<grid1d(n), 256, 0, (cudaStream_t)stream>>>(nbr_dev, h_dev, n, pos_dev, vid_dev);
+    NX_CHECK_LAUNCH("steepest_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}

@@ -1,0 +1,202 @@
+// nx_insolation.cu -- per-vertex insolation accumulated over sun positions.
+//
+// Replaces the loop of climate.sample_insolation calls (climate.py:415-444;
+// driven over rotations as in brute_daily_insolation, climate.py:450-489).
+// For one sun position (rotation theta about z, tilt tau about y) the
+// reference adds, per vertex,
+//   max(cos|lat|, 0) * max(cos lon, 0)
+// with lat, lon of the rotated and tilted point (util.xyz2latlon,
+// util.py:59-75).  For a vertex on the sphere of the given radius r this
+// equals max(t, 0) / r with
+//   t = A cos(theta) + B sin(theta) + C,  A = x cos(tau), B = -y cos(tau),
+//   C = z sin(tau)
+// (cos lat = sqrt(tx^2+ty^2)/r, cos lon = tx/sqrt(tx^2+ty^2)).  When the
+// rotations come in pairs theta, theta + 180 degrees (every even uniform
+// schedule, e.g. 24 hours of 15 degrees), the pair contributes
+//   max(C+u, 0) + max(C-u, 0) = C + max(|C|, |u|),  u = A cos + B sin,
+// i.e. two operations per sun position.  Vertices off that sphere
+// (| |v|^2 - r^2 | > 1e-12 r^2) take the reference's general formula.
+//
+// Sums per tilt are binary32 (<= 360 terms); the running total over tilts
+// is compensated (Kahan) so the result tracks the binary64 sum.
+#include "nx_common.cuh"
+
+namespace nx {
+void note_launch(int k);
+}
+
+namespace {
+
+struct InsoArgs {
+    const double *xyz;
+    int64_t n;
+    double r;
+    float inv_r;
+    const float2 *tilt;    // (cos tau, sin tau) per tilt
+    int n_tilt;
+    const float2 *rot;     // (cos theta, sin theta): all rotations, or the first half in pair mode
+    int n_rot;             // number of entries in rot
+    int pairs;             // 1: each rot entry stands for theta and theta + 180
+    float *out;
+    int accumulate;
+};
+
+// climate.py:419-442 for a vertex off the sphere of radius r (binary32).
+__device__ __forceinline__ float general_term(float x, float y, float z, float inv_r, float ct, float st, float cr, float sr)
+{
+    float rx = x * cr - y * sr;
+    float ry = x * sr + y * cr;
+    float tx = rx * ct + z * st;
+    float ty = ry;
+    float tz = z * ct - rx * st;
+    float q = fminf(fmaxf(tz * inv_r, -1.0f), 1.0f);
+    float clat = sqrtf(fmaxf(1.0f - q * q, 0.0f));
+    float h2 = tx * tx + ty * ty;
+    float clon = h2 > 0.0f ? tx * rsqrtf(h2) : 1.0f;    // atan2(0, 0) = 0 -> cos = 1
+    return clat * fmaxf(clon, 0.0f);
+}
+
+template <int HP>
+__global__ void __launch_bounds__(256) insolation_kernel(InsoArgs a)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double X = a.xyz[3 * i], Y = a.xyz[3 * i + 1], Z = a.xyz[3 * i + 2];
+        const double rho2 = X * X + Y * Y + Z * Z;
+        const double r2 = a.r * a.r;
+        const bool on_sphere = fabs(rho2 - r2) <= 1e-12 * r2;
+        const float x = (float)X, y = (float)Y, z = (float)Z;
+        float tot = 0.0f, comp = 0.0f;          // Kahan over tilts
+        const int nr = HP > 0 ? HP : a.n_rot;
+        if (on_sphere) {
+            float2 rt[HP > 0 ? HP : 1];
+            if (HP > 0) {
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 1); ++h) rt[h] = a.rot[h];
+            }
+            for (int d = 0; d < a.n_tilt; ++d) {
+                const float2 t = a.tilt[d];
+                const float A = x * t.x, B = -(y * t.x), C = z * t.y;
+                float s = 0.0f;
+                if (a.pairs) {
+                    const float aC = fabsf(C);
+                    if (HP > 0) {
+#pragma unroll
+                        for (int h = 0; h < (HP > 0 ? HP : 1); ++h) {
+                            float u = fmaf(A, rt[h].x, B * rt[h].y);
+                            s += fmaxf(aC, fabsf(u));
+                        }
+                    } else {
+                        for (int h = 0; h < nr; ++h) {
+                            float2 q = a.rot[h];
+                            float u = fmaf(A, q.x, B * q.y);
+                            s += fmaxf(aC, fabsf(u));
+                        }
+                    }
+                    s = fmaf((float)nr, C, s);
+                } else {
+                    for (int h = 0; h < nr; ++h) {
+                        float2 q = a.rot[h];
+                        s += fmaxf(fmaf(A, q.x, fmaf(B, q.y, C)), 0.0f);
+                    }
+                }
+                float yk = s - comp;
+                float tk = tot + yk;
+                comp = (tk - tot) - yk;
+                tot = tk;
+            }
+            tot *= a.inv_r;
+        } else {
+            for (int d = 0; d < a.n_tilt; ++d) {
+                const float2 t = a.tilt[d];
+                float s = 0.0f;
+                for (int h = 0; h < nr; ++h) {
+                    float2 q = a.rot[h];
+                    s += general_term(x, y, z, a.inv_r, t.x, t.y, q.x, q.y);
+                    if (a.pairs) s += general_term(x, y, z, a.inv_r, t.x, t.y, -q.x, -q.y);
+                }
+                float yk = s - comp;
+                float tk = tot + yk;
+                comp = (tk - tot) - yk;
+                tot = tk;
+            }
+        }
+        a.out[i] = a.accumulate ? a.out[i] + tot : tot;
+    }
+}
+
+int grid_for(int64_t n)
+{
+    int64_t g = (n + 255) / 256;
+    int64_t cap = (int64_t)nx::sm_count() * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+// Degrees -> (cos, sin) as the reference computes them (climate.py:423-436:
+// cos(angle * pi / 180) in binary64), rounded to binary32.
+static void trig_table(const double *deg, int n, float *out)
+{
+    const double PI = 3.141592653589793;
+    for (int i = 0; i < n; ++i) {
+        double a = deg[i] * PI / 180;
+        out[2 * i] = (float)cos(a);
+        out[2 * i + 1] = (float)sin(a);
+    }
+}
+
+NX_EXPORT int nx_insolation_plan(const double *rot_deg, int n_rot, const double *tilt_deg, int n_tilt,
+                                 float *table_host, int *n_rot_entries, int *pairs)
+{
+    if (n_rot < 0 || n_tilt < 0 || !table_host || !n_rot_entries || !pairs || (n_rot && !rot_deg) ||
+        (n_tilt && !tilt_deg))
+        return nx::fail(NX_EINVAL, "nx_insolation_plan: bad arguments");
+    // pair mode: rotation h + n/2 is rotation h + 180 degrees exactly
+    int pr = 0;
+    if (n_rot > 0 && n_rot % 2 == 0) {
+        pr = 1;
+        for (int h = 0; h < n_rot / 2; ++h)
+            if (rot_deg[h + n_rot / 2] != rot_deg[h] + 180.0) { pr = 0; break; }
+    }
+    int nr = pr ? n_rot / 2 : n_rot;
+    trig_table(rot_deg, nr, table_host);
+    trig_table(tilt_deg, n_tilt, table_host + 2 * nr);
+    *n_rot_entries = nr;
+    *pairs = pr;
+    return NX_OK;
+}
+
+NX_EXPORT int nx_insolation(const double *xyz_dev, int64_t n, double radius, const float *table_dev, int n_rot_entries,
+                            int pairs, int n_tilt, float *out_dev, int accumulate, void *stream)
+{
+    if (n < 0 || n_rot_entries < 0 || n_tilt < 0) return nx::fail(NX_EINVAL, "nx_insolation: negative size");
+    if (n == 0) return NX_OK;
+    if (!xyz_dev || !out_dev || ((n_rot_entries || n_tilt) && !table_dev))
+        return nx::fail(NX_EINVAL, "nx_insolation: null pointer");
+    if (!(radius > 0.0)) return nx::fail(NX_EINVAL, "nx_insolation: radius must be > 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_rot_entries == 0 || n_tilt == 0) {
+        if (!accumulate) NX_CHECK_CUDA(cudaMemsetAsync(out_dev, 0, sizeof(float) * (size_t)n, s));
+        return NX_OK;
+    }
+    InsoArgs a;
+    a.xyz = xyz_dev;
+    a.n = n;
+    a.r = radius;
+    a.inv_r = (float)(1.0 / radius);
+    a.rot = (const float2 *)table_dev;
+    a.n_rot = n_rot_entries;
+    a.pairs = pairs ? 1 : 0;
+    a.tilt = (const float2 *)table_dev + n_rot_entries;
+    a.n_tilt = n_tilt;
+    a.out = out_dev;
+    a.accumulate = accumulate;
+    if (a.pairs && n_rot_entries == 12)
+        insolation_kernel<12><<<grid_for(n), 256, 0, s>>>(a);
+    else
+        insolation_kernel<0><<<grid_for(n), 256, 0, s>>>(a);
+    NX_CHECK_LAUNCH("insolation_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}

@@ -1,0 +1,348 @@
+// nx_mesh.cu -- icosphere generation, adjacency and per-slot edge lengths.
+//
+// The reference gets its sphere from meshzoo.icosa_sphere (util.py:43) and
+// its neighbour table from build_adjacency + sort_adjacency (util.py:591-662).
+// meshzoo is not available, so the vertex layout here is this project's own
+// (documented in nixis_gb300/icosphere.py); the adjacency kernels implement
+// the reference's two functions for any consistently wound triangle mesh, so
+// the neighbour table equals what the reference computes from the same
+// triangles.
+#include "nx_common.cuh"
+
+namespace nx {
+void note_launch(int k);
+}
+
+namespace {
+
+struct IcoTables {
+    double corner[12][3];
+    int face[20][3];
+    int fedge[20][3][2];   // per face side (AB, AC, BC): edge id, 1 if it runs low->high corner
+    int edge[30][2];
+};
+
+__constant__ IcoTables c_ico;
+
+// Point = normalise(w0*A + w1*B + w2*C), sums in the written order, no FMA.
+__device__ __forceinline__ void blend3(const double *A, const double *B, const double *C, double w0, double w1,
+                                       double w2, double *out)
+{
+    double p[3];
+    for (int c = 0; c < 3; ++c)
+        p[c] = __dadd_rn(__dadd_rn(__dmul_rn(w0, A[c]), __dmul_rn(w1, B[c])), __dmul_rn(w2, C[c]));
+    double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])), __dmul_rn(p[2], p[2])));
+    for (int c = 0; c < 3; ++c) out[c] = __ddiv_rn(p[c], r);
+}
+
+__device__ __forceinline__ void blend2(const double *A, const double *B, double w0, double w1, double *out)
+{
+    double p[3];
+    for (int c = 0; c < 3; ++c) p[c] = __dadd_rn(__dmul_rn(w0, A[c]), __dmul_rn(w1, B[c]));
+    double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])), __dmul_rn(p[2], p[2])));
+    for (int c = 0; c < 3; ++c) out[c] = __ddiv_rn(p[c], r);
+}
+
+__global__ void ico_vertices_kernel(int k, int64_t nv, double *__restrict__ xyz)
+{
+    const int64_t ne = (int64_t)30 * (k - 1);
+    const int64_t npf = (int64_t)(k - 1) * (k - 2) / 2;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        double out[3];
+        if (v < 12) {
+            for (int c = 0; c < 3; ++c) out[c] = c_ico.corner[v][c];
+        } else if (v < 12 + ne) {
+            int64_t q = v - 12;
+            int e = (int)(q / (k - 1));
+            int t = (int)(q - (int64_t)e * (k - 1)) + 1;
+            blend2(c_ico.corner[c_ico.edge[e][0]], c_ico.corner[c_ico.edge[e][1]], (double)(k - t), (double)t, out);
+        } else {
+            int64_t q = v - 12 - ne;
+            int f = (int)(q / npf);
+            int64_t off = q - (int64_t)f * npf;
+            // row i (1..k-2) holds k-1-i points; invert the running offset
+            // (i-1)(k-1) - (i-1)i/2 with a float estimate plus correction.
+            double kk = (double)k;
+            double disc = (2.0 * kk - 3.0) * (2.0 * kk - 3.0) - 8.0 * (double)off;
+            int i0 = (int)floor(((2.0 * kk - 3.0) - sqrt(disc > 0 ? disc : 0.0)) / 2.0);
+            int i = i0 + 1;
+            if (i < 1) i = 1;
+            if (i > k - 2) i = k - 2;
+            auto start = [&](int ii) -> int64_t { return (int64_t)(ii - 1) * (k - 1) - (int64_t)(ii - 1) * ii / 2; };
+            while (i > 1 && start(i) > off) --i;
+            while (i < k - 2 && start(i + 1) <= off) ++i;
+            int j = (int)(off - start(i)) + 1;
+            const int *F = c_ico.face[f];
+            blend3(c_ico.corner[F[0]], c_ico.corner[F[1]], c_ico.corner[F[2]], (double)(k - i - j), (double)i,
+                   (double)j, out);
+        }
+        xyz[3 * v] = out[0];
+        xyz[3 * v + 1] = out[1];
+        xyz[3 * v + 2] = out[2];
+    }
+}
+
+// Vertex id of face point (i, j); layout in icosphere.py.
+__device__ __forceinline__ int32_t face_vid(int f, int i, int j, int k)
+{
+    const int *F = c_ico.face[f];
+    if (i == 0 && j == 0) return F[0];
+    if (i == k && j == 0) return F[1];
+    if (i == 0 && j == k) return F[2];
+    int side, pos;
+    if (j == 0) { side = 0; pos = i; }
+    else if (i == 0) { side = 1; pos = j; }
+    else if (i + j == k) { side = 2; pos = j; }
+    else {
+        int64_t npf = (int64_t)(k - 1) * (k - 2) / 2;
+        int64_t off = (int64_t)(i - 1) * (k - 1) - (int64_t)(i - 1) * i / 2 + (j - 1);
+        return (int32_t)(12 + (int64_t)30 * (k - 1) + (int64_t)f * npf + off);
+    }
+    int e = c_ico.fedge[f][side][0];
+    int t = c_ico.fedge[f][side][1] ? pos : k - pos;
+    return (int32_t)(12 + (int64_t)e * (k - 1) + t - 1);
+}
+
+// Triangles of one face row-pair: triangle index within the face for
+// (i, j): rows before i hold sum_{i'<i} (2(k-i') - 1) = i(2k - i) triangles.
+__global__ void ico_triangles_kernel(int k, int64_t nt, int32_t *__restrict__ tris)
+{
+    const int64_t per_face = (int64_t)k * k;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        int f = (int)(t / per_face);
+        int64_t q = t - (int64_t)f * per_face;
+        // find row i with i(2k-i) <= q < (i+1)(2k-i-1)
+        double kk = (double)k;
+        int i = (int)floor(kk - sqrt(kk * kk - (double)q));
+        if (i < 0) i = 0;
+        if (i > k - 1) i = k - 1;
+        while (i > 0 && (int64_t)i * (2 * k - i) > q) --i;
+        while (i < k - 1 && (int64_t)(i + 1) * (2 * k - i - 1) <= q) ++i;
+        int64_t r = q - (int64_t)i * (2 * k - i);   // 0 .. 2(k-i)-2
+        int j = (int)(r / 2);
+        bool down = (r & 1) != 0;
+        int32_t a, b, c;
+        if (!down) {
+            a = face_vid(f, i, j, k); b = face_vid(f, i + 1, j, k); c = face_vid(f, i, j + 1, k);
+        } else {
+            a = face_vid(f, i + 1, j, k); b = face_vid(f, i + 1, j + 1, k); c = face_vid(f, i, j + 1, k);
+        }
+        tris[3 * t] = a;
+        tris[3 * t + 1] = b;
+        tris[3 * t + 2] = c;
+    }
+}
+
+// build_adjacency (util.py:591-613): every triangle t appends t1 to t0's row,
+// t2 to t1's, t0 to t2's, in triangle order.  Records (t, neighbour) are
+// gathered with an atomic slot per vertex, then each row is ordered by t.
+__global__ void adj_records_kernel(const int32_t *__restrict__ tris, int64_t nt, int64_t nv,
+                                   unsigned *__restrict__ cnt, unsigned long long *__restrict__ rec,
+                                   int *__restrict__ err)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        for (int e = 0; e < 3; ++e) {
+            int32_t a = tris[3 * t + e], b = tris[3 * t + (e + 1) % 3];
+            if ((uint64_t)(uint32_t)a >= (uint64_t)nv || (uint64_t)(uint32_t)b >= (uint64_t)nv) {
+                atomicOr(err, 1);
+                continue;
+            }
+            unsigned s = atomicAdd(&cnt[a], 1u);
+            if (s >= 6) {
+                atomicOr(err, 2);
+                continue;
+            }
+            rec[6 * (int64_t)a + s] = ((unsigned long long)t << 32) | (uint32_t)b;
+        }
+    }
+}
+
+__global__ void adj_rows_kernel(int64_t nv, const unsigned *__restrict__ cnt,
+                                const unsigned long long *__restrict__ rec, int32_t *__restrict__ adj)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        unsigned c = cnt[v];
+        if (c > 6) c = 6;
+        unsigned long long r[6];
+        for (int s = 0; s < 6; ++s) r[s] = s < (int)c ? rec[6 * v + s] : ~0ull;
+        for (int a = 1; a < 6; ++a) {       // insertion sort by triangle index
+            unsigned long long x = r[a];
+            int b = a - 1;
+            while (b >= 0 && r[b] > x) { r[b + 1] = r[b]; --b; }
+            r[b + 1] = x;
+        }
+        for (int s = 0; s < 6; ++s) adj[6 * v + s] = s < (int)c ? (int32_t)(uint32_t)r[s] : -1;
+    }
+}
+
+__device__ __forceinline__ bool row_has(const int32_t *row, int32_t v)
+{
+    bool f = false;
+    for (int s = 0; s < 6; ++s) f |= row[s] == v;
+    return f;
+}
+
+// sort_adjacency (util.py:638-662) with next_vert (util.py:623-629): walk the
+// neighbours of each vertex into a ring starting at slot 0.  Reads the
+// unsorted rows `in`, writes `out` (membership tests do not depend on order).
+__global__ void adj_sort_kernel(int64_t nv, const int32_t *__restrict__ in, int32_t *__restrict__ out)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        int32_t row[6], vis[6];
+        for (int s = 0; s < 6; ++s) { row[s] = in[6 * v + s]; vis[s] = -1; }
+        int deg = v < 12 ? 5 : 6;
+        int32_t pv = (int32_t)v, cur = row[0];
+        for (int i = 0; i < deg - 1; ++i) {
+            vis[i] = cur;
+            int32_t nxt = -1;
+            if (cur >= 0 && (int64_t)cur < nv) {
+                const int32_t *other = in + 6 * (int64_t)cur;
+                int32_t o[6];
+                for (int s = 0; s < 6; ++s) o[s] = other[s];
+                for (int s = 0; s < 6; ++s) {
+                    int32_t c = row[s];
+                    if (row_has(o, c) && c != pv) { nxt = c; break; }
+                }
+            }
+            cur = nxt;
+            pv = vis[i];
+        }
+        vis[deg - 1] = cur;
+        for (int s = 0; s < 6; ++s) out[6 * v + s] = vis[s];
+    }
+}
+
+// erosion.py:38-40 in binary64 (squares by multiplication), rounded to binary32.
+__global__ void edge_len_kernel(const double *__restrict__ xyz, const int32_t *__restrict__ nbr, int64_t nv,
+                                float *__restrict__ el, int *__restrict__ err)
+{
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 6 * nv; q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t v = q / 6;
+        int32_t j = nbr[q];
+        float d = 0.0f;
+        if (j >= 0 && (int64_t)j < nv) {
+            double dx = __dsub_rn(xyz[3 * v], xyz[3 * (int64_t)j]);
+            double dy = __dsub_rn(xyz[3 * v + 1], xyz[3 * (int64_t)j + 1]);
+            double dz = __dsub_rn(xyz[3 * v + 2], xyz[3 * (int64_t)j + 2]);
+            d = (float)__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+        } else if (j != -1 && err) {
+            atomicOr(err, 1);
+        }
+        el[q] = d;
+    }
+}
+
+int grid1d(int64_t n, int block = 256)
+{
+    int64_t g = (n + block - 1) / block;
+    int64_t cap = (int64_t)nx::sm_count() * 16;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+bool g_tables_ready[64] = {false};
+
+int upload_tables(const double *corners, const int *faces, const int *fedge, const int *edges)
+{
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && g_tables_ready[dev]) return NX_OK;
+    IcoTables t;
+    for (int i = 0; i < 12; ++i)
+        for (int c = 0; c < 3; ++c) t.corner[i][c] = corners[3 * i + c];
+    for (int f = 0; f < 20; ++f)
+        for (int c = 0; c < 3; ++c) {
+            t.face[f][c] = faces[3 * f + c];
+            t.fedge[f][c][0] = fedge[6 * f + 2 * c];
+            t.fedge[f][c][1] = fedge[6 * f + 2 * c + 1];
+        }
+    for (int e = 0; e < 30; ++e) {
+        t.edge[e][0] = edges[2 * e];
+        t.edge[e][1] = edges[2 * e + 1];
+    }
+    NX_CHECK_CUDA(cudaMemcpyToSymbol(c_ico, &t, sizeof(t)));
+    if (dev >= 0 && dev < 64) g_tables_ready[dev] = true;
+    return NX_OK;
+}
+
+}  // namespace
+
+NX_EXPORT int nx_icosphere_tables(const double *corners, const int32_t *faces, const int32_t *face_edges,
+                                  const int32_t *edges)
+{
+    if (!corners || !faces || !face_edges || !edges) return nx::fail(NX_EINVAL, "nx_icosphere_tables: null pointer");
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64) g_tables_ready[dev] = false;
+    return upload_tables(corners, faces, face_edges, edges);
+}
+
+NX_EXPORT int nx_icosphere(int k, double *xyz_dev, int32_t *tris_dev, void *stream)
+{
+    if (k < 1 || (int64_t)10 * k * k + 2 > 0x7FFFFFFFLL) return nx::fail(NX_EINVAL, "nx_icosphere: bad divisions %d", k);
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !g_tables_ready[dev])
+        return nx::fail(NX_EINVAL, "nx_icosphere: call nx_icosphere_tables first on this device");
+    int64_t nv = (int64_t)10 * k * k + 2, nt = (int64_t)20 * k * k;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (xyz_dev) {
+        ico_vertices_kernel<<<grid1d(nv), 256, 0, s>>>(k, nv, xyz_dev);
+        NX_CHECK_LAUNCH("ico_vertices_kernel");
+        nx::note_launch(1);
+    }
+    if (tris_dev) {
+        ico_triangles_kernel<<<grid1d(nt), 256, 0, s>>>(k, nt, tris_dev);
+        NX_CHECK_LAUNCH("ico_triangles_kernel");
+        nx::note_launch(1);
+    }
+    return NX_OK;
+}
+
+NX_EXPORT size_t nx_adjacency_workspace_size(int64_t nv)
+{
+    return (size_t)nv * (6 * sizeof(unsigned long long) + sizeof(unsigned)) + 256;
+}
+
+NX_EXPORT int nx_build_adjacency(const int32_t *tris_dev, int64_t nt, int64_t nv, int32_t *adj_dev, void *workspace,
+                                 size_t ws_bytes, int *err_dev, void *stream)
+{
+    if (nt < 0 || nv < 0 || (nt + 4) / 2 != nv) return nx::fail(NX_EINVAL, "nx_build_adjacency: need nv = (nt+4)/2");
+    if (nv == 0) return NX_OK;
+    if (!tris_dev || !adj_dev || !workspace || !err_dev) return nx::fail(NX_EINVAL, "nx_build_adjacency: null pointer");
+    if (ws_bytes < nx_adjacency_workspace_size(nv)) return nx::fail(NX_EINVAL, "nx_build_adjacency: workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long *rec = (unsigned long long *)workspace;
+    unsigned *cnt = (unsigned *)(rec + 6 * nv);
+    NX_CHECK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (size_t)nv, s));
+    adj_records_kernel<<<grid1d(nt), 256, 0, s>>>(tris_dev, nt, nv, cnt, rec, err_dev);
+    NX_CHECK_LAUNCH("adj_records_kernel");
+    adj_rows_kernel<<<grid1d(nv), 256, 0, s>>>(nv, cnt, rec, adj_dev);
+    NX_CHECK_LAUNCH("adj_rows_kernel");
+    nx::note_launch(2);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_sort_adjacency(const int32_t *adj_in_dev, int32_t *adj_out_dev, int64_t nv, void *stream)
+{
+    if (nv < 0) return nx::fail(NX_EINVAL, "nx_sort_adjacency: nv < 0");
+    if (nv == 0) return NX_OK;
+    if (!adj_in_dev || !adj_out_dev || adj_in_dev == adj_out_dev)
+        return nx::fail(NX_EINVAL, "nx_sort_adjacency: need distinct input and output rows");
+    adj_sort_kernel<<<grid1d(nv), 256, 0, (cudaStream_t)stream>>>(nv, adj_in_dev, adj_out_dev);
+    NX_CHECK_LAUNCH("adj_sort_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, float *edge_dev,
+                              int *err_dev, void *stream)
+{
+    if (nv < 0) return nx::fail(NX_EINVAL, "nx_edge_lengths: nv < 0");
+    if (nv == 0) return NX_OK;
+    if (!xyz_dev || !nbr_dev || !edge_dev) return nx::fail(NX_EINVAL, "nx_edge_lengths: null pointer");
+    edge_len_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, edge_dev, err_dev);
+    NX_CHECK_LAUNCH("edge_len_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}

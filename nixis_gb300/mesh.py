@@ -1,0 +1,163 @@
+"""Icosphere meshes on the GPU: vertices, triangles, neighbour table and
+per-slot edge lengths, kept resident per subdivision.
+
+``create_mesh`` replaces util.create_mesh (util.py:17-50, meshzoo);
+``build_adjacency`` / ``sort_adjacency`` implement util.py:591-662 on the
+GPU and give the reference's neighbour table for the same triangles.
+"""
+import ctypes
+import threading
+
+import numpy as np
+import torch
+
+from . import _dev
+from . import icosphere as ico
+from ._lib import call, lib
+
+_tables_done = set()
+_lock = threading.Lock()
+
+
+def _ensure_tables():
+    dev = torch.cuda.current_device()
+    if dev in _tables_done:
+        return
+    with _lock:
+        if dev in _tables_done:
+            return
+        c = np.ascontiguousarray(ico.corners(), np.float64)
+        f = np.ascontiguousarray(ico.FACES, np.int32)
+        fe = np.ascontiguousarray(ico.face_edge_table(), np.int32)
+        e = np.ascontiguousarray(ico.edges(), np.int32)
+        vp = ctypes.c_void_p
+        call("nx_icosphere_tables", c.ctypes.data_as(vp), f.ctypes.data_as(vp), fe.ctypes.data_as(vp),
+             e.ctypes.data_as(vp))
+        _tables_done.add(dev)
+
+
+def icosphere(divisions, with_tris=True, stream=None):
+    """(points float64 (N,3), cells int32 (T,3) or None) as CUDA tensors."""
+    _dev.require_cuda()
+    k = ico.check_divisions(divisions)
+    _ensure_tables()
+    nv, nt = ico.counts(k)
+    xyz = torch.empty((nv, 3), dtype=torch.float64, device="cuda")
+    tris = torch.empty((nt, 3), dtype=torch.int32, device="cuda") if with_tris else None
+    call("nx_icosphere", k, _dev.ptr(xyz), _dev.ptr(tris), _dev.stream_handle(stream))
+    return xyz, tris
+
+
+def create_mesh(divisions):
+    """util.create_mesh: (points float64 (10k^2+2, 3), cells int32 (20k^2, 3))
+    as numpy arrays (the reference returns numpy)."""
+    xyz, tris = icosphere(divisions)
+    return xyz.cpu().numpy(), tris.cpu().numpy()
+
+
+def build_adjacency(triangles, stream=None):
+    """util.build_adjacency: (N,6) int32 neighbour rows in triangle order,
+    -1 padded (CUDA tensor; numpy in -> numpy out)."""
+    host = _dev.is_host(triangles)
+    t = _dev.to_device(triangles, np.int32, name="triangles")
+    if t.ndim != 2 or t.shape[1] != 3:
+        raise ValueError("triangles must have shape (T, 3)")
+    nt = t.shape[0]
+    nv = (nt + 4) // 2
+    adj = torch.empty((nv, 6), dtype=torch.int32, device="cuda")
+    ws = torch.empty(int(lib().nx_adjacency_workspace_size(nv)), dtype=torch.uint8, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("nx_build_adjacency", _dev.ptr(t), nt, nv, _dev.ptr(adj), _dev.ptr(ws), ws.numel(), _dev.ptr(err),
+         _dev.stream_handle(stream))
+    e = int(err.item())
+    if e & 1:
+        raise ValueError("build_adjacency: a triangle references a vertex id outside [0, (T+4)/2)")
+    if e & 2:
+        raise ValueError("build_adjacency: a vertex has more than 6 neighbours")
+    return adj.cpu().numpy() if host else adj
+
+
+def sort_adjacency(adj, stream=None):
+    """util.sort_adjacency, in place (numpy or CUDA tensor)."""
+    host = _dev.is_host(adj)
+    a = _dev.to_device(adj, np.int32, name="adj")
+    out = torch.empty_like(a)
+    call("nx_sort_adjacency", _dev.ptr(a), _dev.ptr(out), a.shape[0], _dev.stream_handle(stream))
+    if host:
+        adj[...] = out.cpu().numpy()
+    else:
+        adj.copy_(out)
+    return adj
+
+
+def edge_lengths(xyz, nbr, stream=None):
+    """float32 (N,6) per-slot neighbour distances (binary64, rounded)."""
+    x = _dev.to_device(xyz, np.float64, name="verts")
+    nb = _dev.to_device(nbr, np.int32, name="neighbors")
+    n = x.shape[0]
+    if nb.shape != (n, 6):
+        raise ValueError("neighbors must have shape (N, 6)")
+    el = torch.empty((n, 6), dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("nx_edge_lengths", _dev.ptr(x), _dev.ptr(nb), n, _dev.ptr(el), _dev.ptr(err), _dev.stream_handle(stream))
+    return el, err
+
+
+class PlanetMesh:
+    """A subdivision's resident mesh: xyz float64 (N,3), nbr int32 (N,6),
+    edge float32 (N,6); triangles are dropped after the adjacency is built."""
+
+    def __init__(self, divisions, stream=None):
+        self.k = ico.check_divisions(divisions)
+        self.n = ico.counts(self.k)[0]
+        xyz, tris = icosphere(self.k, stream=stream)
+        adj = build_adjacency(tris, stream=stream)
+        del tris
+        nbr = torch.empty_like(adj)
+        call("nx_sort_adjacency", _dev.ptr(adj), _dev.ptr(nbr), self.n, _dev.stream_handle(stream))
+        del adj
+        self.xyz = xyz
+        self.nbr = nbr
+        self.edge, err = edge_lengths(xyz, nbr, stream=stream)
+        if int(err.item()):
+            raise RuntimeError("mesh adjacency produced an invalid neighbour id")
+
+    @property
+    def nbytes(self):
+        return self.xyz.numel() * 8 + self.nbr.numel() * 4 + self.edge.numel() * 4
+
+
+class MeshCache:
+    """Meshes kept resident in HBM, keyed by divisions, LRU-evicted past a
+    byte budget."""
+
+    def __init__(self, budget_bytes=None):
+        self.budget = budget_bytes
+        self._m = {}
+        self._order = []
+
+    def get(self, divisions, stream=None):
+        k = int(divisions)
+        if k in self._m:
+            self._order.remove(k)
+            self._order.append(k)
+            return self._m[k]
+        m = PlanetMesh(k, stream=stream)
+        self._m[k] = m
+        self._order.append(k)
+        self._evict()
+        return m
+
+    def _evict(self):
+        if self.budget is None:
+            return
+        while len(self._order) > 1 and self.nbytes > self.budget:
+            k = self._order.pop(0)
+            del self._m[k]
+
+    @property
+    def nbytes(self):
+        return sum(m.nbytes for m in self._m.values())
+
+    def __contains__(self, k):
+        return int(k) in self._m

@@ -1,0 +1,220 @@
+"""GPU erosion (variant 3) against the oracle and the reference's goldens.
+
+* binary32 step: bit-exact against the oracle's binary32 restatement of
+  erosion_iteration3 (same operation order), for 1 and 50 iterations;
+* flow choice (sign of h_n - h_i per slot): bit-exact against the binary64
+  reference on binary32-representable inputs;
+* trajectories against the binary64 reference: max|err| / max|field| <=
+  ERO_TOL at 1, 10 and 50 iterations (stated tolerance);
+* the power-of-two rescale is exact (scaling inputs by 2^100 scales
+  outputs by 2^100 bit for bit) and keeps 200 iterations finite;
+* batched planets give the same bits as each planet alone.
+"""
+import numpy as np
+import pytest
+import torch
+
+import golden_io
+import meshref
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ERO_TOL = {1: 1e-6, 10: 1e-5, 30: 3e-5, 50: 3e-5}
+
+
+def golden_case(k):
+    g = golden_io.load("mesh_erosion")
+    pts, _ = meshref.icosphere(k, with_tris=False)
+    return g, pts, g[f"adj_k{k}"]
+
+
+def run_gpu(pts, adj, h, w, s, iters, rain=0.0, flow=False, mass=False):
+    from nixis_gb300 import erosion
+    r = erosion.ErosionRun(pts, adj)
+    r.load(torch.from_numpy(np.asarray(h, np.float64)).cuda(), torch.from_numpy(np.asarray(w, np.float64)).cuda(),
+           torch.from_numpy(np.asarray(s, np.float64)).cuda())
+    m, f = r.steps(iters, rain=rain, flow=flow, mass=mass)
+    r.check()
+    hd = torch.empty(r.n, dtype=torch.float64, device="cuda")
+    wd, sd = torch.empty_like(hd), torch.empty_like(hd)
+    r.store(hd, wd, sd)
+    return hd.cpu().numpy(), wd.cpu().numpy(), sd.cpu().numpy(), m, f, r
+
+
+def test_edge_lengths_match_mirror():
+    from nixis_gb300 import mesh
+    for k in (6, 12):
+        g, pts, adj = golden_case(k)
+        el, err = mesh.edge_lengths(pts, adj)
+        assert int(err.item()) == 0
+        assert np.array_equal(el.cpu().numpy(), meshref.edge_lengths(pts, adj))
+
+
+@pytest.mark.parametrize("k", [6, 12])
+def test_binary32_steps_bit_exact_and_flow_choice(k):
+    g, pts, adj = golden_case(k)
+    h0 = g[f"ero_k{k}_f32_h0"].astype(np.float32)
+    w0 = g[f"ero_k{k}_f32_w0"].astype(np.float32)
+    s0 = np.zeros_like(h0)
+    el = meshref.edge_lengths(pts, adj)
+    # one step + flow bits
+    h1, w1, s1, _, flow, _ = run_gpu(pts, adj, h0, w0, s0, 1, flow=True)
+    ho, wo, so = O.erosion_iteration3_f32(el, adj, h0, w0, s0)
+    assert np.array_equal(h1, ho.astype(np.float64))
+    assert np.array_equal(w1, wo.astype(np.float64))
+    assert np.array_equal(s1, so.astype(np.float64))
+    # flow choice equals the binary64 reference's slope sign on the same inputs
+    hh = h0.astype(np.float64)
+    f = flow.cpu().numpy().astype(np.int64) & 0xFFFF
+    for slot in range(6):
+        j = adj[:, slot]
+        code = (f >> (2 * slot)) & 3
+        ok = j >= 0
+        d = np.where(ok, hh[np.where(ok, j, 0)] - hh, 0.0)
+        want = np.where(~ok, 0, np.where(d > 0, 1, np.where(d < 0, 2, 0)))
+        assert np.array_equal(code, want), slot
+    # 50 steps, still bit-exact against the binary32 restatement
+    hG, wG, sG, _, _, _ = run_gpu(pts, adj, h0, w0, s0, 50)
+    h, w, s = h0, w0, s0
+    for _ in range(50):
+        h, w, s = O.erosion_iteration3_f32(el, adj, h, w, s)
+    assert np.array_equal(hG, h.astype(np.float64))
+    assert np.array_equal(wG, w.astype(np.float64))
+    assert np.array_equal(sG, s.astype(np.float64))
+
+
+def rel_err(got, ref):
+    return np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+@pytest.mark.parametrize("k", [6, 12])
+@pytest.mark.parametrize("variant", ["smooth", "terraced", "f32"])
+def test_trajectory_against_binary64_reference(k, variant):
+    from nixis_gb300 import erosion
+    g, pts, adj = golden_case(k)
+    h = g[f"ero_k{k}_{variant}_h0"].copy()
+    w = g[f"ero_k{k}_{variant}_w0"].copy()
+    s = np.zeros_like(h)
+    done = 0
+    for it in g[f"ero_k{k}_{variant}_iters"]:
+        for _ in range(int(it) - done):
+            erosion.erosion_iteration3(pts, adj, h, w, s)      # the drop-in, float64 in place
+        done = int(it)
+        ref = g[f"ero_k{k}_{variant}_it{it}"]
+        for f, (got, want) in enumerate(zip((h, w, s), ref)):
+            e = rel_err(got, want)
+            assert e <= ERO_TOL[int(it)], (k, variant, int(it), f, e)
+
+
+@pytest.mark.parametrize("k", [6, 12])
+def test_erode_terrain3_against_reference(k):
+    from nixis_gb300 import erosion
+    g, pts, adj = golden_case(k)
+    h0 = g[f"ero_k{k}_smooth_h0"]
+    for n_iter in (0, 3):
+        h = h0.copy()
+        erosion.erode_terrain3(pts, adj, h, n_iter)
+        assert rel_err(h, g[f"erode3_k{k}_n{n_iter}"]) <= 1e-6
+
+
+def test_rescale_is_exact_and_keeps_long_runs_finite():
+    g, pts, adj = golden_case(12)
+    h0 = g["ero_k12_f32_h0"]
+    w0 = g["ero_k12_f32_w0"]
+    s0 = np.zeros_like(h0)
+    a = run_gpu(pts, adj, h0, w0, s0, 40)
+    b = run_gpu(pts, adj, h0 * 2.0 ** 100, w0 * 2.0 ** 100, s0, 40)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x * 2.0 ** 100, y)
+    # 200 iterations pass binary32's range; the scaled state stays exact
+    hG, wG, sG, mass, _, run = run_gpu(pts, adj, h0, w0, s0, 200, mass=True)
+    assert run.scale_exponent() > 0
+    assert np.isfinite(hG).all() and np.isfinite(wG).all() and np.isfinite(sG).all()
+    h, w, s = h0.copy(), w0.copy(), s0.copy()
+    for _ in range(200):
+        O.erosion_iteration3(pts, adj, h, w, s)
+    assert np.abs(wG).max() > 1e40
+    for got, want in ((hG, h), (wG, w), (sG, s)):
+        assert rel_err(got, want) <= 2e-4
+    # mass sums: sum(h + s) is invariant; the per-iteration sums match the state
+    m = mass.cpu().numpy()
+    assert np.allclose(m[-1], [hG.sum(), wG.sum(), sG.sum()], rtol=1e-9)
+    inv = m[:, 0] + m[:, 2]
+    assert np.abs(inv - inv[0]).max() <= 1e-6 * np.abs(m[:, :3]).max()
+
+
+def test_steepest_descent_matches_find_lowest():
+    from nixis_gb300 import erosion
+    g, pts, adj = golden_case(6)
+    h = g["ero_k6_terraced_h0"]
+    pos, vid = erosion.steepest_descent(adj, h)
+    pos = pos.cpu().numpy()
+    assert np.array_equal(pos, g["find_lowest_k6"])
+    vid = vid.cpu().numpy()
+    for v in range(len(adj)):
+        if pos[v] >= 0:
+            assert vid[v] == [j for j in adj[v] if j != -1][pos[v]]
+        assert erosion.find_lowest(v, adj[v], h) == (None if pos[v] < 0 else pos[v])
+
+
+def test_batched_planets_equal_planets_alone():
+    import ctypes
+    from nixis_gb300 import _lib, _dev
+    planets = []
+    for k, seed, iters in ((12, 1, 37), (6, 2, 50), (9, 3, 0), (4, 4, 11), (7, 5, 36)):
+        p, t = meshref.icosphere(k)
+        adj = O.build_adjacency(t)
+        O.sort_adjacency(adj)
+        perm, pgi = O.init(seed)
+        h = O.rescale(O.sample_octaves(p, None, perm, pgi, 5, 1.0, 1.0, 2.0, 0.5, 1.0), -8000, 8000)
+        h = h.astype(np.float32).astype(np.float64)
+        planets.append((p, adj, h, iters))
+    planets.sort(key=lambda x: -x[3])
+    # pack: each range starts at a multiple of 256, neighbour ids global
+    off, descs, nbrs, els, hs = 0, [], [], [], []
+    for p, adj, h, iters in planets:
+        n = len(p)
+        pad = (-n) % 256
+        descs.append((off, off + n, iters))
+        nb = np.where(adj >= 0, adj + off, -1).astype(np.int32)
+        nbrs.append(np.concatenate([nb, np.full((pad, 6), -1, np.int32)]))
+        el = meshref.edge_lengths(p, adj)
+        els.append(np.concatenate([el, np.zeros((pad, 6), np.float32)]))
+        hs.append(np.concatenate([h, np.zeros(pad)]))
+        off += n + pad
+    N = off
+    nbr = torch.from_numpy(np.concatenate(nbrs)).cuda()
+    el = torch.from_numpy(np.concatenate(els)).cuda()
+    hall = np.concatenate(hs).astype(np.float32)
+    hw = torch.zeros((N, 2), dtype=torch.float32, device="cuda")
+    s = torch.zeros(N, dtype=torch.float32, device="cuda")
+    hw_t, s_t = torch.zeros_like(hw), torch.zeros_like(s)
+    for (b, e, iters) in descs:
+        dst_hw = hw_t if iters & 1 else hw
+        dst_hw[b:e, 0] = torch.from_numpy(hall[b:e]).cuda()
+        dst_hw[b:e, 1] = 1e-3
+    arr = (_lib.ErosionPlanet * len(descs))(*[_lib.ErosionPlanet(b, e, it, 0.0) for b, e, it in descs])
+    pd = torch.from_numpy(np.frombuffer(bytes(arr), np.uint8).copy()).cuda()
+    ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(N, len(descs))), dtype=torch.uint8, device="cuda")
+    st = _dev.stream_handle()
+    _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), len(descs), st)
+    _lib.call("nx_erosion_batch", _dev.ptr(pd), ctypes.cast(arr, ctypes.c_void_p), len(descs), _dev.ptr(nbr),
+              _dev.ptr(el), _dev.ptr(hw), _dev.ptr(s), _dev.ptr(hw_t), _dev.ptr(s_t), None, _dev.ptr(ws),
+              ws.numel(), st)
+    out_hw = hw.cpu().numpy()
+    out_s = s.cpu().numpy()
+    for (p, adj, h, iters), (b, e, _) in zip(planets, descs):
+        ha, wa, sa, _, _, _ = run_gpu(p, adj, h, np.full(len(p), np.float32(1e-3)), np.zeros(len(p)), iters)
+        assert np.array_equal(out_hw[b:e, 0].astype(np.float64), ha)
+        assert np.array_equal(out_hw[b:e, 1].astype(np.float64), wa)
+        assert np.array_equal(out_s[b:e].astype(np.float64), sa)
+
+
+def test_bad_neighbour_id_is_reported_not_faulted():
+    from nixis_gb300 import erosion
+    g, pts, adj = golden_case(6)
+    bad = adj.copy()
+    bad[20, 3] = len(pts) + 5
+    with pytest.raises(IndexError):
+        erosion.erosion_iteration3(pts, bad, g["ero_k6_smooth_h0"].copy(), np.full(len(pts), 1e-3), np.zeros(len(pts)))

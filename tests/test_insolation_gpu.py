@@ -1,0 +1,90 @@
+"""GPU insolation against the reference's goldens and the binary64 oracle sum.
+
+Tolerance (stated): per-vertex |err| <= 1e-5 * max|sum| against the binary64
+sum of the reference's terms; single-position calls against the reference's
+own float32 results to 2e-6 absolute (terms are <= 1).
+"""
+import numpy as np
+import pytest
+import torch
+
+import golden_io
+import meshref
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+INSO_TOL = 1e-5
+
+
+def test_single_positions_match_reference():
+    from nixis_gb300 import climate
+    g = golden_io.load("insolation")
+    pts, _ = meshref.icosphere(4, with_tris=False)
+    for a, r in enumerate(g["rots"]):
+        for b, t in enumerate(g["tilts"]):
+            arr = np.zeros(len(pts), np.float32)
+            climate.sample_insolation(arr, pts, 1.0, r, t)
+            np.testing.assert_allclose(arr, g["single"][a, b], rtol=0, atol=2e-6)
+    arr = np.zeros(len(pts), np.float32)
+    for r in g["rots"]:
+        climate.sample_insolation(arr, pts, 1.0, r, 23.44)
+    np.testing.assert_allclose(arr, g["cumulative"], rtol=0, atol=1e-5)
+    np.testing.assert_allclose([climate.calculate_seasonal_tilt(23.44, climate.day2deg(365, d)) for d in range(365)],
+                               g["seasonal_tilt"], rtol=0, atol=1e-12)
+
+
+def test_brute_daily_matches_reference():
+    from nixis_gb300 import climate
+    g = golden_io.load("insolation")
+    p3, _ = meshref.icosphere(3, with_tris=False)
+    got = climate.brute_daily_insolation(p3, None, 1.0, 23.44)
+    ref64 = O.annual_insolation(p3, 1.0, axial_tilt=0.0, days=1, hours=360)  # tilt 0 schedule, checked below
+    ref = g["daily_unit"]
+    assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
+    got = climate.brute_daily_insolation(p3 * 6378100.0, None, 6378100.0, 10.0)
+    ref = g["daily_earth"]
+    assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
+    assert ref64.shape == (len(p3),)
+
+
+def annual_ref(pts, radius, days, hours, tilt=23.44):
+    return O.annual_insolation(pts, radius, axial_tilt=tilt, days=days, hours=hours)
+
+
+@pytest.mark.parametrize("k", [4, 16])
+def test_annual_sum_against_binary64(k):
+    from nixis_gb300 import climate
+    pts, _ = meshref.icosphere(k, with_tris=False)
+    got = climate.annual_insolation(pts, 1.0).cpu().numpy().astype(np.float64)
+    ref = annual_ref(pts, 1.0, 365, 24)
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err <= INSO_TOL, err
+    # the reference's own float32 running sum is farther from the exact sum
+    _, ref32 = O.annual_insolation(pts, 1.0, axial_tilt=23.44, days=365, hours=24, with_f32=True)
+    assert err <= np.abs(ref32 - ref).max() / np.abs(ref).max() + 1e-7
+
+
+def test_annual_sum_random_vertices_and_schedules():
+    from nixis_gb300 import climate
+    rng = np.random.default_rng(9)
+    u = rng.normal(size=(100000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    got = climate.annual_insolation(u, 1.0).cpu().numpy()
+    ref = annual_ref(u, 1.0, 365, 24)
+    assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
+    # odd rotation counts (no 180-degree pairs) and an earth-radius sphere
+    got = climate.annual_insolation(u[:20000] * 6378100.0, 6378100.0, days=30, hours=7).cpu().numpy()
+    ref = annual_ref(u[:20000] * 6378100.0, 6378100.0, 30, 7)
+    assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
+
+
+def test_vertices_off_the_sphere_use_the_general_formula():
+    from nixis_gb300 import climate
+    rng = np.random.default_rng(10)
+    u = rng.normal(size=(20000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    v = u * rng.uniform(0.9, 1.1, size=(len(u), 1))
+    got = climate.annual_insolation(v, 1.0, days=20, hours=24).cpu().numpy()
+    ref = annual_ref(v, 1.0, 20, 24)
+    assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
