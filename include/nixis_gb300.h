@@ -154,38 +154,41 @@ size_t nx_erosion_workspace_size(int64_t n_padded_total, int nplanets);
 /* Zero the per-planet control words (scale exponent 0) of a workspace. */
 int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream);
 
+/* Erosion state: float4 per vertex (h_hi, h_lo, w, s): water and sediment
+ * binary32, height as an unevaluated sum h_hi + h_lo of binary32s; values
+ * are true values * 2^-K for the planet's scale exponent K (below). */
+
 /* Load binary64 fields (the reference's r_buff/heights, wat, sed; w/s may
- * be NULL for zeros) into the binary32 state: hw_dev float[2n] interleaved
- * (h, w), s_dev float[n], choosing a power-of-two scale so values fit. */
-int nx_erosion_load(const double *h64_dev, const double *w64_dev, const double *s64_dev, int64_t n, float *hw_dev,
-                    float *s_dev, void *workspace, size_t ws_bytes, void *stream);
+ * be NULL for zeros) into the state st_dev float[4n], choosing a
+ * power-of-two scale so every value fits. */
+int nx_erosion_load(const double *h64_dev, const double *w64_dev, const double *s64_dev, int64_t n, float *st_dev,
+                    void *workspace, size_t ws_bytes, void *stream);
 
 /* `iters` Jacobi iterations of erosion.erosion_iteration3 (erosion.py:
- * 197-279) on one planet, result left in (hw_dev, s_dev).  hw_tmp/s_tmp:
- * second buffer of the same sizes.  planet_dev: device scratch for one
+ * 197-279) on one planet, result left in st_dev.  st_tmp_dev: second
+ * buffer of the same size.  planet_dev: device scratch for one
  * nx_erosion_planet.  mass_dev (optional): float64[iters*3] per-iteration
- * (sum h, sum w, sum s), compensated, scaled back to true units.  flow_dev
- * (optional): uint16[n], per slot k bits 2k..2k+1 = 1 if the neighbour is
- * higher, 2 if lower (the reference's slope > 0 / < 0 choice), of the last
- * iteration. */
-int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *hw_dev, float *s_dev,
-                     float *hw_tmp_dev, float *s_tmp_dev, int iters, float rain, const nx_erosion_planet *planet_dev,
-                     double *mass_dev, uint16_t *flow_dev, void *workspace, size_t ws_bytes, void *stream);
+ * (sum h, sum w, sum s), compensated, in true units.  flow_dev (optional):
+ * uint16[n], per slot k bits 2k..2k+1 = 1 if the neighbour is higher, 2 if
+ * lower (the reference's slope > 0 / < 0 choice), of the last iteration. */
+int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *st_dev, float *st_tmp_dev,
+                     int iters, float rain, nx_erosion_planet *planet_dev, double *mass_dev, uint16_t *flow_dev,
+                     void *workspace, size_t ws_bytes, void *stream);
 
-/* Batched erosion: every planet runs its own iteration count in one
- * launch per iteration over the planets still running.  Each planet's
- * state starts in buffer (iters & 1) -- 0: (hw_dev, s_dev), 1: (hw_tmp,
- * s_tmp) -- and ends in buffer 0.  mass_dev (optional): float64
- * [max_iters][nplanets][3].  Call nx_erosion_ctl_init first. */
+/* Batched erosion: every planet runs its own iteration count, one launch
+ * per iteration over the planets still running.  A planet's state starts
+ * in buffer (iters & 1) -- 0: st_dev, 1: st_tmp_dev -- and ends in st_dev.
+ * mass_dev (optional): float64[max_iters][nplanets][3].  Call
+ * nx_erosion_ctl_init first. */
 int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
-                     const int32_t *nbr_dev, const float *edge_dev, float *hw_dev, float *s_dev, float *hw_tmp_dev,
-                     float *s_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes, void *stream);
+                     const int32_t *nbr_dev, const float *edge_dev, float *st_dev, float *st_tmp_dev,
+                     double *mass_dev, void *workspace, size_t ws_bytes, void *stream);
 
-/* Write one planet's binary32 state back as binary64 true values (undoing
- * its power-of-two scale, kept in the workspace's first control block).
- * w64_dev / s64_dev may be NULL. */
-int nx_erosion_store(const float *hw_dev, const float *s_dev, int64_t n, const void *workspace, double *h64_dev,
-                     double *w64_dev, double *s64_dev, void *stream);
+/* Write one planet's state back as binary64 true values (h_hi + h_lo, w, s
+ * times 2^K, K from the workspace's first control block).  w64_dev /
+ * s64_dev may be NULL. */
+int nx_erosion_store(const float *st_dev, int64_t n, const void *workspace, double *h64_dev, double *w64_dev,
+                     double *s64_dev, void *stream);
 
 /* Layout of a workspace's per-planet control block (32 bytes, planet p at
  * byte 32*p): after a run, K[0] is the planet's scale exponent (stored

@@ -32,11 +32,10 @@ SIGNATURES = {
     "nx_edge_lengths": (_i32, [_p, _p, _i64, _p, _p, _p]),
     "nx_erosion_workspace_size": (ctypes.c_size_t, [_i64, _i32]),
     "nx_erosion_ctl_init": (_i32, [_p, ctypes.c_size_t, _i32, _p]),
-    "nx_erosion_load": (_i32, [_p, _p, _p, _i64, _p, _p, _p, ctypes.c_size_t, _p]),
-    "nx_erosion_steps": (_i32, [_p, _p, _i64, _p, _p, _p, _p, _i32, ctypes.c_float, _p, _p, _p, _p,
-                                ctypes.c_size_t, _p]),
-    "nx_erosion_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
-    "nx_erosion_store": (_i32, [_p, _p, _i64, _p, _p, _p, _p, _p]),
+    "nx_erosion_load": (_i32, [_p, _p, _p, _i64, _p, _p, ctypes.c_size_t, _p]),
+    "nx_erosion_steps": (_i32, [_p, _p, _i64, _p, _p, _i32, ctypes.c_float, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "nx_erosion_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "nx_erosion_store": (_i32, [_p, _i64, _p, _p, _p, _p, _p]),
     "nx_steepest_descent": (_i32, [_p, _p, _i64, _p, _p, _p]),
     "nx_insolation_plan": (_i32, [_p, _i32, _p, _i32, _p, _p, _p]),
     "nx_insolation": (_i32, [_p, _i64, _d, _p, _i32, _i32, _i32, _p, _i32, _p]),

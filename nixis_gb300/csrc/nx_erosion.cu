@@ -1,9 +1,14 @@
 // nx_erosion.cu -- erosion variant 3 (erosion.py:172-279) for sm_103a.
 //
-// State per vertex: (h, w) as float2 and s as float, binary32, double
-// buffered (the reference reads old arrays and writes copies, erosion.py:
-// 199-201, 274-277).  Neighbour slots are the reference's (n,6) int32 table;
-// edge lengths are precomputed per slot in binary64 and rounded.
+// State per vertex: float4 (h_hi, h_lo, w, s), double buffered (the
+// reference reads old arrays and writes copies, erosion.py:199-201,
+// 274-277).  Water and sediment are binary32; the height is an unevaluated
+// pair hi + lo of binary32s (about 48 significant bits) so that the small
+// per-iteration height changes the binary64 reference makes (1e-8 m on
+// heights of 1e3 m in early iterations) are kept, and the sign of
+// h_n - h_i -- the flow choice -- follows binary64 instead of tying.
+// Neighbour slots are the reference's (n,6) int32 table; edge lengths are
+// precomputed per slot in binary64 and rounded.
 //
 // Overflow: under the reference's update, water and sediment grow about 2x
 // per iteration, past binary32's range after ~140 iterations.  The update is
@@ -53,16 +58,25 @@ struct StepArgs {
     int t;
     const int32_t *nbr;
     const float *el;
-    float2 *hw0;
-    float *s0;
-    float2 *hw1;
-    float *s1;
+    float4 *st0;
+    float4 *st1;
     nx_erosion_ctl *ctl;
     double *partials;      // [gridDim.x][3] (mass sums only)
     double *mass;          // [iteration][planet][3] or null
     int mass_np;           // planets per mass row
     uint16_t *flow;        // optional: per vertex 2 bits per slot (1: neighbour higher, 2: lower)
 };
+
+// (hi, lo) + b with b binary32: two-sum, then renormalise (no FMA).
+__device__ __forceinline__ void df_add(float &hi, float &lo, float b)
+{
+    float s = __fadd_rn(hi, b);
+    float bb = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    e = __fadd_rn(e, lo);
+    hi = __fadd_rn(s, e);
+    lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
 
 __device__ __forceinline__ int find_planet(const nx_erosion_planet *P, int np, int64_t v)
 {
@@ -115,22 +129,20 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
     const int p = s_p;
     const nx_erosion_planet P = a.planets[p];
     const float lam = s_lam, rain = s_rain;
-    // buffers: read B[(iters - t) & 1], write the other; B[0] = (hw0, s0)
+    // buffers: read B[(iters - t) & 1], write the other; B[0] = st0
     const bool par = ((P.iters - a.t) & 1) != 0;
-    const float2 *__restrict__ ihw = par ? a.hw1 : a.hw0;
-    const float *__restrict__ is = par ? a.s1 : a.s0;
-    float2 *__restrict__ ohw = par ? a.hw0 : a.hw1;
-    float *__restrict__ os = par ? a.s0 : a.s1;
+    const float4 *__restrict__ ist = par ? a.st1 : a.st0;
+    float4 *__restrict__ ost = par ? a.st0 : a.st1;
 
     const int64_t i = vblk + threadIdx.x;
     float vmax = 0.0f;
     double sh = 0.0, sw = 0.0, ss = 0.0;
     if (i < P.vend) {
         const float sol = c_sol, evap = c_evap, cap = c_cap;
-        float2 hwi = ihw[i];
-        const float hi = __fmul_rn(hwi.x, lam);
-        const float wi = __fadd_rn(__fmul_rn(hwi.y, lam), rain);
-        const float si = __fmul_rn(is[i], lam);
+        const float4 me = ist[i];
+        const float hh = __fmul_rn(me.x, lam), hl = __fmul_rn(me.y, lam);
+        const float wi = __fadd_rn(__fmul_rn(me.z, lam), rain);
+        const float si = __fmul_rn(me.w, lam);
         float sed = si, wat = wi;
         const int2 *nb2 = reinterpret_cast<const int2 *>(a.nbr + 6 * i);
         const float2 *el2 = reinterpret_cast<const float2 *>(a.el + 6 * i);
@@ -147,10 +159,10 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
                 a.ctl[p].err = 1;
                 continue;
             }
-            float2 hwj = ihw[j];
-            float hj = __fmul_rn(hwj.x, lam);
-            float wj = __fadd_rn(__fmul_rn(hwj.y, lam), rain);
-            float diff = __fsub_rn(hj, hi);     // sign of the slope (erosion.py:230)
+            float4 o = ist[j];
+            float wj = __fadd_rn(__fmul_rn(o.z, lam), rain);
+            // sign of the slope (erosion.py:230): sign of h_j - h_i
+            float diff = __fadd_rn(__fsub_rn(__fmul_rn(o.x, lam), hh), __fsub_rn(__fmul_rn(o.y, lam), hl));
             if (diff > 0.0f) {
                 sed = __fadd_rn(sed, __fmul_rn(sol, wj));
                 wat = __fadd_rn(wat, __fmul_rn(wj, dd[k]));
@@ -162,20 +174,20 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
             }
         }
         // erosion.py:262-267
-        float hn = __fsub_rn(hi, sed);
+        float nh = hh, nl = hl;
+        df_add(nh, nl, -sed);
         float sn = __fadd_rn(si, sed);
         float wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, evap)));
         float cw = __fmul_rn(cap, wn);
         if (sn > cw) {
             float ex = __fsub_rn(sn, cw);
-            hn = __fadd_rn(hn, ex);
+            df_add(nh, nl, ex);
             sn = __fsub_rn(sn, ex);
         }
-        ohw[i] = make_float2(hn, wn);
-        os[i] = sn;
+        ost[i] = make_float4(nh, nl, wn, sn);
         if (a.flow) a.flow[i] = (uint16_t)flow;
-        vmax = fmaxf(fabsf(hn), fmaxf(fabsf(wn), fabsf(sn)));
-        if (a.mass) { sh = (double)hn; sw = (double)wn; ss = (double)sn; }
+        vmax = fmaxf(fabsf(nh), fmaxf(fabsf(wn), fabsf(sn)));
+        if (a.mass) { sh = (double)nh + (double)nl; sw = (double)wn; ss = (double)sn; }
     }
     // block max -> planet max for the next iteration's rescale decision
     vmax = warp_max(vmax);
@@ -277,17 +289,18 @@ __global__ void erosion_maxabs64_kernel(const double *__restrict__ h, const doub
 
 __global__ void erosion_load64_kernel(const double *__restrict__ h, const double *__restrict__ w,
                                       const double *__restrict__ s, int64_t n, const unsigned long long *__restrict__ mbits,
-                                      float2 *__restrict__ hw, float *__restrict__ so, nx_erosion_ctl *__restrict__ ctl)
+                                      float4 *__restrict__ st, nx_erosion_ctl *__restrict__ ctl)
 {
     double m = __longlong_as_double((long long)*mbits);
     int K = 0;
     if (m > 0x1p64) K = ilogb(m) - 64;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float hv = (float)ldexp(h[i], -K);
+        double hv = ldexp(h[i], -K);
+        float hh = (float)hv;
+        float hl = (float)(hv - (double)hh);
         float wv = w ? (float)ldexp(w[i], -K) : 0.0f;
         float sv = s ? (float)ldexp(s[i], -K) : 0.0f;
-        hw[i] = make_float2(hv, wv);
-        so[i] = sv;
+        st[i] = make_float4(hh, hl, wv, sv);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         float mf = (float)ldexp(m, -K);
@@ -301,16 +314,15 @@ __global__ void erosion_load64_kernel(const double *__restrict__ h, const double
     }
 }
 
-__global__ void erosion_store64_kernel(const float2 *__restrict__ hw, const float *__restrict__ s, int64_t n,
-                                       const nx_erosion_ctl *__restrict__ ctl, double *__restrict__ h,
-                                       double *__restrict__ w, double *__restrict__ so)
+__global__ void erosion_store64_kernel(const float4 *__restrict__ st, int64_t n, const nx_erosion_ctl *__restrict__ ctl,
+                                       double *__restrict__ h, double *__restrict__ w, double *__restrict__ so)
 {
     const int K = ctl->K[0];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float2 v = hw[i];
-        h[i] = ldexp((double)v.x, K);
-        if (w) w[i] = ldexp((double)v.y, K);
-        if (so) so[i] = ldexp((double)s[i], K);
+        float4 v = st[i];
+        h[i] = ldexp((double)v.x + (double)v.y, K);
+        if (w) w[i] = ldexp((double)v.z, K);
+        if (so) so[i] = ldexp((double)v.w, K);
     }
 }
 
@@ -372,10 +384,10 @@ Workspace carve(void *ws, int np)
 }  // namespace
 
 NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, const double *s64_dev, int64_t n,
-                              float *hw_dev, float *s_dev, void *workspace, size_t ws_bytes, void *stream)
+                              float *st_dev, void *workspace, size_t ws_bytes, void *stream)
 {
     if (n <= 0) return nx::fail(NX_EINVAL, "nx_erosion_load: n must be > 0");
-    if (!h64_dev || !hw_dev || !s_dev || !workspace) return nx::fail(NX_EINVAL, "nx_erosion_load: null pointer");
+    if (!h64_dev || !st_dev || !workspace) return nx::fail(NX_EINVAL, "nx_erosion_load: null pointer");
     if (ws_bytes < nx_erosion_workspace_size(n, 1)) return nx::fail(NX_EINVAL, "nx_erosion_load: workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
     Workspace w = carve(workspace, 1);
@@ -383,19 +395,18 @@ NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, cons
     NX_CHECK_CUDA(cudaMemsetAsync(mb, 0, sizeof(unsigned long long), s));
     erosion_maxabs64_kernel<<<grid1d(n), 256, 0, s>>>(h64_dev, w64_dev, s64_dev, n, mb);
     NX_CHECK_LAUNCH("erosion_maxabs64_kernel");
-    erosion_load64_kernel<<<grid1d(n), 256, 0, s>>>(h64_dev, w64_dev, s64_dev, n, mb, (float2 *)hw_dev, s_dev, w.ctl);
+    erosion_load64_kernel<<<grid1d(n), 256, 0, s>>>(h64_dev, w64_dev, s64_dev, n, mb, (float4 *)st_dev, w.ctl);
     NX_CHECK_LAUNCH("erosion_load64_kernel");
     nx::note_launch(2);
     return NX_OK;
 }
 
 static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
-                     const int32_t *nbr_dev, const float *edge_dev, float *hw_dev, float *s_dev, float *hw_tmp,
-                     float *s_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace, size_t ws_bytes,
-                     cudaStream_t s)
+                     const int32_t *nbr_dev, const float *edge_dev, float *st_dev, float *st_tmp, double *mass_dev,
+                     uint16_t *flow_dev, void *workspace, size_t ws_bytes, cudaStream_t s)
 {
     if (np <= 0) return NX_OK;
-    if (!planets_dev || !planets_host || !nbr_dev || !edge_dev || !hw_dev || !s_dev || !hw_tmp || !s_tmp || !workspace)
+    if (!planets_dev || !planets_host || !nbr_dev || !edge_dev || !st_dev || !st_tmp || !workspace)
         return nx::fail(NX_EINVAL, "erosion: null pointer");
     int max_it = 0;
     int64_t total = 0;
@@ -415,10 +426,8 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     a.np = np;
     a.nbr = nbr_dev;
     a.el = edge_dev;
-    a.hw0 = (float2 *)hw_dev;
-    a.s0 = s_dev;
-    a.hw1 = (float2 *)hw_tmp;
-    a.s1 = s_tmp;
+    a.st0 = (float4 *)st_dev;
+    a.st1 = (float4 *)st_tmp;
     a.ctl = w.ctl;
     a.partials = w.partials;
     a.mass = mass_dev;
@@ -443,10 +452,9 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     return NX_OK;
 }
 
-NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *hw_dev, float *s_dev,
-                               float *hw_tmp_dev, float *s_tmp_dev, int iters, float rain,
-                               const nx_erosion_planet *planet_dev, double *mass_dev, uint16_t *flow_dev,
-                               void *workspace, size_t ws_bytes, void *stream)
+NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *st_dev,
+                               float *st_tmp_dev, int iters, float rain, nx_erosion_planet *planet_dev,
+                               double *mass_dev, uint16_t *flow_dev, void *workspace, size_t ws_bytes, void *stream)
 {
     if (n <= 0 || iters < 0) return nx::fail(NX_EINVAL, "nx_erosion_steps: bad n or iters");
     if (!planet_dev) return nx::fail(NX_EINVAL, "nx_erosion_steps: planet descriptor (device) required");
@@ -456,23 +464,19 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
     P.iters = iters;
     P.rain = rain;
     cudaStream_t s = (cudaStream_t)stream;
-    NX_CHECK_CUDA(cudaMemcpyAsync((void *)planet_dev, &P, sizeof(P), cudaMemcpyHostToDevice, s));
-    // state enters in buffer 0; with an odd count the first iteration must read buffer 1
-    if (iters & 1) {
-        NX_CHECK_CUDA(cudaMemcpyAsync(hw_tmp_dev, hw_dev, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-        NX_CHECK_CUDA(cudaMemcpyAsync(s_tmp_dev, s_dev, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    }
-    return run_batch(planet_dev, &P, 1, nbr_dev, edge_dev, hw_dev, s_dev, hw_tmp_dev, s_tmp_dev, mass_dev, flow_dev,
-                     workspace, ws_bytes, s);
+    NX_CHECK_CUDA(cudaMemcpyAsync(planet_dev, &P, sizeof(P), cudaMemcpyHostToDevice, s));
+    // state enters in buffer 0; with an odd count the first iteration reads buffer 1
+    if (iters & 1)
+        NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp_dev, st_dev, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    return run_batch(planet_dev, &P, 1, nbr_dev, edge_dev, st_dev, st_tmp_dev, mass_dev, flow_dev, workspace, ws_bytes, s);
 }
 
 NX_EXPORT int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
-                               const int32_t *nbr_dev, const float *edge_dev, float *hw_dev, float *s_dev,
-                               float *hw_tmp_dev, float *s_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes,
-                               void *stream)
+                               const int32_t *nbr_dev, const float *edge_dev, float *st_dev, float *st_tmp_dev,
+                               double *mass_dev, void *workspace, size_t ws_bytes, void *stream)
 {
-    return run_batch(planets_dev, planets_host, nplanets, nbr_dev, edge_dev, hw_dev, s_dev, hw_tmp_dev, s_tmp_dev,
-                     mass_dev, nullptr, workspace, ws_bytes, (cudaStream_t)stream);
+    return run_batch(planets_dev, planets_host, nplanets, nbr_dev, edge_dev, st_dev, st_tmp_dev, mass_dev, nullptr,
+                     workspace, ws_bytes, (cudaStream_t)stream);
 }
 
 NX_EXPORT int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream)
@@ -483,18 +487,17 @@ NX_EXPORT int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets
     return NX_OK;
 }
 
-NX_EXPORT int nx_erosion_store(const float *hw_dev, const float *s_dev, int64_t n, const void *workspace,
-                               double *h64_dev, double *w64_dev, double *s64_dev, void *stream)
+NX_EXPORT int nx_erosion_store(const float *st_dev, int64_t n, const void *workspace, double *h64_dev, double *w64_dev,
+                               double *s64_dev, void *stream)
 {
-    if (n <= 0 || !hw_dev || !s_dev || !workspace || !h64_dev) return nx::fail(NX_EINVAL, "nx_erosion_store: bad arguments");
+    if (n <= 0 || !st_dev || !workspace || !h64_dev) return nx::fail(NX_EINVAL, "nx_erosion_store: bad arguments");
     const nx_erosion_ctl *ctl = (const nx_erosion_ctl *)workspace;
-    erosion_store64_kernel<<<grid1d(n), 256, 0, (cudaStream_t)stream>>>((const float2 *)hw_dev, s_dev, n, ctl,
-                                                                         h64_dev, w64_dev, s64_dev);
+    erosion_store64_kernel<<<grid1d(n), 256, 0, (cudaStream_t)stream>>>((const float4 *)st_dev, n, ctl, h64_dev, w64_dev,
+                                                                         s64_dev);
     NX_CHECK_LAUNCH("erosion_store64_kernel");
     nx::note_launch(1);
     return NX_OK;
 }
-
 NX_EXPORT int nx_steepest_descent(const int32_t *nbr_dev, const double *h_dev, int64_t n, int32_t *pos_dev,
                                   int32_t *vid_dev, void *stream)
 {

@@ -36,10 +36,8 @@ class ErosionRun:
                 raise IndexError("neighbors holds an id outside [-1, N)")
         self.edge = edge
         n = self.n
-        self.hw = torch.empty((n, 2), dtype=torch.float32, device="cuda")
-        self.s = torch.empty(n, dtype=torch.float32, device="cuda")
-        self.hw_tmp = torch.empty_like(self.hw)
-        self.s_tmp = torch.empty_like(self.s)
+        self.st = torch.empty((n, 4), dtype=torch.float32, device="cuda")    # (h_hi, h_lo, w, s)
+        self.st_tmp = torch.empty_like(self.st)
         self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
         self.planet = torch.zeros(4, dtype=torch.int64, device="cuda")   # one nx_erosion_planet (24 B)
         self.iters_done = 0
@@ -48,7 +46,7 @@ class ErosionRun:
         h = _dev.to_device(heights, np.float64, (self.n,), "heights")
         w = None if water is None else _dev.to_device(water, np.float64, (self.n,), "water")
         s = None if sediment is None else _dev.to_device(sediment, np.float64, (self.n,), "sediment")
-        call("nx_erosion_load", _dev.ptr(h), _dev.ptr(w), _dev.ptr(s), self.n, _dev.ptr(self.hw), _dev.ptr(self.s),
+        call("nx_erosion_load", _dev.ptr(h), _dev.ptr(w), _dev.ptr(s), self.n, _dev.ptr(self.st),
              _dev.ptr(self.ws), self.ws.numel(), _dev.stream_handle(self.stream))
         self.iters_done = 0
         return self
@@ -59,15 +57,15 @@ class ErosionRun:
         iters = int(iters)
         m = torch.empty((max(iters, 1), 3), dtype=torch.float64, device="cuda") if mass else None
         f = torch.zeros(self.n, dtype=torch.int16, device="cuda") if flow else None
-        call("nx_erosion_steps", _dev.ptr(self.nbr), _dev.ptr(self.edge), self.n, _dev.ptr(self.hw), _dev.ptr(self.s),
-             _dev.ptr(self.hw_tmp), _dev.ptr(self.s_tmp), iters, float(rain), _dev.ptr(self.planet), _dev.ptr(m),
-             _dev.ptr(f), _dev.ptr(self.ws), self.ws.numel(), _dev.stream_handle(self.stream))
+        call("nx_erosion_steps", _dev.ptr(self.nbr), _dev.ptr(self.edge), self.n, _dev.ptr(self.st),
+             _dev.ptr(self.st_tmp), iters, float(rain), _dev.ptr(self.planet), _dev.ptr(m), _dev.ptr(f),
+             _dev.ptr(self.ws), self.ws.numel(), _dev.stream_handle(self.stream))
         self.iters_done += iters
         return (m[:iters] if mass else None), f
 
     def store(self, heights, water=None, sediment=None):
         """Write the state as float64 true values into the given CUDA tensors."""
-        call("nx_erosion_store", _dev.ptr(self.hw), _dev.ptr(self.s), self.n, _dev.ptr(self.ws),
+        call("nx_erosion_store", _dev.ptr(self.st), self.n, _dev.ptr(self.ws),
              _dev.ptr(heights), _dev.ptr(water), _dev.ptr(sediment), _dev.stream_handle(self.stream))
 
     def scale_exponent(self):

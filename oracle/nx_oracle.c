@@ -447,39 +447,52 @@ NXO_API int nxo_erode_terrain3(const double *xyz, const int32_t *nbr, int64_t n,
 }
 
 /*
- * The same update evaluated in binary32, with the edge length supplied per
- * neighbour slot (edge_len[6*i+k], computed once in binary64 and rounded).
- * Used to check the GPU kernel operation for operation; `scale_exp` applies
- * a power-of-two rescale to the inputs first (exact in binary32 without
- * overflow/underflow), which is how the GPU keeps the exploding state finite.
+ * The same update evaluated with the GPU kernel's arithmetic: water and
+ * sediment in binary32, the height as an unevaluated pair hi + lo of
+ * binary32s, the slope sign taken from (hj_hi - hi_hi) + (hj_lo - hi_lo),
+ * and the edge length supplied per neighbour slot (edge_len[6*i+k],
+ * computed once in binary64 and rounded).  State rows are (h_hi, h_lo, w, s).
+ * Used to check the kernel operation for operation (bit for bit).
  */
+static void df_add(float *hi, float *lo, float b)
+{
+    float s = *hi + b;
+    float bb = s - *hi;
+    float e = (*hi - (s - bb)) + (b - bb);
+    e = e + *lo;
+    float h2 = s + e;
+    *lo = e - (h2 - s);
+    *hi = h2;
+}
+
 NXO_API void nxo_erosion_iteration3_f32(const float *edge_len, const int32_t *nbr, int64_t n,
-                                        const float *h, const float *w, const float *s,
-                                        float *ho, float *wo, float *so)
+                                        const float *st, float *out)
 {
     const float sol = (float)SOLUBILITY, evap = (float)EVAPORATION, cap = (float)CAPACITY;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
-        float self = h[i];
-        float sed_amt = s[i], wat_amt = w[i];
+        const float hh = st[4 * i], hl = st[4 * i + 1], wi = st[4 * i + 2], si = st[4 * i + 3];
+        float sed_amt = si, wat_amt = wi;
         for (int k = 0; k < 6; ++k) {
             int32_t j = nbr[6 * i + k];
             if (j == -1) continue;
             float d = edge_len[6 * i + k];
-            float diff = h[j] - self;       /* sign of slope = sign of difference */
-            if (diff > 0) { sed_amt += sol * w[j]; wat_amt += w[j] * d; }
-            else if (diff < 0) { sed_amt -= sol * w[j]; wat_amt -= w[j] * d; }
+            const float *o = st + 4 * (int64_t)j;
+            float diff = (o[0] - hh) + (o[1] - hl);
+            if (diff > 0) { sed_amt += sol * o[2]; wat_amt += o[2] * d; }
+            else if (diff < 0) { sed_amt -= sol * o[2]; wat_amt -= o[2] * d; }
         }
-        float hn = h[i] - sed_amt;
-        float sn = s[i] + sed_amt;
-        float wn = w[i] + (wat_amt - wat_amt * evap);
+        float nh = hh, nl = hl;
+        df_add(&nh, &nl, -sed_amt);
+        float sn = si + sed_amt;
+        float wn = wi + (wat_amt - wat_amt * evap);
         float cw = cap * wn;
         if (sn > cw) {
             float ex = sn - cw;
-            hn += ex;
+            df_add(&nh, &nl, ex);
             sn -= ex;
         }
-        ho[i] = hn; so[i] = sn; wo[i] = wn;
+        out[4 * i] = nh; out[4 * i + 1] = nl; out[4 * i + 2] = wn; out[4 * i + 3] = sn;
     }
 }
 

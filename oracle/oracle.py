@@ -46,7 +46,7 @@ def lib():
             "nxo_make_bool_elevation_mask": (None, [_p, _i64, _d, _p]),
             "nxo_erosion_iteration3": (_i32, [_p, _p, _i64, _p, _p, _p]),
             "nxo_erode_terrain3": (_i32, [_p, _p, _i64, _p, _i32]),
-            "nxo_erosion_iteration3_f32": (None, [_p, _p, _i64, _p, _p, _p, _p, _p, _p]),
+            "nxo_erosion_iteration3_f32": (None, [_p, _p, _i64, _p, _p]),
             "nxo_find_lowest": (_i32, [_i64, _p, _p]),
             "nxo_day2deg": (_d, [_d, _d]),
             "nxo_calculate_seasonal_tilt": (_d, [_d, _d]),
@@ -150,17 +150,23 @@ def erode_terrain3(nodes, neighbors, heights, num_iter=1):
         raise MemoryError("oracle erode_terrain3: allocation failed")
 
 
-def erosion_iteration3_f32(edge_len, neighbors, h, w, s):
-    """The update in binary32 with per-slot edge lengths; returns new (h, w, s)."""
+def erosion_iteration3_f32(edge_len, neighbors, st):
+    """The update with the GPU kernel's arithmetic on rows (h_hi, h_lo, w, s)
+    (float32 (N,4)); returns the new rows."""
     el = _c(edge_len, np.float32)
     nbr = _c(neighbors, np.int32)
-    h = _c(h, np.float32)
-    w = _c(w, np.float32)
-    s = _c(s, np.float32)
-    ho, wo, so = np.empty_like(h), np.empty_like(w), np.empty_like(s)
-    lib().nxo_erosion_iteration3_f32(_ptr(el), _ptr(nbr), len(nbr), _ptr(h), _ptr(w), _ptr(s),
-                                     _ptr(ho), _ptr(wo), _ptr(so))
-    return ho, wo, so
+    st = _c(st, np.float32)
+    out = np.empty_like(st)
+    lib().nxo_erosion_iteration3_f32(_ptr(el), _ptr(nbr), len(nbr), _ptr(st), _ptr(out))
+    return out
+
+
+def split_heights(h):
+    """float64 heights -> (h_hi, h_lo) float32 pairs, as the GPU loads them."""
+    h = np.asarray(h, np.float64)
+    hi = h.astype(np.float32)
+    lo = (h - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo
 
 
 def find_lowest(vert, nbr6, height):

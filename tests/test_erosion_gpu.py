@@ -1,9 +1,9 @@
 """GPU erosion (variant 3) against the oracle and the reference's goldens.
 
-* binary32 step: bit-exact against the oracle's binary32 restatement of
-  erosion_iteration3 (same operation order), for 1 and 50 iterations;
+* kernel arithmetic (binary32 water and sediment, height as a binary32
+  pair): bit-exact against the oracle's restatement, 1 and 50 iterations;
 * flow choice (sign of h_n - h_i per slot): bit-exact against the binary64
-  reference on binary32-representable inputs;
+  reference on the same input heights;
 * trajectories against the binary64 reference: max|err| / max|field| <=
   ERO_TOL at 1, 10 and 50 iterations (stated tolerance);
 * the power-of-two rescale is exact (scaling inputs by 2^100 scales
@@ -51,37 +51,41 @@ def test_edge_lengths_match_mirror():
         assert np.array_equal(el.cpu().numpy(), meshref.edge_lengths(pts, adj))
 
 
-@pytest.mark.parametrize("k", [6, 12])
-def test_binary32_steps_bit_exact_and_flow_choice(k):
-    g, pts, adj = golden_case(k)
-    h0 = g[f"ero_k{k}_f32_h0"].astype(np.float32)
-    w0 = g[f"ero_k{k}_f32_w0"].astype(np.float32)
-    s0 = np.zeros_like(h0)
-    el = meshref.edge_lengths(pts, adj)
-    # one step + flow bits
-    h1, w1, s1, _, flow, _ = run_gpu(pts, adj, h0, w0, s0, 1, flow=True)
-    ho, wo, so = O.erosion_iteration3_f32(el, adj, h0, w0, s0)
-    assert np.array_equal(h1, ho.astype(np.float64))
-    assert np.array_equal(w1, wo.astype(np.float64))
-    assert np.array_equal(s1, so.astype(np.float64))
-    # flow choice equals the binary64 reference's slope sign on the same inputs
-    hh = h0.astype(np.float64)
-    f = flow.cpu().numpy().astype(np.int64) & 0xFFFF
+def flow_codes(adj, h):
+    """Per slot: 1 if the neighbour is higher, 2 if lower, 0 if equal or -1
+    (the reference's slope > 0 / < 0 / == 0 branches, erosion.py:238-247)."""
+    out = np.zeros(len(adj), np.int64)
     for slot in range(6):
         j = adj[:, slot]
-        code = (f >> (2 * slot)) & 3
         ok = j >= 0
-        d = np.where(ok, hh[np.where(ok, j, 0)] - hh, 0.0)
-        want = np.where(~ok, 0, np.where(d > 0, 1, np.where(d < 0, 2, 0)))
-        assert np.array_equal(code, want), slot
-    # 50 steps, still bit-exact against the binary32 restatement
-    hG, wG, sG, _, _, _ = run_gpu(pts, adj, h0, w0, s0, 50)
-    h, w, s = h0, w0, s0
+        d = np.where(ok, h[np.where(ok, j, 0)] - h, 0.0)
+        code = np.where(~ok, 0, np.where(d > 0, 1, np.where(d < 0, 2, 0)))
+        out |= code << (2 * slot)
+    return out
+
+
+@pytest.mark.parametrize("k", [6, 12])
+@pytest.mark.parametrize("variant", ["f32", "smooth", "terraced"])
+def test_kernel_arithmetic_bit_exact_and_flow_choice(k, variant):
+    g, pts, adj = golden_case(k)
+    h0 = g[f"ero_k{k}_{variant}_h0"]
+    w0 = g[f"ero_k{k}_{variant}_w0"]
+    s0 = np.zeros_like(h0)
+    el = meshref.edge_lengths(pts, adj)
+    hi, lo = O.split_heights(h0)
+    st0 = np.stack([hi, lo, w0.astype(np.float32), s0.astype(np.float32)], axis=1)
+    # one step + flow bits: state rows identical to the oracle's restatement
+    _, _, _, _, flow, run = run_gpu(pts, adj, h0, w0, s0, 1, flow=True)
+    assert np.array_equal(run.st.cpu().numpy(), O.erosion_iteration3_f32(el, adj, st0))
+    # flow choice equals the binary64 reference's slope sign on the same heights
+    f = flow.cpu().numpy().astype(np.int64) & 0xFFFF
+    assert np.array_equal(f, flow_codes(adj, h0))
+    # 50 steps, still bit-exact
+    _, _, _, _, _, run = run_gpu(pts, adj, h0, w0, s0, 50)
+    st = st0
     for _ in range(50):
-        h, w, s = O.erosion_iteration3_f32(el, adj, h, w, s)
-    assert np.array_equal(hG, h.astype(np.float64))
-    assert np.array_equal(wG, w.astype(np.float64))
-    assert np.array_equal(sG, s.astype(np.float64))
+        st = O.erosion_iteration3_f32(el, adj, st)
+    assert np.array_equal(run.st.cpu().numpy(), st)
 
 
 def rel_err(got, ref):
@@ -187,28 +191,22 @@ def test_batched_planets_equal_planets_alone():
     nbr = torch.from_numpy(np.concatenate(nbrs)).cuda()
     el = torch.from_numpy(np.concatenate(els)).cuda()
     hall = np.concatenate(hs).astype(np.float32)
-    hw = torch.zeros((N, 2), dtype=torch.float32, device="cuda")
-    s = torch.zeros(N, dtype=torch.float32, device="cuda")
-    hw_t, s_t = torch.zeros_like(hw), torch.zeros_like(s)
+    st = torch.zeros((N, 4), dtype=torch.float32, device="cuda")
+    st_t = torch.zeros_like(st)
     for (b, e, iters) in descs:
-        dst_hw = hw_t if iters & 1 else hw
-        dst_hw[b:e, 0] = torch.from_numpy(hall[b:e]).cuda()
-        dst_hw[b:e, 1] = 1e-3
+        dst = st_t if iters & 1 else st
+        dst[b:e, 0] = torch.from_numpy(hall[b:e]).cuda()
+        dst[b:e, 2] = 1e-3
     arr = (_lib.ErosionPlanet * len(descs))(*[_lib.ErosionPlanet(b, e, it, 0.0) for b, e, it in descs])
     pd = torch.from_numpy(np.frombuffer(bytes(arr), np.uint8).copy()).cuda()
     ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(N, len(descs))), dtype=torch.uint8, device="cuda")
-    st = _dev.stream_handle()
-    _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), len(descs), st)
+    _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), len(descs), _dev.stream_handle())
     _lib.call("nx_erosion_batch", _dev.ptr(pd), ctypes.cast(arr, ctypes.c_void_p), len(descs), _dev.ptr(nbr),
-              _dev.ptr(el), _dev.ptr(hw), _dev.ptr(s), _dev.ptr(hw_t), _dev.ptr(s_t), None, _dev.ptr(ws),
-              ws.numel(), st)
-    out_hw = hw.cpu().numpy()
-    out_s = s.cpu().numpy()
+              _dev.ptr(el), _dev.ptr(st), _dev.ptr(st_t), None, _dev.ptr(ws), ws.numel(), _dev.stream_handle())
+    out = st.cpu().numpy()
     for (p, adj, h, iters), (b, e, _) in zip(planets, descs):
-        ha, wa, sa, _, _, _ = run_gpu(p, adj, h, np.full(len(p), np.float32(1e-3)), np.zeros(len(p)), iters)
-        assert np.array_equal(out_hw[b:e, 0].astype(np.float64), ha)
-        assert np.array_equal(out_hw[b:e, 1].astype(np.float64), wa)
-        assert np.array_equal(out_s[b:e].astype(np.float64), sa)
+        _, _, _, _, _, run = run_gpu(p, adj, h, np.full(len(p), np.float32(1e-3)), np.zeros(len(p)), iters)
+        assert np.array_equal(out[b:e], run.st.cpu().numpy())
 
 
 def test_bad_neighbour_id_is_reported_not_faulted():
