@@ -96,6 +96,36 @@ int nx_noise3d_trace(const double *xyz_dev, int64_t n, const int32_t *perm_dev,
                      int32_t *slots_dev, unsigned long long *n_fallback_dev, void *stream);
 
 
+/* One planet of a batched fBm launch (device-resident array of these). */
+typedef struct nx_fbm_planet {
+    const double *xyz;      /* (n,3) float64 vertices (its mesh) */
+    int64_t n;
+    const int32_t *perm;    /* device int32[256] tables of its seed */
+    const int32_t *pgi;
+    float *out;             /* n binary32 sums over octaves */
+    uint32_t *minmax;       /* optional: 2 ordered keys, caller sets {0xFFFFFFFF, 0}; */
+                            /* key(f) = f >= 0 ? bits ^ 0x80000000 : ~bits        */
+    int32_t n_octaves;
+    int32_t chunk0;         /* index of its first chunk: sum of ceil(n/chunk) of earlier planets */
+    float s_hi[NX_MAX_OCTAVES];   /* filled by nx_fbm_planet_fill */
+    float s_lo[NX_MAX_OCTAVES];
+    float amp[NX_MAX_OCTAVES];
+    double s[NX_MAX_OCTAVES];
+} nx_fbm_planet;
+
+/* Host: fill a planet's octave constants (same meaning as nx_fbm). */
+int nx_fbm_planet_fill(nx_fbm_planet *planet, int n_octaves, const double *scale, const double *strength,
+                       double radius);
+
+/* Vertices per work item of nx_fbm_batch (for chunk0). */
+int nx_fbm_chunk_size(void);
+
+/* fBm of many planets (uneven sizes, seeds, octave counts) in one
+ * persistent launch; planets_dev/planets_host: the same array on device
+ * and host. */
+int nx_fbm_batch(const nx_fbm_planet *planets_dev, const nx_fbm_planet *planets_host, int nplanets,
+                 unsigned long long *n_fallback_dev, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Mesh: icosphere, adjacency, edge lengths                            */
 /* ------------------------------------------------------------------ */
@@ -135,14 +165,18 @@ int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, f
 /* Erosion (variant 3)                                                 */
 /* ------------------------------------------------------------------ */
 
-/* One planet's range in a packed batch.  vbeg must be a multiple of 256;
- * planets are packed in order of non-increasing `iters`.  `rain` is added
- * to every water value before each iteration (erode_terrain3 adds 0.3/320,
- * erosion.py:182-183; 0 gives bare erosion_iteration3 steps).  Neighbour
- * ids in a batch are global (packed) indices. */
+/* One planet of an erosion batch.  Its state occupies rows [vbeg, vbeg+n)
+ * of the packed state buffers (vbeg a multiple of 256); nbr (n,6) local
+ * neighbour ids and edge (n,6) per-slot lengths are its mesh (device
+ * pointers, shared by planets of equal divisions).  Planets are packed in
+ * order of non-increasing `iters`.  `rain` is added to every water value
+ * before each iteration (erode_terrain3 adds 0.3/320, erosion.py:182-183;
+ * 0 gives bare erosion_iteration3 steps). */
 typedef struct nx_erosion_planet {
     int64_t vbeg;
-    int64_t vend;
+    int64_t n;
+    const int32_t *nbr;
+    const float *edge;
     int32_t iters;
     float rain;
 } nx_erosion_planet;
@@ -181,8 +215,8 @@ int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, f
  * mass_dev (optional): float64[max_iters][nplanets][3].  Call
  * nx_erosion_ctl_init first. */
 int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
-                     const int32_t *nbr_dev, const float *edge_dev, float *st_dev, float *st_tmp_dev,
-                     double *mass_dev, void *workspace, size_t ws_bytes, void *stream);
+                     float *st_dev, float *st_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes,
+                     void *stream);
 
 /* Write one planet's state back as binary64 true values (h_hi + h_lo, w, s
  * times 2^K, K from the workspace's first control block).  w64_dev /
@@ -201,6 +235,19 @@ typedef struct nx_erosion_ctl {
     int32_t err;
     int32_t pad;
 } nx_erosion_ctl;
+
+/* Initial state of a batch from raw fBm sums (nx_fbm_batch output rows
+ * and min/max keys, 2 per planet): h = util.rescale(raw, elev_lo, elev_hi)
+ * (util.py:110-140), w = water0, s = 0, written to buffer (iters & 1). */
+int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                          int nplanets, const float *raw_dev, const uint32_t *minmax_dev, float elev_lo,
+                          float elev_hi, float water0, float *st_dev, float *st_tmp_dev, void *stream);
+
+/* Heights of every planet of a finished batch into out_dev (packed rows):
+ * (h_hi + h_lo) * 2^K, binary32. */
+int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                             int nplanets, const float *st_dev, const void *workspace, float *out_dev,
+                             void *stream);
 
 /* erosion.find_lowest (erosion.py:398-406) for every vertex: pos_dev gets
  * the position, among the neighbours that are not -1, of the first lowest
@@ -230,6 +277,20 @@ int nx_insolation_plan(const double *rot_deg, int n_rot, const double *tilt_deg,
  * a compensated total. */
 int nx_insolation(const double *xyz_dev, int64_t n, double radius, const float *table_dev, int n_rot_entries,
                   int pairs, int n_tilt, float *out_dev, int accumulate, void *stream);
+
+/* One planet of a batched insolation launch: its vertices and radius; its
+ * sums go to packed output rows [vbeg, vbeg + n) (vbeg a multiple of 256). */
+typedef struct nx_inso_planet {
+    const double *xyz;
+    int64_t n;
+    int64_t vbeg;
+    double radius;
+} nx_inso_planet;
+
+/* nx_insolation for many planets (same schedule) in one launch. */
+int nx_insolation_batch(const nx_inso_planet *planets_dev, const nx_inso_planet *planets_host, int nplanets,
+                        const float *table_dev, int n_rot_entries, int pairs, int n_tilt, float *out_dev,
+                        void *stream);
 
 #ifdef __cplusplus
 }

@@ -34,18 +34,42 @@ SIGNATURES = {
     "nx_erosion_ctl_init": (_i32, [_p, ctypes.c_size_t, _i32, _p]),
     "nx_erosion_load": (_i32, [_p, _p, _p, _i64, _p, _p, ctypes.c_size_t, _p]),
     "nx_erosion_steps": (_i32, [_p, _p, _i64, _p, _p, _i32, ctypes.c_float, _p, _p, _p, _p, ctypes.c_size_t, _p]),
-    "nx_erosion_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "nx_erosion_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "nx_erosion_store": (_i32, [_p, _i64, _p, _p, _p, _p, _p]),
     "nx_steepest_descent": (_i32, [_p, _p, _i64, _p, _p, _p]),
     "nx_insolation_plan": (_i32, [_p, _i32, _p, _i32, _p, _p, _p]),
     "nx_insolation": (_i32, [_p, _i64, _d, _p, _i32, _i32, _i32, _p, _i32, _p]),
+    "nx_insolation_batch": (_i32, [_p, _p, _i32, _p, _i32, _i32, _i32, _p, _p]),
+    "nx_fbm_planet_fill": (_i32, [_p, _i32, _p, _p, _d]),
+    "nx_fbm_chunk_size": (_i32, []),
+    "nx_fbm_batch": (_i32, [_p, _p, _i32, _p, _p]),
+    "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_float, _p, _p,
+                                     _p]),
+    "nx_erosion_heights_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p]),
 }
+
+NX_MAX_OCTAVES = 32
+
+
+class FbmPlanet(ctypes.Structure):
+    """nx_fbm_planet (include/nixis_gb300.h)."""
+    _fields_ = [("xyz", ctypes.c_void_p), ("n", ctypes.c_int64), ("perm", ctypes.c_void_p),
+                ("pgi", ctypes.c_void_p), ("out", ctypes.c_void_p), ("minmax", ctypes.c_void_p),
+                ("n_octaves", ctypes.c_int32), ("chunk0", ctypes.c_int32),
+                ("s_hi", ctypes.c_float * NX_MAX_OCTAVES), ("s_lo", ctypes.c_float * NX_MAX_OCTAVES),
+                ("amp", ctypes.c_float * NX_MAX_OCTAVES), ("s", ctypes.c_double * NX_MAX_OCTAVES)]
+
+
+class InsoPlanet(ctypes.Structure):
+    """nx_inso_planet (include/nixis_gb300.h)."""
+    _fields_ = [("xyz", ctypes.c_void_p), ("n", ctypes.c_int64), ("vbeg", ctypes.c_int64),
+                ("radius", ctypes.c_double)]
 
 
 class ErosionPlanet(ctypes.Structure):
     """nx_erosion_planet (include/nixis_gb300.h)."""
-    _fields_ = [("vbeg", ctypes.c_int64), ("vend", ctypes.c_int64), ("iters", ctypes.c_int32),
-                ("rain", ctypes.c_float)]
+    _fields_ = [("vbeg", ctypes.c_int64), ("n", ctypes.c_int64), ("nbr", ctypes.c_void_p),
+                ("edge", ctypes.c_void_p), ("iters", ctypes.c_int32), ("rain", ctypes.c_float)]
 
 _lock = threading.Lock()
 _LIB = None

@@ -56,8 +56,6 @@ struct StepArgs {
     const nx_erosion_planet *planets;
     int np;
     int t;
-    const int32_t *nbr;
-    const float *el;
     float4 *st0;
     float4 *st1;
     nx_erosion_ctl *ctl;
@@ -134,18 +132,19 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
     const float4 *__restrict__ ist = par ? a.st1 : a.st0;
     float4 *__restrict__ ost = par ? a.st0 : a.st1;
 
-    const int64_t i = vblk + threadIdx.x;
+    const int64_t i = vblk + threadIdx.x;       // packed state row
+    const int64_t li = i - P.vbeg;                // vertex id within the planet
     float vmax = 0.0f;
     double sh = 0.0, sw = 0.0, ss = 0.0;
-    if (i < P.vend) {
+    if (li < P.n) {
         const float sol = c_sol, evap = c_evap, cap = c_cap;
         const float4 me = ist[i];
         const float hh = __fmul_rn(me.x, lam), hl = __fmul_rn(me.y, lam);
         const float wi = __fadd_rn(__fmul_rn(me.z, lam), rain);
         const float si = __fmul_rn(me.w, lam);
         float sed = si, wat = wi;
-        const int2 *nb2 = reinterpret_cast<const int2 *>(a.nbr + 6 * i);
-        const float2 *el2 = reinterpret_cast<const float2 *>(a.el + 6 * i);
+        const int2 *nb2 = reinterpret_cast<const int2 *>(P.nbr + 6 * li);
+        const float2 *el2 = reinterpret_cast<const float2 *>(P.edge + 6 * li);
         int2 n01 = nb2[0], n23 = nb2[1], n45 = nb2[2];
         float2 d01 = el2[0], d23 = el2[1], d45 = el2[2];
         const int nbr[6] = {n01.x, n01.y, n23.x, n23.y, n45.x, n45.y};
@@ -155,11 +154,11 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
         for (int k = 0; k < 6; ++k) {
             int j = nbr[k];
             if (j < 0) continue;
-            if ((int64_t)j < P.vbeg || (int64_t)j >= P.vend) {
+            if ((int64_t)j >= P.n) {
                 a.ctl[p].err = 1;
                 continue;
             }
-            float4 o = ist[j];
+            float4 o = ist[P.vbeg + j];
             float wj = __fadd_rn(__fmul_rn(o.z, lam), rain);
             // sign of the slope (erosion.py:230): sign of h_j - h_i
             float diff = __fadd_rn(__fsub_rn(__fmul_rn(o.x, lam), hh), __fsub_rn(__fmul_rn(o.y, lam), hl));
@@ -210,7 +209,7 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
             double *pp = a.partials + 3 * (int64_t)blockIdx.x;
             pp[0] = t0; pp[1] = t1; pp[2] = t2;
             __threadfence();
-            int64_t nblk = (P.vend - P.vbeg + BLOCK - 1) / BLOCK;
+            int64_t nblk = (P.n + BLOCK - 1) / BLOCK;
             unsigned prev = atomicAdd(&a.ctl[p].done, 1u);
             s_last = (int64_t)prev + 1 == nblk;
         }
@@ -220,7 +219,7 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
         // last block of this planet: compensated (Neumaier) sum of the
         // planet's block partials in a fixed order, scaled by 2^K
         __threadfence();
-        const int64_t b0 = P.vbeg / BLOCK, nblk = (P.vend - P.vbeg + BLOCK - 1) / BLOCK;
+        const int64_t b0 = P.vbeg / BLOCK, nblk = (P.n + BLOCK - 1) / BLOCK;
         double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
         for (int64_t b = threadIdx.x; b < nblk; b += BLOCK) {
             const volatile double *pp = a.partials + 3 * (b0 + b);
@@ -326,6 +325,58 @@ __global__ void erosion_store64_kernel(const float4 *__restrict__ st, int64_t n,
     }
 }
 
+// Ordered key -> float (inverse of the fBm kernel's min/max keys).
+__device__ __forceinline__ float unkey(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k ^ 0x80000000u) : ~k);
+}
+
+__device__ __forceinline__ int block_planet(const nx_erosion_planet *P, int np, int64_t row)
+{
+    return find_planet(P, np, row);
+}
+
+// util.rescale (util.py:110-140) of the raw fBm sums to [lo, hi], and the
+// initial state (h, 0, water0, 0) in the buffer the planet's first
+// iteration reads: B[iters & 1].
+__global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_planet *__restrict__ P, int np,
+                                                           const float *__restrict__ raw,
+                                                           const uint32_t *__restrict__ minmax, float lo, float hi,
+                                                           float water0, float4 *__restrict__ st0,
+                                                           float4 *__restrict__ st1, int64_t total)
+{
+    for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
+        const int p = block_planet(P, np, blk * 256);
+        const int64_t row = blk * 256 + threadIdx.x;
+        const int64_t i = row - P[p].vbeg;
+        if (i < 0 || i >= P[p].n) continue;
+        const float mn = unkey(minmax[2 * p]), mx = unkey(minmax[2 * p + 1]);
+        const float range = __fsub_rn(mx, mn);
+        const float sc = __fdiv_rn(__fsub_rn(hi, lo), range);
+        // ((x - min) * ((hi - lo) / (max - min))) + lo, unfused
+        const float h = __fadd_rn(__fmul_rn(__fsub_rn(raw[row], mn), sc), lo);
+        float4 *dst = (P[p].iters & 1) ? st1 : st0;
+        dst[row] = make_float4(h, 0.0f, water0, 0.0f);
+    }
+}
+
+// Heights of every planet after its run: (h_hi + h_lo) * 2^K, summed in
+// binary64 and rounded once to binary32.
+__global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_planet *__restrict__ P, int np,
+                                                              const float4 *__restrict__ st,
+                                                              const nx_erosion_ctl *__restrict__ ctl,
+                                                              float *__restrict__ out, int64_t total)
+{
+    for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
+        const int p = block_planet(P, np, blk * 256);
+        const int64_t row = blk * 256 + threadIdx.x;
+        const int64_t i = row - P[p].vbeg;
+        if (i < 0 || i >= P[p].n) continue;
+        float4 v = st[row];
+        out[row] = (float)ldexp((double)v.x + (double)v.y, ctl[p].K[0]);
+    }
+}
+
 // find_lowest (erosion.py:398-406, util.py:580-587): position, within the
 // neighbours that are not -1, of the first lowest one if it is strictly
 // lower than the vertex, else -1; `vid` gets that neighbour's id (or -1).
@@ -402,30 +453,29 @@ NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, cons
 }
 
 static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
-                     const int32_t *nbr_dev, const float *edge_dev, float *st_dev, float *st_tmp, double *mass_dev,
-                     uint16_t *flow_dev, void *workspace, size_t ws_bytes, cudaStream_t s)
+                     float *st_dev, float *st_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace,
+                     size_t ws_bytes, cudaStream_t s)
 {
     if (np <= 0) return NX_OK;
-    if (!planets_dev || !planets_host || !nbr_dev || !edge_dev || !st_dev || !st_tmp || !workspace)
+    if (!planets_dev || !planets_host || !st_dev || !st_tmp || !workspace)
         return nx::fail(NX_EINVAL, "erosion: null pointer");
     int max_it = 0;
     int64_t total = 0;
     for (int p = 0; p < np; ++p) {
         const nx_erosion_planet &P = planets_host[p];
-        if (P.vbeg % BLOCK != 0 || P.vend < P.vbeg || P.iters < 0)
-            return nx::fail(NX_EINVAL, "erosion: planet %d range must start at a multiple of %d", p, BLOCK);
-        if (p > 0 && (P.vbeg < planets_host[p - 1].vend || P.iters > planets_host[p - 1].iters))
+        if (P.vbeg % BLOCK != 0 || P.n < 0 || P.iters < 0)
+            return nx::fail(NX_EINVAL, "erosion: planet %d state rows must start at a multiple of %d", p, BLOCK);
+        if (P.n > 0 && (!P.nbr || !P.edge)) return nx::fail(NX_EINVAL, "erosion: planet %d has no mesh", p);
+        if (p > 0 && (P.vbeg < planets_host[p - 1].vbeg + planets_host[p - 1].n || P.iters > planets_host[p - 1].iters))
             return nx::fail(NX_EINVAL, "erosion: planets must be packed in order of descending iterations");
         if (P.iters > max_it) max_it = P.iters;
-        total = P.vend;
+        total = P.vbeg + P.n;
     }
     if (ws_bytes < nx_erosion_workspace_size(total, np)) return nx::fail(NX_EINVAL, "erosion: workspace too small");
     Workspace w = carve(workspace, np);
     StepArgs a;
     a.planets = planets_dev;
     a.np = np;
-    a.nbr = nbr_dev;
-    a.el = edge_dev;
     a.st0 = (float4 *)st_dev;
     a.st1 = (float4 *)st_tmp;
     a.ctl = w.ctl;
@@ -437,7 +487,7 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     for (int t = 0; t < max_it; ++t) {
         while (last >= 0 && planets_host[last].iters <= t) --last;
         if (last < 0) break;
-        int64_t end = planets_host[last].vend;
+        int64_t end = planets_host[last].vbeg + planets_host[last].n;
         int64_t nblk = (end + BLOCK - 1) / BLOCK;
         a.t = t;
         erosion_step_kernel<<<(unsigned)nblk, BLOCK, 0, s>>>(a);
@@ -460,7 +510,9 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
     if (!planet_dev) return nx::fail(NX_EINVAL, "nx_erosion_steps: planet descriptor (device) required");
     nx_erosion_planet P;
     P.vbeg = 0;
-    P.vend = n;
+    P.n = n;
+    P.nbr = nbr_dev;
+    P.edge = edge_dev;
     P.iters = iters;
     P.rain = rain;
     cudaStream_t s = (cudaStream_t)stream;
@@ -468,15 +520,15 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
     // state enters in buffer 0; with an odd count the first iteration reads buffer 1
     if (iters & 1)
         NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp_dev, st_dev, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    return run_batch(planet_dev, &P, 1, nbr_dev, edge_dev, st_dev, st_tmp_dev, mass_dev, flow_dev, workspace, ws_bytes, s);
+    return run_batch(planet_dev, &P, 1, st_dev, st_tmp_dev, mass_dev, flow_dev, workspace, ws_bytes, s);
 }
 
 NX_EXPORT int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
-                               const int32_t *nbr_dev, const float *edge_dev, float *st_dev, float *st_tmp_dev,
-                               double *mass_dev, void *workspace, size_t ws_bytes, void *stream)
+                               float *st_dev, float *st_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes,
+                               void *stream)
 {
-    return run_batch(planets_dev, planets_host, nplanets, nbr_dev, edge_dev, st_dev, st_tmp_dev, mass_dev, nullptr,
-                     workspace, ws_bytes, (cudaStream_t)stream);
+    return run_batch(planets_dev, planets_host, nplanets, st_dev, st_tmp_dev, mass_dev, nullptr, workspace, ws_bytes,
+                     (cudaStream_t)stream);
 }
 
 NX_EXPORT int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream)
@@ -505,6 +557,55 @@ NX_EXPORT int nx_steepest_descent(const int32_t *nbr_dev, const double *h_dev, i
     if (n == 0) return NX_OK;
     steepest_kernel<<<grid1d(n), 256, 0, (cudaStream_t)stream>>>(nbr_dev, h_dev, n, pos_dev, vid_dev);
     NX_CHECK_LAUNCH("steepest_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+static int check_packed(const nx_erosion_planet *ph, int np, int64_t *total)
+{
+    int64_t t = 0;
+    for (int p = 0; p < np; ++p) {
+        if (ph[p].vbeg % BLOCK || ph[p].vbeg < t || ph[p].n < 0)
+            return nx::fail(NX_EINVAL, "erosion batch: planet %d rows must be packed and %d-aligned", p, BLOCK);
+        t = ph[p].vbeg + ph[p].n;
+    }
+    *total = t;
+    return NX_OK;
+}
+
+NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                                    int nplanets, const float *raw_dev, const uint32_t *minmax_dev, float elev_lo,
+                                    float elev_hi, float water0, float *st_dev, float *st_tmp_dev, void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !raw_dev || !minmax_dev || !st_dev || !st_tmp_dev)
+        return nx::fail(NX_EINVAL, "nx_erosion_init_batch: null pointer");
+    int64_t total = 0;
+    int rc = check_packed(planets_host, nplanets, &total);
+    if (rc) return rc;
+    if (total == 0) return NX_OK;
+    erosion_init_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(planets_dev, nplanets, raw_dev, minmax_dev,
+                                                                         elev_lo, elev_hi, water0, (float4 *)st_dev,
+                                                                         (float4 *)st_tmp_dev, total);
+    NX_CHECK_LAUNCH("erosion_init_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                                       int nplanets, const float *st_dev, const void *workspace, float *out_dev,
+                                       void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !st_dev || !workspace || !out_dev)
+        return nx::fail(NX_EINVAL, "nx_erosion_heights_batch: null pointer");
+    int64_t total = 0;
+    int rc = check_packed(planets_host, nplanets, &total);
+    if (rc) return rc;
+    if (total == 0) return NX_OK;
+    erosion_heights_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(
+        planets_dev, nplanets, (const float4 *)st_dev, (const nx_erosion_ctl *)workspace, out_dev, total);
+    NX_CHECK_LAUNCH("erosion_heights_kernel");
     nx::note_launch(1);
     return NX_OK;
 }

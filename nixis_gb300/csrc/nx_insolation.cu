@@ -56,71 +56,99 @@ __device__ __forceinline__ float general_term(float x, float y, float z, float i
     return clat * fmaxf(clon, 0.0f);
 }
 
+// Sum over the schedule for one vertex.
+template <int HP>
+__device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double Y, double Z, double r, float inv_r)
+{
+    const double rho2 = X * X + Y * Y + Z * Z;
+    const double r2 = r * r;
+    const bool on_sphere = fabs(rho2 - r2) <= 1e-12 * r2;
+    const float x = (float)X, y = (float)Y, z = (float)Z;
+    float tot = 0.0f, comp = 0.0f;          // Kahan over tilts
+    const int nr = HP > 0 ? HP : a.n_rot;
+    if (on_sphere) {
+        float2 rt[HP > 0 ? HP : 1];
+        if (HP > 0) {
+#pragma unroll
+            for (int h = 0; h < (HP > 0 ? HP : 1); ++h) rt[h] = a.rot[h];
+        }
+        for (int d = 0; d < a.n_tilt; ++d) {
+            const float2 t = a.tilt[d];
+            const float A = x * t.x, B = -(y * t.x), C = z * t.y;
+            float s = 0.0f;
+            if (a.pairs) {
+                const float aC = fabsf(C);
+                if (HP > 0) {
+#pragma unroll
+                    for (int h = 0; h < (HP > 0 ? HP : 1); ++h) {
+                        float u = fmaf(A, rt[h].x, B * rt[h].y);
+                        s += fmaxf(aC, fabsf(u));
+                    }
+                } else {
+                    for (int h = 0; h < nr; ++h) {
+                        float2 q = a.rot[h];
+                        float u = fmaf(A, q.x, B * q.y);
+                        s += fmaxf(aC, fabsf(u));
+                    }
+                }
+                s = fmaf((float)nr, C, s);
+            } else {
+                for (int h = 0; h < nr; ++h) {
+                    float2 q = a.rot[h];
+                    s += fmaxf(fmaf(A, q.x, fmaf(B, q.y, C)), 0.0f);
+                }
+            }
+            float yk = s - comp;
+            float tk = tot + yk;
+            comp = (tk - tot) - yk;
+            tot = tk;
+        }
+        return tot * inv_r;
+    }
+    for (int d = 0; d < a.n_tilt; ++d) {
+        const float2 t = a.tilt[d];
+        float s = 0.0f;
+        for (int h = 0; h < nr; ++h) {
+            float2 q = a.rot[h];
+            s += general_term(x, y, z, inv_r, t.x, t.y, q.x, q.y);
+            if (a.pairs) s += general_term(x, y, z, inv_r, t.x, t.y, -q.x, -q.y);
+        }
+        float yk = s - comp;
+        float tk = tot + yk;
+        comp = (tk - tot) - yk;
+        tot = tk;
+    }
+    return tot;
+}
+
 template <int HP>
 __global__ void __launch_bounds__(256) insolation_kernel(InsoArgs a)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double X = a.xyz[3 * i], Y = a.xyz[3 * i + 1], Z = a.xyz[3 * i + 2];
-        const double rho2 = X * X + Y * Y + Z * Z;
-        const double r2 = a.r * a.r;
-        const bool on_sphere = fabs(rho2 - r2) <= 1e-12 * r2;
-        const float x = (float)X, y = (float)Y, z = (float)Z;
-        float tot = 0.0f, comp = 0.0f;          // Kahan over tilts
-        const int nr = HP > 0 ? HP : a.n_rot;
-        if (on_sphere) {
-            float2 rt[HP > 0 ? HP : 1];
-            if (HP > 0) {
-#pragma unroll
-                for (int h = 0; h < (HP > 0 ? HP : 1); ++h) rt[h] = a.rot[h];
-            }
-            for (int d = 0; d < a.n_tilt; ++d) {
-                const float2 t = a.tilt[d];
-                const float A = x * t.x, B = -(y * t.x), C = z * t.y;
-                float s = 0.0f;
-                if (a.pairs) {
-                    const float aC = fabsf(C);
-                    if (HP > 0) {
-#pragma unroll
-                        for (int h = 0; h < (HP > 0 ? HP : 1); ++h) {
-                            float u = fmaf(A, rt[h].x, B * rt[h].y);
-                            s += fmaxf(aC, fabsf(u));
-                        }
-                    } else {
-                        for (int h = 0; h < nr; ++h) {
-                            float2 q = a.rot[h];
-                            float u = fmaf(A, q.x, B * q.y);
-                            s += fmaxf(aC, fabsf(u));
-                        }
-                    }
-                    s = fmaf((float)nr, C, s);
-                } else {
-                    for (int h = 0; h < nr; ++h) {
-                        float2 q = a.rot[h];
-                        s += fmaxf(fmaf(A, q.x, fmaf(B, q.y, C)), 0.0f);
-                    }
-                }
-                float yk = s - comp;
-                float tk = tot + yk;
-                comp = (tk - tot) - yk;
-                tot = tk;
-            }
-            tot *= a.inv_r;
-        } else {
-            for (int d = 0; d < a.n_tilt; ++d) {
-                const float2 t = a.tilt[d];
-                float s = 0.0f;
-                for (int h = 0; h < nr; ++h) {
-                    float2 q = a.rot[h];
-                    s += general_term(x, y, z, a.inv_r, t.x, t.y, q.x, q.y);
-                    if (a.pairs) s += general_term(x, y, z, a.inv_r, t.x, t.y, -q.x, -q.y);
-                }
-                float yk = s - comp;
-                float tk = tot + yk;
-                comp = (tk - tot) - yk;
-                tot = tk;
-            }
-        }
+        float tot = inso_vertex<HP>(a, a.xyz[3 * i], a.xyz[3 * i + 1], a.xyz[3 * i + 2], a.r, a.inv_r);
         a.out[i] = a.accumulate ? a.out[i] + tot : tot;
+    }
+}
+
+// Many planets: planet p's vertices fill packed rows [vbeg, vbeg + n)
+// (vbeg a multiple of 256); one block covers 256 rows of one planet.
+template <int HP>
+__global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const nx_inso_planet *__restrict__ P, int np,
+                                                               int64_t total_rows)
+{
+    for (int64_t blk = blockIdx.x; blk * 256 < total_rows; blk += gridDim.x) {
+        const int64_t row = blk * 256 + threadIdx.x;
+        int lo = 0, hi = np - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (P[mid].vbeg <= blk * 256) lo = mid; else hi = mid - 1;
+        }
+        const nx_inso_planet &pl = P[lo];
+        const int64_t i = row - pl.vbeg;
+        if (i < 0 || i >= pl.n) continue;
+        const double r = pl.radius;
+        float tot = inso_vertex<HP>(a, pl.xyz[3 * i], pl.xyz[3 * i + 1], pl.xyz[3 * i + 2], r, (float)(1.0 / r));
+        a.out[row] = tot;
     }
 }
 
@@ -197,6 +225,43 @@ NX_EXPORT int nx_insolation(const double *xyz_dev, int64_t n, double radius, con
     else
         insolation_kernel<0><<<grid_for(n), 256, 0, s>>>(a);
     NX_CHECK_LAUNCH("insolation_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_insolation_batch(const nx_inso_planet *planets_dev, const nx_inso_planet *planets_host, int nplanets,
+                                  const float *table_dev, int n_rot_entries, int pairs, int n_tilt, float *out_dev,
+                                  void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !out_dev || !table_dev || n_rot_entries <= 0 || n_tilt <= 0)
+        return nx::fail(NX_EINVAL, "nx_insolation_batch: bad arguments");
+    int64_t total = 0;
+    for (int p = 0; p < nplanets; ++p) {
+        const nx_inso_planet &P = planets_host[p];
+        if (P.vbeg % 256 || P.n < 0 || (P.n > 0 && !P.xyz) || !(P.radius > 0) || P.vbeg < total)
+            return nx::fail(NX_EINVAL, "nx_insolation_batch: planet %d: rows must be packed, 256-aligned", p);
+        total = P.vbeg + P.n;
+    }
+    InsoArgs a;
+    a.xyz = nullptr;
+    a.n = 0;
+    a.r = 1.0;
+    a.inv_r = 1.0f;
+    a.rot = (const float2 *)table_dev;
+    a.n_rot = n_rot_entries;
+    a.pairs = pairs ? 1 : 0;
+    a.tilt = (const float2 *)table_dev + n_rot_entries;
+    a.n_tilt = n_tilt;
+    a.out = out_dev;
+    a.accumulate = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    int grid = grid_for(total);
+    if (a.pairs && n_rot_entries == 12)
+        insolation_batch_kernel<12><<<grid, 256, 0, s>>>(a, planets_dev, nplanets, total);
+    else
+        insolation_batch_kernel<0><<<grid, 256, 0, s>>>(a, planets_dev, nplanets, total);
+    NX_CHECK_LAUNCH("insolation_batch_kernel");
     nx::note_launch(1);
     return NX_OK;
 }

@@ -461,6 +461,88 @@ __global__ void __launch_bounds__(256) trace_kernel(const double *__restrict__ x
     }
 }
 
+// Ordered-key transform: unsigned comparisons of keys follow float order.
+__device__ __forceinline__ uint32_t fkey(float f)
+{
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b ^ 0x80000000u);
+}
+
+constexpr int CHUNK = 2048;   // vertices per work item of the batched kernel
+
+__device__ __forceinline__ int chunk_planet(const nx_fbm_planet *P, int np, int c)
+{
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (P[mid].chunk0 <= c) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Many planets in one persistent launch: work items are chunks of CHUNK
+// vertices of one planet, handed out round-robin; a block rebuilds its
+// shared table when its next chunk belongs to another planet.  Each chunk
+// also folds its min/max into the planet's ordered keys (for the rescale
+// to metres that follows).
+__global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__restrict__ planets, int np,
+                                                        int total_chunks, unsigned long long *nfb_out)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint32_t s_mm[2][8];
+    const uint32_t lb = lane_base(smem);
+    int cur = -1;
+    unsigned nfb = 0;
+    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
+        const int p = chunk_planet(planets, np, c);
+        const nx_fbm_planet &P = planets[p];
+        if (p != cur) {
+            __syncthreads();
+            build_table(smem, P.perm, P.pgi);
+            __syncthreads();
+            cur = p;
+        }
+        const int64_t base = (int64_t)(c - P.chunk0) * CHUNK;
+        float mn = INFINITY, mx = -INFINITY;
+        for (int64_t i = base + threadIdx.x; i < base + CHUNK && i < P.n; i += blockDim.x) {
+            double X = P.xyz[3 * i], Y = P.xyz[3 * i + 1], Z = P.xyz[3 * i + 2];
+            float xh, xl, yh, yl, zh, zl;
+            split_f64(X, xh, xl);
+            split_f64(Y, yh, yl);
+            split_f64(Z, zh, zl);
+            float acc = 0.0f;
+            for (int o = 0; o < P.n_octaves; ++o) {
+                float v = noise_raw<false>(xh, xl, yh, yl, zh, zl, P.s_hi[o], P.s_lo[o], X, Y, Z, P.s[o], lb, nfb,
+                                           nullptr, nullptr);
+                acc += fmaf(v, P.amp[o] * (1.0f / 103.0f), P.amp[o]);
+            }
+            P.out[i] = acc;
+            mn = fminf(mn, acc);
+            mx = fmaxf(mx, acc);
+        }
+        if (P.minmax) {
+            for (int o = 16; o > 0; o >>= 1) {
+                mn = fminf(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+                mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+            }
+            const int w = threadIdx.x >> 5;
+            if ((threadIdx.x & 31) == 0) { s_mm[0][w] = fkey(mn); s_mm[1][w] = fkey(mx); }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t a0 = s_mm[0][0], a1 = s_mm[1][0];
+                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { a0 = min(a0, s_mm[0][k]); a1 = max(a1, s_mm[1][k]); }
+                atomicMin(&P.minmax[0], a0);
+                atomicMax(&P.minmax[1], a1);
+            }
+            __syncthreads();
+        }
+    }
+    if (nfb_out) {
+        unsigned tot = __reduce_add_sync(0xFFFFFFFFu, nfb);
+        if ((threadIdx.x & 31) == 0 && tot) atomicAdd(nfb_out, (unsigned long long)tot);
+    }
+}
+
 int grid_for(int64_t n, int block, const void *kernel, int smem)
 {
     int per_sm = 1;
@@ -479,6 +561,7 @@ int configure_smem()
     if (smem_configured) return NX_OK;
     NX_CHECK_CUDA(cudaFuncSetAttribute(fbm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
     NX_CHECK_CUDA(cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
+    NX_CHECK_CUDA(cudaFuncSetAttribute(fbm_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
     smem_configured = true;
     return NX_OK;
 }
@@ -561,3 +644,48 @@ NX_EXPORT int nx_noise3d_trace(const double *xyz_dev, int64_t n, const int32_t *
     nx::note_launch(1);
     return NX_OK;
 }
+
+NX_EXPORT int nx_fbm_planet_fill(nx_fbm_planet *planet, int n_octaves, const double *scale, const double *strength,
+                                 double radius)
+{
+    if (!planet || n_octaves < 0 || n_octaves > NX_MAX_OCTAVES || (n_octaves && (!scale || !strength)))
+        return nx::fail(NX_EINVAL, "nx_fbm_planet_fill: bad arguments");
+    planet->n_octaves = n_octaves;
+    for (int o = 0; o < NX_MAX_OCTAVES; ++o) {
+        double sc = o < n_octaves ? scale[o] : 0.0;
+        float hi = (float)sc;
+        planet->s_hi[o] = hi;
+        planet->s_lo[o] = (float)(sc - (double)hi);
+        planet->s[o] = sc;
+        planet->amp[o] = o < n_octaves ? (float)(0.5 * strength[o] * radius) : 0.0f;
+    }
+    return NX_OK;
+}
+
+NX_EXPORT int nx_fbm_batch(const nx_fbm_planet *planets_dev, const nx_fbm_planet *planets_host, int nplanets,
+                           unsigned long long *n_fallback_dev, void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !planets_host) return nx::fail(NX_EINVAL, "nx_fbm_batch: null pointer");
+    int total = 0;
+    for (int p = 0; p < nplanets; ++p) {
+        const nx_fbm_planet &P = planets_host[p];
+        if (P.n < 0 || (P.n > 0 && (!P.xyz || !P.perm || !P.pgi || !P.out)))
+            return nx::fail(NX_EINVAL, "nx_fbm_batch: planet %d incomplete", p);
+        if (P.n_octaves < 0 || P.n_octaves > NX_MAX_OCTAVES) return nx::fail(NX_EINVAL, "nx_fbm_batch: octaves");
+        if (P.chunk0 != total)
+            return nx::fail(NX_EINVAL, "nx_fbm_batch: planet %d chunk0 must be %d (chunks of %d vertices)", p, total,
+                            CHUNK);
+        total += (int)((P.n + CHUNK - 1) / CHUNK);
+    }
+    if (total == 0) return NX_OK;
+    int rc = configure_smem();
+    if (rc) return rc;
+    int grid = grid_for((int64_t)total * 256, 256, (const void *)fbm_batch_kernel, TABLE_BYTES);
+    fbm_batch_kernel<<<grid, 256, TABLE_BYTES, (cudaStream_t)stream>>>(planets_dev, nplanets, total, n_fallback_dev);
+    NX_CHECK_LAUNCH("fbm_batch_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_fbm_chunk_size(void) { return CHUNK; }

@@ -39,7 +39,7 @@ class ErosionRun:
         self.st = torch.empty((n, 4), dtype=torch.float32, device="cuda")    # (h_hi, h_lo, w, s)
         self.st_tmp = torch.empty_like(self.st)
         self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
-        self.planet = torch.zeros(4, dtype=torch.int64, device="cuda")   # one nx_erosion_planet (24 B)
+        self.planet = torch.zeros(8, dtype=torch.int64, device="cuda")   # one nx_erosion_planet (40 B)
         self.iters_done = 0
 
     def load(self, heights, water=None, sediment=None):

@@ -1,0 +1,323 @@
+"""Whole-planet generation: fBm elevations -> metres -> erosion -> insolation.
+
+Two execution paths over the same kernels:
+
+* ``PlanetBatch`` -- many planets of uneven size in a handful of launches:
+  one persistent fBm launch over all planets (with fused per-planet
+  min/max), one launch for the rescale to metres and the initial erosion
+  state, one erosion launch per iteration over the planets still running,
+  one height-extraction launch and one insolation launch per sun schedule.
+  The whole sequence can be captured once as a CUDA graph and replayed.
+* ``generate_plain`` -- the plain per-planet GPU path: one planet at a time,
+  one launch per octave and per erosion iteration, synchronised per planet.
+
+A planet is fully determined by its request (seed, divisions, octaves,
+iterations, ...), so results are reproducible and a planet gives the same
+bits alone or in any batch.
+"""
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _dev
+from . import climate as _climate
+from . import mesh as _mesh
+from . import opensimplex as _osx
+from ._lib import ErosionPlanet, FbmPlanet, InsoPlanet, call, lib
+
+ALIGN = 256
+
+
+@dataclass(frozen=True)
+class PlanetRequest:
+    seed: int
+    divisions: int
+    octaves: int
+    erosion_iters: int = 0
+    insolation: bool = False
+    init_roughness: float = 1.0     # base frequency
+    init_strength: float = 1.0
+    roughness: float = 2.0          # lacunarity
+    persistence: float = 0.5
+    radius: float = 1.0
+    elev_lo: float = -8000.0        # util.rescale bounds (metres)
+    elev_hi: float = 8000.0
+    water0: float = 1e-3            # initial water (m), sediment 0
+    rain: float = 0.0               # per-iteration rain (erode_terrain3 uses 0.3/320)
+    axial_tilt: float = 23.44
+    days: int = 365
+    hours: int = 24
+
+    @property
+    def n_vertices(self):
+        return 10 * self.divisions * self.divisions + 2
+
+    def octave_args(self):
+        scale, strength = [], []
+        f, a = self.init_roughness, self.init_strength
+        for _ in range(self.octaves):
+            scale.append(f / self.radius)
+            strength.append(a / self.radius)
+            f *= self.roughness
+            a *= self.persistence
+        return scale, strength
+
+    def schedule_key(self):
+        return (self.axial_tilt, self.days, self.hours)
+
+    def state_bytes(self):
+        """Device bytes a planet needs beyond its mesh (batched path)."""
+        n = self.n_vertices + ALIGN
+        return n * (4 + 16 + 16 + 4 + (4 if self.insolation else 0))
+
+
+def mesh_bytes(divisions):
+    n = 10 * divisions * divisions + 2
+    return n * (24 + 24 + 24)
+
+
+@dataclass
+class PlanetResult:
+    request: PlanetRequest
+    heights: torch.Tensor               # float32 (N,), metres
+    insolation: torch.Tensor = None     # float32 (N,), mean TOA W/m^2 over the schedule
+    scale_exponent: int = 0
+
+
+def _struct_tensor(arr):
+    raw = np.frombuffer(bytes(arr), np.uint8).copy()
+    return torch.from_numpy(raw).cuda()
+
+
+class PlanetBatch:
+    """A fixed set of planets, packed for batched execution."""
+
+    def __init__(self, requests, meshes=None, stream=None):
+        _dev.require_cuda()
+        if not requests:
+            raise ValueError("empty batch")
+        for r in requests:
+            if not (0 <= r.octaves <= 32):
+                raise ValueError("octaves must be in [0, 32]")
+            if r.erosion_iters < 0:
+                raise ValueError("erosion_iters must be >= 0")
+        self.requests = list(requests)
+        self.meshes = meshes if meshes is not None else _mesh.MeshCache()
+        self.stream = stream
+        np_ = len(requests)
+        # pack in order of descending iteration count (stable)
+        self.order = sorted(range(np_), key=lambda i: -requests[i].erosion_iters)
+        self.vbeg = [0] * np_
+        off = 0
+        for i in self.order:
+            self.vbeg[i] = off
+            off += requests[i].n_vertices
+            off = (off + ALIGN - 1) // ALIGN * ALIGN
+        self.total = off
+        N = off
+        dev = "cuda"
+        self.raw = torch.empty(N, dtype=torch.float32, device=dev)
+        self.st = torch.empty((N, 4), dtype=torch.float32, device=dev)
+        self.st_tmp = torch.empty((N, 4), dtype=torch.float32, device=dev)
+        self.heights = torch.empty(N, dtype=torch.float32, device=dev)
+        self.any_inso = any(r.insolation for r in requests)
+        self.inso = torch.empty(N, dtype=torch.float32, device=dev) if self.any_inso else None
+        # per-planet tables (host init, bit-exact) and min/max keys
+        tabs = np.zeros((np_, 2, 256), np.int32)
+        for j, i in enumerate(self.order):
+            tabs[j, 0], tabs[j, 1] = _osx.init(requests[i].seed)
+        self.tables = torch.from_numpy(tabs).cuda()
+        mm0 = np.zeros((np_, 2), np.uint32)
+        mm0[:, 0] = 0xFFFFFFFF
+        self.minmax0 = torch.from_numpy(mm0.view(np.int32)).cuda()
+        self.minmax = self.minmax0.clone()
+        # descriptors (in packed order)
+        chunk = int(lib().nx_fbm_chunk_size())
+        fb = (FbmPlanet * np_)()
+        er = (ErosionPlanet * np_)()
+        c0 = 0
+        self._meshes = []
+        for j, i in enumerate(self.order):
+            r = requests[i]
+            m = self.meshes.get(r.divisions, stream=stream)
+            self._meshes.append(m)
+            f = fb[j]
+            f.xyz = m.xyz.data_ptr()
+            f.n = m.n
+            f.perm = self.tables[j, 0].data_ptr()
+            f.pgi = self.tables[j, 1].data_ptr()
+            f.out = self.raw.data_ptr() + 4 * self.vbeg[i]
+            f.minmax = self.minmax[j].data_ptr()
+            f.chunk0 = c0
+            c0 += (m.n + chunk - 1) // chunk
+            sc, st = r.octave_args()
+            sca = (ctypes.c_double * max(1, len(sc)))(*sc)
+            sta = (ctypes.c_double * max(1, len(st)))(*st)
+            call("nx_fbm_planet_fill", ctypes.byref(f), r.octaves, sca, sta, float(r.radius))
+            e = er[j]
+            e.vbeg = self.vbeg[i]
+            e.n = m.n
+            e.nbr = m.nbr.data_ptr()
+            e.edge = m.edge.data_ptr()
+            e.iters = r.erosion_iters
+            e.rain = r.rain
+        self.fb_host, self.er_host = fb, er
+        self.fb_dev = _struct_tensor(fb)
+        self.er_dev = _struct_tensor(er)
+        self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(N, np_)), dtype=torch.uint8, device=dev)
+        self.max_iters = max(r.erosion_iters for r in requests)
+        # insolation groups by schedule
+        self.inso_groups = []
+        if self.any_inso:
+            groups = {}
+            for j, i in enumerate(self.order):
+                if requests[i].insolation:
+                    groups.setdefault(requests[i].schedule_key(), []).append(i)
+            for (tilt, days, hours), members in groups.items():
+                rot, tilts = _climate.annual_schedule(tilt, 365 if days == 365 else days, days, hours)
+                tab, nre, pairs = _climate._plan(rot, tilts)
+                ip = (InsoPlanet * len(members))()
+                for q, i in enumerate(members):
+                    m = self.meshes.get(requests[i].divisions)
+                    ip[q].xyz = m.xyz.data_ptr()
+                    ip[q].n = m.n
+                    ip[q].vbeg = self.vbeg[i]
+                    ip[q].radius = requests[i].radius
+                self.inso_groups.append(dict(table=torch.from_numpy(tab).cuda(), nre=nre, pairs=pairs,
+                                             n_tilt=len(tilts), host=ip, dev=_struct_tensor(ip), members=members,
+                                             scale=_climate.SOLAR_CONSTANT / (days * hours)))
+        self.graph = None
+
+    # ------------------------------------------------------------------
+    def launch(self):
+        """Enqueue the whole batch on the current stream (no host sync)."""
+        s = _dev.stream_handle(self.stream)
+        np_ = len(self.requests)
+        self.minmax.copy_(self.minmax0)
+        call("nx_fbm_batch", _dev.ptr(self.fb_dev), ctypes.cast(self.fb_host, ctypes.c_void_p), np_, None, s)
+        call("nx_erosion_init_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
+             _dev.ptr(self.raw), _dev.ptr(self.minmax), ctypes.c_float(self.requests[0].elev_lo),
+             ctypes.c_float(self.requests[0].elev_hi), ctypes.c_float(self.requests[0].water0), _dev.ptr(self.st),
+             _dev.ptr(self.st_tmp), s)
+        call("nx_erosion_ctl_init", _dev.ptr(self.ws), self.ws.numel(), np_, s)
+        call("nx_erosion_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
+             _dev.ptr(self.st), _dev.ptr(self.st_tmp), None, _dev.ptr(self.ws), self.ws.numel(), s)
+        call("nx_erosion_heights_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
+             _dev.ptr(self.st), _dev.ptr(self.ws), _dev.ptr(self.heights), s)
+        for g in self.inso_groups:
+            call("nx_insolation_batch", _dev.ptr(g["dev"]), ctypes.cast(g["host"], ctypes.c_void_p),
+                 len(g["members"]), _dev.ptr(g["table"]), g["nre"], g["pairs"], g["n_tilt"], _dev.ptr(self.inso), s)
+
+    def capture(self):
+        """Record launch() as a CUDA graph (after one eager run)."""
+        self.launch()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch()
+        self.graph = g
+        return g
+
+    def run(self):
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.launch()
+
+    def kernels_per_run(self):
+        return 4 + self.max_iters + (1 if self.max_iters > 0 else 0) + len(self.inso_groups)
+
+    def results(self):
+        """PlanetResult per request, in request order (views into the batch)."""
+        uniform = len({(r.elev_lo, r.elev_hi, r.water0) for r in self.requests}) == 1
+        if not uniform:
+            raise ValueError("a batch shares elev_lo/elev_hi/water0")
+        K = self.ws[:32 * len(self.requests)].view(torch.int32).view(-1, 8)[:, 3].cpu().numpy()
+        out = []
+        pos = {i: j for j, i in enumerate(self.order)}
+        for i, r in enumerate(self.requests):
+            b, n = self.vbeg[i], r.n_vertices
+            ins = None
+            if r.insolation:
+                sc = _climate.SOLAR_CONSTANT / (r.days * r.hours)
+                ins = self.inso[b:b + n] * sc
+            out.append(PlanetResult(r, self.heights[b:b + n], ins, int(K[pos[i]])))
+        return out
+
+
+def generate_batched(requests, meshes=None):
+    b = PlanetBatch(requests, meshes)
+    b.run()
+    return b.results()
+
+
+# ----------------------------------------------------------------------
+# plain per-planet path (the comparator)
+
+class _PlainWork:
+    """Reusable buffers for the plain path (grown on demand)."""
+
+    def __init__(self):
+        self.n = 0
+
+    def ensure(self, n):
+        if n > self.n:
+            self.raw = torch.empty(n, dtype=torch.float32, device="cuda")
+            self.hm = torch.empty(n, dtype=torch.float64, device="cuda")
+            self.st = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+            self.st_tmp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+            self.inso = torch.empty(n, dtype=torch.float32, device="cuda")
+            self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
+            self.planet = torch.zeros(8, dtype=torch.int64, device="cuda")
+            self.perm = torch.empty(256, dtype=torch.int32, device="cuda")
+            self.pgi = torch.empty(256, dtype=torch.int32, device="cuda")
+            self.n = n
+
+
+_plain = _PlainWork()
+
+
+def generate_plain(request, meshes=None, sync=True, out=None):
+    """One planet: a launch per octave, per erosion iteration; synchronised."""
+    r = request
+    meshes = meshes if meshes is not None else _mesh.MeshCache()
+    m = meshes.get(r.divisions)
+    n = m.n
+    w = _plain
+    w.ensure(n)
+    s = _dev.stream_handle()
+    perm, pgi = _osx.init(r.seed)
+    w.perm.copy_(torch.from_numpy(perm))
+    w.pgi.copy_(torch.from_numpy(pgi))
+    scale, strength = r.octave_args()
+    for o in range(r.octaves):
+        sc = (ctypes.c_double * 1)(scale[o])
+        st = (ctypes.c_double * 1)(strength[o])
+        call("nx_fbm", _dev.ptr(m.xyz), n, _dev.ptr(w.perm), _dev.ptr(w.pgi), 1, sc, st, float(r.radius), None,
+             _dev.ptr(w.raw), 1 if o > 0 else 0, None, s)
+    if r.octaves == 0:
+        w.raw[:n].zero_()
+    raw = w.raw[:n]
+    mn, mx = torch.aminmax(raw)
+    rng_ = mx - mn
+    sc = torch.tensor(r.elev_hi - r.elev_lo, dtype=torch.float32, device="cuda") / rng_
+    h = (raw - mn) * sc + torch.tensor(r.elev_lo, dtype=torch.float32, device="cuda")
+    hd = w.hm[:n]
+    hd.copy_(h)
+    wat = torch.full((n,), r.water0, dtype=torch.float64, device="cuda")
+    call("nx_erosion_load", _dev.ptr(hd), _dev.ptr(wat), None, n, _dev.ptr(w.st), _dev.ptr(w.ws), w.ws.numel(), s)
+    call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(w.st), _dev.ptr(w.st_tmp),
+         r.erosion_iters, ctypes.c_float(r.rain), _dev.ptr(w.planet), None, None, _dev.ptr(w.ws), w.ws.numel(), s)
+    call("nx_erosion_store", _dev.ptr(w.st), n, _dev.ptr(w.ws), _dev.ptr(hd), None, None, s)
+    heights = hd.float() if out is None else out.copy_(hd)
+    ins = None
+    if r.insolation:
+        rot, tilts = _climate.annual_schedule(r.axial_tilt, r.days, r.days, r.hours)
+        ins = _climate.insolation_sum(m.xyz, r.radius, rot, tilts)
+        ins.mul_(_climate.SOLAR_CONSTANT / (r.days * r.hours))
+    if sync:
+        torch.cuda.synchronize()
+    return PlanetResult(r, heights, ins, 0)

@@ -677,6 +677,81 @@ NXO_API int nxo_sort_adjacency(int32_t *adj, int64_t nv)
     return 0;
 }
 
+/*
+ * Icosphere inputs on the CPU (this project's construction, documented in
+ * nixis_gb300/icosphere.py; the reference's meshzoo is unavailable).  Tables:
+ * corners float64[36], faces int32[60], face sides int32[120], edges
+ * int32[60].  Same binary64 operation order as the GPU generator.
+ */
+static void nrm3(double *p)
+{
+    double r = sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
+    p[0] = p[0] / r; p[1] = p[1] / r; p[2] = p[2] / r;
+}
+
+static int32_t face_vid(const int32_t *faces, const int32_t *fe, int f, int64_t i, int64_t j, int64_t k)
+{
+    const int32_t *F = faces + 3 * f;
+    if (i == 0 && j == 0) return F[0];
+    if (i == k && j == 0) return F[1];
+    if (i == 0 && j == k) return F[2];
+    int side; int64_t pos;
+    if (j == 0) { side = 0; pos = i; }
+    else if (i == 0) { side = 1; pos = j; }
+    else if (i + j == k) { side = 2; pos = j; }
+    else {
+        int64_t npf = (k - 1) * (k - 2) / 2;
+        int64_t off = (i - 1) * (k - 1) - (i - 1) * i / 2 + (j - 1);
+        return (int32_t)(12 + 30 * (k - 1) + f * npf + off);
+    }
+    int e = fe[6 * f + 2 * side];
+    int64_t t = fe[6 * f + 2 * side + 1] ? pos : k - pos;
+    return (int32_t)(12 + e * (k - 1) + t - 1);
+}
+
+NXO_API int nxo_icosphere(int k, const double *corners, const int32_t *faces, const int32_t *fe,
+                          const int32_t *edges, double *xyz, int32_t *tris)
+{
+    if (k < 1) return -1;
+    int64_t K = k;
+    for (int c = 0; c < 36; ++c) xyz[c] = corners[c];
+    for (int e = 0; e < 30; ++e) {
+        const double *A = corners + 3 * edges[2 * e], *B = corners + 3 * edges[2 * e + 1];
+        for (int64_t t = 1; t < K; ++t) {
+            double *p = xyz + 3 * (12 + e * (K - 1) + t - 1);
+            for (int c = 0; c < 3; ++c) p[c] = (double)(K - t) * A[c] + (double)t * B[c];
+            nrm3(p);
+        }
+    }
+    int64_t npf = (K - 1) * (K - 2) / 2, base = 12 + 30 * (K - 1);
+    for (int f = 0; f < 20; ++f) {
+        const double *A = corners + 3 * faces[3 * f], *B = corners + 3 * faces[3 * f + 1], *C = corners + 3 * faces[3 * f + 2];
+        int64_t q = 0;
+        for (int64_t i = 1; i < K - 1; ++i)
+            for (int64_t j = 1; j < K - i; ++j, ++q) {
+                double *p = xyz + 3 * (base + f * npf + q);
+                for (int c = 0; c < 3; ++c) p[c] = ((double)(K - i - j) * A[c] + (double)i * B[c]) + (double)j * C[c];
+                nrm3(p);
+            }
+    }
+    if (tris) {
+        int64_t n = 0;
+        for (int f = 0; f < 20; ++f)
+            for (int64_t i = 0; i < K; ++i)
+                for (int64_t j = 0; j < K - i; ++j) {
+                    int32_t *t = tris + 3 * n++;
+                    t[0] = face_vid(faces, fe, f, i, j, K); t[1] = face_vid(faces, fe, f, i + 1, j, K);
+                    t[2] = face_vid(faces, fe, f, i, j + 1, K);
+                    if (i + j < K - 1) {
+                        t = tris + 3 * n++;
+                        t[0] = face_vid(faces, fe, f, i + 1, j, K); t[1] = face_vid(faces, fe, f, i + 1, j + 1, K);
+                        t[2] = face_vid(faces, fe, f, i, j + 1, K);
+                    }
+                }
+    }
+    return 0;
+}
+
 /* util.py:110-140 (mode=None, mid=None): min/max normalise to [lower, upper]. */
 NXO_API void nxo_rescale(const double *x, int64_t n, double lower, double upper, double *out)
 {

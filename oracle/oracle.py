@@ -57,6 +57,7 @@ def lib():
             "nxo_sort_adjacency": (_i32, [_p, _i64]),
             "nxo_rescale": (None, [_p, _i64, _d, _d, _p]),
             "nxo_num_threads": (_i32, []),
+            "nxo_icosphere": (_i32, [_i32, _p, _p, _p, _p, _p, _p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -230,3 +231,31 @@ def rescale(x, lower, upper):
     out = np.empty_like(x)
     lib().nxo_rescale(_ptr(x), len(x), float(lower), float(upper), _ptr(out))
     return out
+
+
+def icosphere(k, with_tris=True):
+    """CPU icosphere with the GPU generator's layout (vertices, triangles)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "_ico_tables", os.path.join(os.path.dirname(_HERE), "nixis_gb300", "icosphere.py"))
+    ico = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ico)
+    k = int(k)
+    nv, nt = ico.counts(k)
+    c = _c(ico.corners(), np.float64)
+    f = _c(ico.FACES, np.int32)
+    fe = _c(ico.face_edge_table(), np.int32)
+    e = _c(ico.edges(), np.int32)
+    xyz = np.empty((nv, 3), np.float64)
+    tris = np.empty((nt, 3), np.int32) if with_tris else None
+    if lib().nxo_icosphere(k, _ptr(c), _ptr(f), _ptr(fe), _ptr(e), _ptr(xyz), _ptr(tris) if with_tris else None):
+        raise ValueError("bad divisions")
+    return xyz, tris
+
+
+def planet_mesh(k):
+    """(vertices, neighbour table) for divisions k, all on the CPU."""
+    xyz, tris = icosphere(k)
+    adj = build_adjacency(tris)
+    sort_adjacency(adj)
+    return xyz, adj
