@@ -290,6 +290,14 @@ def bench_ours(args):
         cache.get(r.divisions)
     torch.cuda.synchronize()
     batch = planets.PlanetBatch(reqs, cache)
+    if args.profile:
+        # one eager run of the batch (what the ncu captures record), then exit
+        batch.launch()
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"profile_run": args.workload, "kernels": batch.kernels_per_run(),
+                              "erosion_launches": batch.max_iters, "config": config(reqs)}))
+        return
     if args.eager:
         batch.launch()
     else:
@@ -421,6 +429,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--workload", choices=["batch64", "small"], default="batch64")
     ap.add_argument("--eager", action="store_true", help="launch without a CUDA graph (for profilers)")
+    ap.add_argument("--profile", action="store_true", help="build the batch, run it once eagerly, exit (ncu)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
