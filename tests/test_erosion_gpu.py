@@ -198,38 +198,34 @@ def test_batched_planets_equal_planets_alone():
         h = h.astype(np.float32).astype(np.float64)
         planets.append((p, adj, h, iters))
     planets.sort(key=lambda x: -x[3])
-    # pack: each range starts at a multiple of 256, neighbour ids global
-    off, descs, nbrs, els, hs = 0, [], [], [], []
+    # pack the states: each planet's rows start at a multiple of 256; its
+    # neighbour ids stay local and its mesh arrays stay separate
+    off, descs, meshes, hs = 0, [], [], []
     for p, adj, h, iters in planets:
         n = len(p)
-        pad = (-n) % 256
-        descs.append((off, off + n, iters))
-        nb = np.where(adj >= 0, adj + off, -1).astype(np.int32)
-        nbrs.append(np.concatenate([nb, np.full((pad, 6), -1, np.int32)]))
-        el = meshref.edge_lengths(p, adj)
-        els.append(np.concatenate([el, np.zeros((pad, 6), np.float32)]))
-        hs.append(np.concatenate([h, np.zeros(pad)]))
-        off += n + pad
+        descs.append((off, n, iters))
+        meshes.append((torch.from_numpy(adj).cuda(), torch.from_numpy(meshref.edge_lengths(p, adj)).cuda()))
+        hs.append(np.concatenate([h, np.zeros((-n) % 256)]))
+        off += n + (-n) % 256
     N = off
-    nbr = torch.from_numpy(np.concatenate(nbrs)).cuda()
-    el = torch.from_numpy(np.concatenate(els)).cuda()
     hall = np.concatenate(hs).astype(np.float32)
     st = torch.zeros((N, 4), dtype=torch.float32, device="cuda")
     st_t = torch.zeros_like(st)
-    for (b, e, iters) in descs:
+    for (b, n, iters) in descs:
         dst = st_t if iters & 1 else st
-        dst[b:e, 0] = torch.from_numpy(hall[b:e]).cuda()
-        dst[b:e, 2] = 1e-3
-    arr = (_lib.ErosionPlanet * len(descs))(*[_lib.ErosionPlanet(b, e, it, 0.0) for b, e, it in descs])
+        dst[b:b + n, 0] = torch.from_numpy(hall[b:b + n]).cuda()
+        dst[b:b + n, 2] = 1e-3
+    arr = (_lib.ErosionPlanet * len(descs))(*[
+        _lib.ErosionPlanet(b, n, nb.data_ptr(), el.data_ptr(), it, 0.0) for (b, n, it), (nb, el) in zip(descs, meshes)])
     pd = torch.from_numpy(np.frombuffer(bytes(arr), np.uint8).copy()).cuda()
     ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(N, len(descs))), dtype=torch.uint8, device="cuda")
     _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), len(descs), _dev.stream_handle())
-    _lib.call("nx_erosion_batch", _dev.ptr(pd), ctypes.cast(arr, ctypes.c_void_p), len(descs), _dev.ptr(nbr),
-              _dev.ptr(el), _dev.ptr(st), _dev.ptr(st_t), None, _dev.ptr(ws), ws.numel(), _dev.stream_handle())
+    _lib.call("nx_erosion_batch", _dev.ptr(pd), ctypes.cast(arr, ctypes.c_void_p), len(descs),
+              _dev.ptr(st), _dev.ptr(st_t), None, _dev.ptr(ws), ws.numel(), _dev.stream_handle())
     out = st.cpu().numpy()
-    for (p, adj, h, iters), (b, e, _) in zip(planets, descs):
+    for (p, adj, h, iters), (b, n, _) in zip(planets, descs):
         _, _, _, _, _, run = run_gpu(p, adj, h, np.full(len(p), np.float32(1e-3)), np.zeros(len(p)), iters)
-        assert np.array_equal(out[b:e], run.st.cpu().numpy())
+        assert np.array_equal(out[b:b + n], run.st.cpu().numpy())
 
 
 def test_bad_neighbour_id_is_reported_not_faulted():
