@@ -249,6 +249,29 @@ int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_eros
                              int nplanets, const float *st_dev, const void *workspace, float *out_dev,
                              void *stream);
 
+/* Erosion for callers that cannot allocate device memory.  No counterpart
+ * in the reference (whose erosion is host code).  Some callers run inside
+ * a host application's own device-memory pool, where a direct cudaMalloc
+ * bypasses the owner's budget, or in loops that must not stall, since
+ * cudaMalloc and cudaFree synchronise the device.  This entry point runs
+ * `iters` iterations like nx_erosion_steps on one planet of at most
+ * NX_NOALLOC_MAX_VERTICES vertices (larger n returns NX_EINVAL) without
+ * allocating: its scratch (second state buffer, control block, partial
+ * sums) is a fixed array inside the library, about 4.2 MB, which every GPU
+ * that loads the library keeps until the process exits.  The caller passes
+ * the mesh, the state st_dev (float4 rows as in nx_erosion_load, true
+ * values with scale exponent 0, magnitudes below 2^96) and the outputs:
+ * the state is updated in place, mass_dev (optional) as in
+ * nx_erosion_steps, status_dev (optional, device int32[2]) gets the final
+ * scale exponent K and the neighbour-range error flag.  The first call on
+ * each device looks up the array's device address (make that first call
+ * before any stream capture).  All calls share the one array and each call
+ * resets what must start at zero; calls whose work overlaps on the GPU
+ * (other streams, other threads) race on it and must be serialised. */
+#define NX_NOALLOC_MAX_VERTICES 262144
+int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *st_dev, int iters,
+                             float rain, double *mass_dev, int32_t *status_dev, void *stream);
+
 /* erosion.find_lowest (erosion.py:398-406) for every vertex: pos_dev gets
  * the position, among the neighbours that are not -1, of the first lowest
  * one if it is strictly lower than the vertex, else -1; vid_dev (optional)

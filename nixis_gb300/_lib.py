@@ -46,6 +46,7 @@ SIGNATURES = {
     "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_float, _p, _p,
                                      _p]),
     "nx_erosion_heights_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p]),
+    "nx_erosion_steps_noalloc": (_i32, [_p, _p, _i64, _p, _i32, ctypes.c_float, _p, _p, _p]),
 }
 
 NX_MAX_OCTAVES = 32

@@ -27,6 +27,8 @@
 // iteration writes buffer 0.
 #include "nx_common.cuh"
 
+#include <mutex>
+
 namespace nx {
 void note_launch(int k);
 }
@@ -607,5 +609,118 @@ NX_EXPORT int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, con
         planets_dev, nplanets, (const float4 *)st_dev, (const nx_erosion_ctl *)workspace, out_dev, total);
     NX_CHECK_LAUNCH("erosion_heights_kernel");
     nx::note_launch(1);
+    return NX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Erosion without allocation.
+//
+// Some callers cannot allocate device memory at the point where they run
+// erosion: code that lives inside a host application's own device-memory
+// pool (where a direct cudaMalloc bypasses the owner's budget), and loops
+// that must not stall, since cudaMalloc/cudaFree synchronise the device.
+// nx_erosion_steps_noalloc takes the same mesh and state buffers as
+// nx_erosion_steps but keeps its scratch -- the planet descriptor, the
+// control block, the per-block mass partials and the second state buffer --
+// in the fixed device array below, sized for NX_NOALLOC_MAX_VERTICES
+// vertices.  Every GPU that loads the library holds this array until the
+// process exits.
+
+namespace {
+
+constexpr int64_t NOALLOC_MAX_N = NX_NOALLOC_MAX_VERTICES;
+constexpr size_t NOALLOC_HEAD = 512;    // descriptor (40 B) + control block (32 B), padded
+constexpr size_t NOALLOC_PARTIALS = 3 * sizeof(double) * (size_t)((NOALLOC_MAX_N + BLOCK - 1) / BLOCK);
+constexpr size_t NOALLOC_STATE = 16 * (size_t)NOALLOC_MAX_N;
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD + NOALLOC_PARTIALS + NOALLOC_STATE;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device; the host-side symbol is only a stand-in for it).
+int noalloc_scratch(unsigned char **out)
+{
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return nx::fail(NX_EINVAL, "nx_erosion_steps_noalloc: device id %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return nx::check_cuda(e, "nx_erosion_steps_noalloc: cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = (unsigned char *)g_noalloc_ptr[dev];
+    return NX_OK;
+}
+
+// Writes the planet descriptor and zeroes the control block (scale exponent
+// 0, no rescale pending, mass counter and error flag cleared): the scratch
+// keeps whatever the previous call left there.
+__global__ void noalloc_prepare_kernel(nx_erosion_planet P, nx_erosion_planet *desc, nx_erosion_ctl *ctl)
+{
+    *desc = P;
+    ctl->maxbits[0] = 0u;
+    ctl->maxbits[1] = 0u;
+    ctl->maxbits[2] = 0u;
+    ctl->K[0] = 0;
+    ctl->K[1] = 0;
+    ctl->done = 0u;
+    ctl->err = 0;
+    ctl->pad = 0;
+}
+
+__global__ void noalloc_status_kernel(const nx_erosion_ctl *ctl, int32_t *status)
+{
+    status[0] = ctl->K[0];
+    status[1] = ctl->err;
+}
+
+}  // namespace
+
+NX_EXPORT int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *st_dev,
+                                       int iters, float rain, double *mass_dev, int32_t *status_dev, void *stream)
+{
+    if (n <= 0 || iters < 0) return nx::fail(NX_EINVAL, "nx_erosion_steps_noalloc: bad n or iters");
+    if (n > NOALLOC_MAX_N)
+        return nx::fail(NX_EINVAL, "nx_erosion_steps_noalloc: %lld vertices exceed the fixed scratch of %lld vertices",
+                        (long long)n, (long long)NOALLOC_MAX_N);
+    if (!nbr_dev || !edge_dev || !st_dev) return nx::fail(NX_EINVAL, "nx_erosion_steps_noalloc: null pointer");
+    unsigned char *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    // scratch layout: descriptor at 0; control block at 256, followed (16-byte
+    // aligned, as the workspace carving expects) by the per-block partials;
+    // second state buffer after NOALLOC_HEAD + NOALLOC_PARTIALS
+    nx_erosion_planet *desc = (nx_erosion_planet *)base;
+    nx_erosion_ctl *ctl = (nx_erosion_ctl *)(base + 256);
+    float *st_tmp = (float *)(base + NOALLOC_HEAD + NOALLOC_PARTIALS);
+    nx_erosion_planet P;
+    P.vbeg = 0;
+    P.n = n;
+    P.nbr = nbr_dev;
+    P.edge = edge_dev;
+    P.iters = iters;
+    P.rain = rain;
+    cudaStream_t s = (cudaStream_t)stream;
+    noalloc_prepare_kernel<<<1, 1, 0, s>>>(P, desc, ctl);
+    NX_CHECK_LAUNCH("noalloc_prepare_kernel");
+    nx::note_launch(1);
+    if (iters & 1)
+        NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp, st_dev, 16 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    size_t ws_bytes = nx_erosion_workspace_size(n, 1);
+    static_assert(256 + sizeof(nx_erosion_ctl) + 16 + NOALLOC_PARTIALS <= NOALLOC_HEAD + NOALLOC_PARTIALS,
+                  "partials fit before the second state buffer");
+    static_assert((NOALLOC_HEAD + NOALLOC_PARTIALS) % 256 == 0, "state buffer alignment");
+    rc = run_batch(desc, &P, 1, st_dev, st_tmp, mass_dev, nullptr, (void *)ctl, ws_bytes, s);
+    if (rc) return rc;
+    if (status_dev) {
+        noalloc_status_kernel<<<1, 1, 0, s>>>(ctl, status_dev);
+        NX_CHECK_LAUNCH("noalloc_status_kernel");
+        nx::note_launch(1);
+    }
     return NX_OK;
 }
