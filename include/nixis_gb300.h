@@ -165,13 +165,15 @@ int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, f
 /* Erosion (variant 3)                                                 */
 /* ------------------------------------------------------------------ */
 
-/* One planet of an erosion batch.  Its state occupies rows [vbeg, vbeg+n)
- * of the packed state buffers (vbeg a multiple of 256); nbr (n,6) local
- * neighbour ids and edge (n,6) per-slot lengths are its mesh (device
- * pointers, shared by planets of equal divisions).  Planets are packed in
- * order of non-increasing `iters`.  `rain` is added to every water value
- * before each iteration (erode_terrain3 adds 0.3/320, erosion.py:182-183;
- * 0 gives bare erosion_iteration3 steps). */
+/* One planet of an erosion launch.  Its state occupies rows [vbeg, vbeg+n)
+ * of the state buffers; nbr (n,6) local neighbour ids and edge (n,6)
+ * per-slot lengths are its mesh (device pointers, shared by planets of
+ * equal divisions).  `rain` is added to every water value before each
+ * iteration (erode_terrain3 adds 0.3/320, erosion.py:182-183; 0 gives bare
+ * erosion_iteration3 steps).  Its iteration t runs at global step
+ * t_start + t; `slot` is its control block in the workspace.  Batches
+ * (nx_erosion_batch) use t_start = 0, slot = index, and order planets by
+ * non-increasing `iters`. */
 typedef struct nx_erosion_planet {
     int64_t vbeg;
     int64_t n;
@@ -179,10 +181,13 @@ typedef struct nx_erosion_planet {
     const float *edge;
     int32_t iters;
     float rain;
+    int32_t t_start;
+    int32_t slot;
 } nx_erosion_planet;
 
-/* Workspace bytes for erosion over n_padded_total packed vertices and
- * nplanets planets (control words + per-block partial sums). */
+/* Workspace bytes for erosion over n_padded_total state rows (a bound on
+ * 256 x the blocks a launch covers) and nplanets control blocks (control
+ * words, per-block partial sums and block map). */
 size_t nx_erosion_workspace_size(int64_t n_padded_total, int nplanets);
 
 /* Zero the per-planet control words (scale exponent 0) of a workspace. */
@@ -217,6 +222,20 @@ int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, f
 int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
                      float *st_dev, float *st_tmp_dev, double *mass_dev, void *workspace, size_t ws_bytes,
                      void *stream);
+
+/* Serving: one launch that advances every listed planet (any order) by one
+ * iteration, planet p at its own iteration t - t_start (planets outside
+ * [0, iters) skip).  Control blocks are workspace slots [0, nslots);
+ * zero a planet's slot (32 bytes at 32*slot) before its first iteration.
+ * remap = 1 rebuilds the launch's block map (whenever the list changed). */
+int nx_erosion_tick(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets, int t,
+                    float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes, int nslots, int remap,
+                    void *stream);
+
+/* After each listed planet's last iteration: record its final scale
+ * exponent in its control block's K[0] (read by nx_erosion_store and
+ * nx_erosion_heights_batch). */
+int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
 
 /* Write one planet's state back as binary64 true values (h_hi + h_lo, w, s
  * times 2^K, K from the workspace's first control block).  w64_dev /

@@ -47,6 +47,8 @@ SIGNATURES = {
                                      _p]),
     "nx_erosion_heights_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p]),
     "nx_erosion_steps_noalloc": (_i32, [_p, _p, _i64, _p, _i32, ctypes.c_float, _p, _p, _p]),
+    "nx_erosion_tick": (_i32, [_p, _p, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
+    "nx_erosion_finish": (_i32, [_p, _i32, _p, _p]),
 }
 
 NX_MAX_OCTAVES = 32
@@ -70,7 +72,8 @@ class InsoPlanet(ctypes.Structure):
 class ErosionPlanet(ctypes.Structure):
     """nx_erosion_planet (include/nixis_gb300.h)."""
     _fields_ = [("vbeg", ctypes.c_int64), ("n", ctypes.c_int64), ("nbr", ctypes.c_void_p),
-                ("edge", ctypes.c_void_p), ("iters", ctypes.c_int32), ("rain", ctypes.c_float)]
+                ("edge", ctypes.c_void_p), ("iters", ctypes.c_int32), ("rain", ctypes.c_float),
+                ("t_start", ctypes.c_int32), ("slot", ctypes.c_int32)]
 
 _lock = threading.Lock()
 _LIB = None

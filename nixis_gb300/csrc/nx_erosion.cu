@@ -56,14 +56,14 @@ namespace {
 
 struct StepArgs {
     const nx_erosion_planet *planets;
-    int np;
-    int t;
+    const int2 *blk_map;   // per block of the launch: (planet index, block within the planet)
+    int t;                 // global step; a planet's iteration is t - t_start
     float4 *st0;
     float4 *st1;
     nx_erosion_ctl *ctl;
-    double *partials;      // [gridDim.x][3] (mass sums only)
-    double *mass;          // [iteration][planet][3] or null
-    int mass_np;           // planets per mass row
+    double *partials;      // [block][3] (mass sums only)
+    double *mass;          // [iteration][mass_np][3] or null
+    int mass_np;
     uint16_t *flow;        // optional: per vertex 2 bits per slot (1: neighbour higher, 2: lower)
 };
 
@@ -100,70 +100,68 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// One erosion iteration (erosion.py:210-267) for the vertices of every
+// block's planet.  No barrier on the common path: every thread reads the
+// (broadcast) planet descriptor and control words itself, and each warp
+// folds its max into the planet's next slot with a reduction atomic.
 __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
 {
-    __shared__ int s_p;
-    __shared__ float s_lam, s_rain;
-    __shared__ int s_K;
-    __shared__ float s_wmax[BLOCK / 32];
-    __shared__ double s_wsum[BLOCK / 32][3];
-    __shared__ bool s_last;
-
-    const int64_t vblk = (int64_t)blockIdx.x * BLOCK;
-    if (threadIdx.x == 0) {
-        int p = find_planet(a.planets, a.np, vblk);
-        s_p = p;
-        nx_erosion_ctl *c = a.ctl + p;
-        float m = __uint_as_float(((volatile unsigned *)c->maxbits)[a.t % 3]);
-        int shift = m > RESCALE_ABOVE ? RESCALE_SHIFT : 0;
-        int K = ((volatile int *)c->K)[a.t & 1] + shift;
-        s_K = K;
-        s_lam = shift ? __int_as_float((127 - shift) << 23) : 1.0f;
-        s_rain = scalbnf(a.planets[p].rain, -K);
-        if (vblk == a.planets[p].vbeg) {
-            c->K[(a.t + 1) & 1] = K;
-            c->maxbits[(a.t + 2) % 3] = 0u;
-        }
+    const int2 bm = a.blk_map[blockIdx.x];
+    const int p = bm.x;
+    const nx_erosion_planet &P = a.planets[p];
+    const int t = a.t - P.t_start;
+    if (t < 0 || t >= P.iters) return;        // whole block: planet not stepping now
+    nx_erosion_ctl *c = a.ctl + P.slot;
+    const float m = __uint_as_float(((volatile unsigned *)c->maxbits)[t % 3]);
+    const int shift = m > RESCALE_ABOVE ? RESCALE_SHIFT : 0;
+    const int K = ((volatile int *)c->K)[t & 1] + shift;
+    const float lam = shift ? __int_as_float((127 - shift) << 23) : 1.0f;
+    const float rain = scalbnf(P.rain, -K);
+    if (bm.y == 0 && threadIdx.x == 0) {
+        c->K[(t + 1) & 1] = K;
+        c->maxbits[(t + 2) % 3] = 0u;
     }
-    __syncthreads();
-    const int p = s_p;
-    const nx_erosion_planet P = a.planets[p];
-    const float lam = s_lam, rain = s_rain;
     // buffers: read B[(iters - t) & 1], write the other; B[0] = st0
-    const bool par = ((P.iters - a.t) & 1) != 0;
+    const bool par = ((P.iters - t) & 1) != 0;
     const float4 *__restrict__ ist = par ? a.st1 : a.st0;
     float4 *__restrict__ ost = par ? a.st0 : a.st1;
 
-    const int64_t i = vblk + threadIdx.x;       // packed state row
-    const int64_t li = i - P.vbeg;                // vertex id within the planet
+    const int64_t li = (int64_t)bm.y * BLOCK + threadIdx.x;   // vertex id within the planet
+    const int64_t i = P.vbeg + li;                             // state row
     float vmax = 0.0f;
     double sh = 0.0, sw = 0.0, ss = 0.0;
     if (li < P.n) {
         const float sol = c_sol, evap = c_evap, cap = c_cap;
+        const int2 *nb2 = reinterpret_cast<const int2 *>(P.nbr + 6 * li);
+        const float2 *el2 = reinterpret_cast<const float2 *>(P.edge + 6 * li);
+        const int2 n01 = nb2[0], n23 = nb2[1], n45 = nb2[2];
         const float4 me = ist[i];
+        const float2 d01 = el2[0], d23 = el2[1], d45 = el2[2];
         const float hh = __fmul_rn(me.x, lam), hl = __fmul_rn(me.y, lam);
         const float wi = __fadd_rn(__fmul_rn(me.z, lam), rain);
         const float si = __fmul_rn(me.w, lam);
         float sed = si, wat = wi;
-        const int2 *nb2 = reinterpret_cast<const int2 *>(P.nbr + 6 * li);
-        const float2 *el2 = reinterpret_cast<const float2 *>(P.edge + 6 * li);
-        int2 n01 = nb2[0], n23 = nb2[1], n45 = nb2[2];
-        float2 d01 = el2[0], d23 = el2[1], d45 = el2[2];
         const int nbr[6] = {n01.x, n01.y, n23.x, n23.y, n45.x, n45.y};
         const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
+        float4 o[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int j = nbr[k];
+            const bool ok = j >= 0 && (int64_t)j < P.n;
+            o[k] = ok ? ist[P.vbeg + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         unsigned flow = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            int j = nbr[k];
+            const int j = nbr[k];
             if (j < 0) continue;
             if ((int64_t)j >= P.n) {
-                a.ctl[p].err = 1;
+                c->err = 1;
                 continue;
             }
-            float4 o = ist[P.vbeg + j];
-            float wj = __fadd_rn(__fmul_rn(o.z, lam), rain);
+            const float wj = __fadd_rn(__fmul_rn(o[k].z, lam), rain);
             // sign of the slope (erosion.py:230): sign of h_j - h_i
-            float diff = __fadd_rn(__fsub_rn(__fmul_rn(o.x, lam), hh), __fsub_rn(__fmul_rn(o.y, lam), hl));
+            const float diff = __fadd_rn(__fsub_rn(__fmul_rn(o[k].x, lam), hh), __fsub_rn(__fmul_rn(o[k].y, lam), hl));
             if (diff > 0.0f) {
                 sed = __fadd_rn(sed, __fmul_rn(sol, wj));
                 wat = __fadd_rn(wat, __fmul_rn(wj, dd[k]));
@@ -178,80 +176,93 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
         float nh = hh, nl = hl;
         df_add(nh, nl, -sed);
         float sn = __fadd_rn(si, sed);
-        float wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, evap)));
-        float cw = __fmul_rn(cap, wn);
+        const float wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, evap)));
+        const float cw = __fmul_rn(cap, wn);
         if (sn > cw) {
-            float ex = __fsub_rn(sn, cw);
+            const float ex = __fsub_rn(sn, cw);
             df_add(nh, nl, ex);
             sn = __fsub_rn(sn, ex);
         }
         ost[i] = make_float4(nh, nl, wn, sn);
-        if (a.flow) a.flow[i] = (uint16_t)flow;
+        if (a.flow) a.flow[li] = (uint16_t)flow;
         vmax = fmaxf(fabsf(nh), fmaxf(fabsf(wn), fabsf(sn)));
         if (a.mass) { sh = (double)nh + (double)nl; sw = (double)wn; ss = (double)sn; }
     }
-    // block max -> planet max for the next iteration's rescale decision
+    // warp max -> the planet's max for the next iteration's rescale decision
+    // (NaN never wins fmaxf; an infinite value still triggers a rescale)
     vmax = warp_max(vmax);
+    if ((threadIdx.x & 31) == 0) atomicMax(&c->maxbits[(t + 1) % 3], __float_as_uint(vmax));
+    if (!a.mass) return;
+
+    // per-iteration mass sums: block partials, then the planet's last block
+    // reduces them in a fixed order (Neumaier), scaled back by 2^K
+    __shared__ double s_wsum[BLOCK / 32][3];
+    __shared__ bool s_last;
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) s_wmax[wid] = vmax;
-    if (a.mass) {
-        sh = warp_sum(sh); sw = warp_sum(sw); ss = warp_sum(ss);
-        if (lane == 0) { s_wsum[wid][0] = sh; s_wsum[wid][1] = sw; s_wsum[wid][2] = ss; }
+    sh = warp_sum(sh); sw = warp_sum(sw); ss = warp_sum(ss);
+    if (lane == 0) { s_wsum[wid][0] = sh; s_wsum[wid][1] = sw; s_wsum[wid][2] = ss; }
+    __syncthreads();
+    const int64_t nblk = (P.n + BLOCK - 1) / BLOCK;
+    const int64_t b0 = (int64_t)blockIdx.x - bm.y;
+    if (threadIdx.x == 0) {
+        double t0 = 0, t1 = 0, t2 = 0;
+        for (int w = 0; w < BLOCK / 32; ++w) { t0 += s_wsum[w][0]; t1 += s_wsum[w][1]; t2 += s_wsum[w][2]; }
+        double *pp = a.partials + 3 * (int64_t)blockIdx.x;
+        pp[0] = t0; pp[1] = t1; pp[2] = t2;
+        __threadfence();
+        const unsigned prev = atomicAdd(&c->done, 1u);
+        s_last = (int64_t)prev + 1 == nblk;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+    for (int64_t b = threadIdx.x; b < nblk; b += BLOCK) {
+        const volatile double *pp = a.partials + 3 * (b0 + b);
+        for (int q = 0; q < 3; ++q) {
+            const double x = pp[q], tt = acc[q] + x;
+            cmp[q] += fabs(acc[q]) >= fabs(x) ? (acc[q] - tt) + x : (x - tt) + acc[q];
+            acc[q] = tt;
+        }
+    }
+    __syncthreads();
+    for (int q = 0; q < 3; ++q) {
+        const double v = warp_sum(acc[q] + cmp[q]);
+        if (lane == 0) s_wsum[wid][q] = v;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float m = 0.0f;
-        for (int w = 0; w < BLOCK / 32; ++w) m = fmaxf(m, s_wmax[w]);
-        // NaN never wins fmaxf; an infinite value still triggers a rescale
-        atomicMax(&a.ctl[p].maxbits[(a.t + 1) % 3], __float_as_uint(m));
-        s_last = false;
-        if (a.mass) {
-            double t0 = 0, t1 = 0, t2 = 0;
-            for (int w = 0; w < BLOCK / 32; ++w) { t0 += s_wsum[w][0]; t1 += s_wsum[w][1]; t2 += s_wsum[w][2]; }
-            double *pp = a.partials + 3 * (int64_t)blockIdx.x;
-            pp[0] = t0; pp[1] = t1; pp[2] = t2;
-            __threadfence();
-            int64_t nblk = (P.n + BLOCK - 1) / BLOCK;
-            unsigned prev = atomicAdd(&a.ctl[p].done, 1u);
-            s_last = (int64_t)prev + 1 == nblk;
+        double out[3];
+        for (int q = 0; q < 3; ++q) {
+            double sacc = 0, e = 0;
+            for (int w = 0; w < BLOCK / 32; ++w) {
+                const double x = s_wsum[w][q], tt = sacc + x;
+                e += fabs(sacc) >= fabs(x) ? (sacc - tt) + x : (x - tt) + sacc;
+                sacc = tt;
+            }
+            out[q] = ldexp(sacc + e, K);
         }
+        double *mrow = a.mass + 3 * ((int64_t)t * a.mass_np + p);
+        mrow[0] = out[0]; mrow[1] = out[1]; mrow[2] = out[2];
+        c->done = 0u;
+    }
+}
+
+// Block map of a launch: planet p owns blocks [sum of earlier planets'
+// blocks, + ceil(n_p / BLOCK)); one block per planet fills its entries.
+__global__ void erosion_blkmap_kernel(const nx_erosion_planet *__restrict__ P, int np, int2 *__restrict__ map)
+{
+    const int p = blockIdx.x;
+    if (p >= np) return;
+    __shared__ int64_t s_b0;
+    if (threadIdx.x == 0) {
+        int64_t b0 = 0;
+        for (int q = 0; q < p; ++q) b0 += (P[q].n + BLOCK - 1) / BLOCK;
+        s_b0 = b0;
     }
     __syncthreads();
-    if (a.mass && s_last) {
-        // last block of this planet: compensated (Neumaier) sum of the
-        // planet's block partials in a fixed order, scaled by 2^K
-        __threadfence();
-        const int64_t b0 = P.vbeg / BLOCK, nblk = (P.n + BLOCK - 1) / BLOCK;
-        double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
-        for (int64_t b = threadIdx.x; b < nblk; b += BLOCK) {
-            const volatile double *pp = a.partials + 3 * (b0 + b);
-            for (int c = 0; c < 3; ++c) {
-                double x = pp[c], tt = acc[c] + x;
-                cmp[c] += fabs(acc[c]) >= fabs(x) ? (acc[c] - tt) + x : (x - tt) + acc[c];
-                acc[c] = tt;
-            }
-        }
-        for (int c = 0; c < 3; ++c) {
-            double v = warp_sum(acc[c] + cmp[c]);
-            if (lane == 0) s_wsum[wid][c] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double out[3] = {0, 0, 0};
-            for (int c = 0; c < 3; ++c) {
-                double s = 0, e = 0;
-                for (int w = 0; w < BLOCK / 32; ++w) {
-                    double x = s_wsum[w][c], tt = s + x;
-                    e += fabs(s) >= fabs(x) ? (s - tt) + x : (x - tt) + s;
-                    s = tt;
-                }
-                out[c] = ldexp(s + e, s_K);
-            }
-            double *m = a.mass + 3 * ((int64_t)a.t * a.mass_np + p);
-            m[0] = out[0]; m[1] = out[1]; m[2] = out[2];
-            a.ctl[p].done = 0u;
-        }
-    }
+    const int64_t nb = (P[p].n + BLOCK - 1) / BLOCK;
+    for (int64_t j = threadIdx.x; j < nb; j += blockDim.x) map[s_b0 + j] = make_int2(p, (int)j);
 }
 
 // After a run: move each planet's final scale exponent and max into slot 0
@@ -262,7 +273,7 @@ __global__ void erosion_rebase_kernel(const nx_erosion_planet *__restrict__ P, i
     if (p >= np) return;
     int it = P[p].iters;
     if (it <= 0) return;
-    nx_erosion_ctl &c = ctl[p];
+    nx_erosion_ctl &c = ctl[P[p].slot];
     unsigned m = c.maxbits[it % 3];
     int K = c.K[it & 1];
     c.maxbits[0] = m;
@@ -375,7 +386,7 @@ __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_p
         const int64_t i = row - P[p].vbeg;
         if (i < 0 || i >= P[p].n) continue;
         float4 v = st[row];
-        out[row] = (float)ldexp((double)v.x + (double)v.y, ctl[p].K[0]);
+        out[row] = (float)ldexp((double)v.x + (double)v.y, ctl[P[p].slot].K[0]);
     }
 }
 
@@ -411,10 +422,13 @@ int grid1d(int64_t n, int block = 256)
 
 }  // namespace
 
+// Workspace: control blocks (one per slot), then per launch block 3 partial
+// sums (float64) and one block-map entry (int2).
 NX_EXPORT size_t nx_erosion_workspace_size(int64_t n_padded_total, int nplanets)
 {
     int64_t nblk = (n_padded_total + BLOCK - 1) / BLOCK;
-    return sizeof(nx_erosion_ctl) * (size_t)(nplanets > 0 ? nplanets : 1) + 3 * sizeof(double) * (size_t)(nblk > 0 ? nblk : 1) + 64;
+    if (nblk < 1) nblk = 1;
+    return sizeof(nx_erosion_ctl) * (size_t)(nplanets > 0 ? nplanets : 1) + (3 * sizeof(double) + sizeof(int2)) * (size_t)nblk + 64;
 }
 
 namespace {
@@ -422,15 +436,17 @@ namespace {
 struct Workspace {
     nx_erosion_ctl *ctl;
     double *partials;
+    int2 *blk_map;
 };
 
-Workspace carve(void *ws, int np)
+Workspace carve(void *ws, int nslots, int64_t nblk)
 {
     Workspace w;
     w.ctl = (nx_erosion_ctl *)ws;
-    uintptr_t p = (uintptr_t)(w.ctl + np);
+    uintptr_t p = (uintptr_t)(w.ctl + nslots);
     p = (p + 15) & ~(uintptr_t)15;
     w.partials = (double *)p;
+    w.blk_map = (int2 *)(w.partials + 3 * nblk);
     return w;
 }
 
@@ -443,7 +459,7 @@ NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, cons
     if (!h64_dev || !st_dev || !workspace) return nx::fail(NX_EINVAL, "nx_erosion_load: null pointer");
     if (ws_bytes < nx_erosion_workspace_size(n, 1)) return nx::fail(NX_EINVAL, "nx_erosion_load: workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
-    Workspace w = carve(workspace, 1);
+    Workspace w = carve(workspace, 1, (n + BLOCK - 1) / BLOCK);
     unsigned long long *mb = (unsigned long long *)w.partials;   // first partial slot as scratch
     NX_CHECK_CUDA(cudaMemsetAsync(mb, 0, sizeof(unsigned long long), s));
     erosion_maxabs64_kernel<<<grid1d(n), 256, 0, s>>>(h64_dev, w64_dev, s64_dev, n, mb);
@@ -454,6 +470,10 @@ NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, cons
     return NX_OK;
 }
 
+static int64_t planet_blocks(const nx_erosion_planet &P) { return (P.n + BLOCK - 1) / BLOCK; }
+
+// Batch: planets packed by non-increasing iteration count, so the planets
+// still running at iteration t are a prefix of the block map.
 static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
                      float *st_dev, float *st_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace,
                      size_t ws_bytes, cudaStream_t s)
@@ -462,22 +482,23 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     if (!planets_dev || !planets_host || !st_dev || !st_tmp || !workspace)
         return nx::fail(NX_EINVAL, "erosion: null pointer");
     int max_it = 0;
-    int64_t total = 0;
+    int64_t total = 0, nblk = 0;
     for (int p = 0; p < np; ++p) {
         const nx_erosion_planet &P = planets_host[p];
-        if (P.vbeg % BLOCK != 0 || P.n < 0 || P.iters < 0)
-            return nx::fail(NX_EINVAL, "erosion: planet %d state rows must start at a multiple of %d", p, BLOCK);
+        if (P.vbeg < 0 || P.n < 0 || P.iters < 0 || P.slot != p || P.t_start != 0)
+            return nx::fail(NX_EINVAL, "erosion: planet %d: bad descriptor (slot must be its index, t_start 0)", p);
         if (P.n > 0 && (!P.nbr || !P.edge)) return nx::fail(NX_EINVAL, "erosion: planet %d has no mesh", p);
-        if (p > 0 && (P.vbeg < planets_host[p - 1].vbeg + planets_host[p - 1].n || P.iters > planets_host[p - 1].iters))
-            return nx::fail(NX_EINVAL, "erosion: planets must be packed in order of descending iterations");
+        if (p > 0 && P.iters > planets_host[p - 1].iters)
+            return nx::fail(NX_EINVAL, "erosion: planets must be ordered by non-increasing iterations");
         if (P.iters > max_it) max_it = P.iters;
-        total = P.vbeg + P.n;
+        if (P.vbeg + P.n > total) total = P.vbeg + P.n;
+        nblk += planet_blocks(P);
     }
-    if (ws_bytes < nx_erosion_workspace_size(total, np)) return nx::fail(NX_EINVAL, "erosion: workspace too small");
-    Workspace w = carve(workspace, np);
+    if (ws_bytes < nx_erosion_workspace_size(nblk * BLOCK, np)) return nx::fail(NX_EINVAL, "erosion: workspace too small");
+    Workspace w = carve(workspace, np, nblk);
     StepArgs a;
     a.planets = planets_dev;
-    a.np = np;
+    a.blk_map = w.blk_map;
     a.st0 = (float4 *)st_dev;
     a.st1 = (float4 *)st_tmp;
     a.ctl = w.ctl;
@@ -485,14 +506,21 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     a.mass = mass_dev;
     a.mass_np = np;
     a.flow = flow_dev;
+    if (max_it > 0) {
+        erosion_blkmap_kernel<<<np, 256, 0, s>>>(planets_dev, np, w.blk_map);
+        NX_CHECK_LAUNCH("erosion_blkmap_kernel");
+        nx::note_launch(1);
+    }
     int last = np - 1;
+    int64_t grid = nblk;
     for (int t = 0; t < max_it; ++t) {
-        while (last >= 0 && planets_host[last].iters <= t) --last;
-        if (last < 0) break;
-        int64_t end = planets_host[last].vbeg + planets_host[last].n;
-        int64_t nblk = (end + BLOCK - 1) / BLOCK;
+        while (last >= 0 && planets_host[last].iters <= t) {
+            grid -= planet_blocks(planets_host[last]);
+            --last;
+        }
+        if (last < 0 || grid <= 0) break;
         a.t = t;
-        erosion_step_kernel<<<(unsigned)nblk, BLOCK, 0, s>>>(a);
+        erosion_step_kernel<<<(unsigned)grid, BLOCK, 0, s>>>(a);
         NX_CHECK_LAUNCH("erosion_step_kernel");
         nx::note_launch(1);
     }
@@ -501,6 +529,61 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         NX_CHECK_LAUNCH("erosion_rebase_kernel");
         nx::note_launch(1);
     }
+    return NX_OK;
+}
+
+// Serving: one launch advances every listed planet by one iteration, each
+// at its own iteration t - t_start (planets outside [0, iters) are skipped).
+NX_EXPORT int nx_erosion_tick(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
+                              int t, float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes, int nslots,
+                              int remap, void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !st_dev || !st_tmp_dev || !workspace || nslots <= 0)
+        return nx::fail(NX_EINVAL, "nx_erosion_tick: bad arguments");
+    int64_t nblk = 0;
+    for (int p = 0; p < nplanets; ++p) {
+        const nx_erosion_planet &P = planets_host[p];
+        if (P.vbeg < 0 || P.n < 0 || P.iters < 0 || P.slot < 0 || P.slot >= nslots || (P.n > 0 && (!P.nbr || !P.edge)))
+            return nx::fail(NX_EINVAL, "nx_erosion_tick: planet %d: bad descriptor", p);
+        nblk += planet_blocks(P);
+    }
+    if (ws_bytes < nx_erosion_workspace_size(nblk * BLOCK, nslots))
+        return nx::fail(NX_EINVAL, "nx_erosion_tick: workspace too small");
+    if (nblk == 0) return NX_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    Workspace w = carve(workspace, nslots, nblk);
+    if (remap) {
+        erosion_blkmap_kernel<<<nplanets, 256, 0, s>>>(planets_dev, nplanets, w.blk_map);
+        NX_CHECK_LAUNCH("erosion_blkmap_kernel");
+        nx::note_launch(1);
+    }
+    StepArgs a;
+    a.planets = planets_dev;
+    a.blk_map = w.blk_map;
+    a.t = t;
+    a.st0 = (float4 *)st_dev;
+    a.st1 = (float4 *)st_tmp_dev;
+    a.ctl = w.ctl;
+    a.partials = w.partials;
+    a.mass = nullptr;
+    a.mass_np = 0;
+    a.flow = nullptr;
+    erosion_step_kernel<<<(unsigned)nblk, BLOCK, 0, s>>>(a);
+    NX_CHECK_LAUNCH("erosion_step_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+// After a planet's last iteration: its final scale exponent into K[0].
+NX_EXPORT int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !workspace) return nx::fail(NX_EINVAL, "nx_erosion_finish: null pointer");
+    erosion_rebase_kernel<<<(nplanets + 127) / 128, 128, 0, (cudaStream_t)stream>>>(planets_dev, nplanets,
+                                                                                    (nx_erosion_ctl *)workspace);
+    NX_CHECK_LAUNCH("erosion_rebase_kernel");
+    nx::note_launch(1);
     return NX_OK;
 }
 
@@ -517,6 +600,8 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
     P.edge = edge_dev;
     P.iters = iters;
     P.rain = rain;
+    P.t_start = 0;
+    P.slot = 0;
     cudaStream_t s = (cudaStream_t)stream;
     NX_CHECK_CUDA(cudaMemcpyAsync(planet_dev, &P, sizeof(P), cudaMemcpyHostToDevice, s));
     // state enters in buffer 0; with an odd count the first iteration reads buffer 1
@@ -630,7 +715,7 @@ namespace {
 
 constexpr int64_t NOALLOC_MAX_N = NX_NOALLOC_MAX_VERTICES;
 constexpr size_t NOALLOC_HEAD = 512;    // descriptor (40 B) + control block (32 B), padded
-constexpr size_t NOALLOC_PARTIALS = 3 * sizeof(double) * (size_t)((NOALLOC_MAX_N + BLOCK - 1) / BLOCK);
+constexpr size_t NOALLOC_PARTIALS = (3 * sizeof(double) + sizeof(int2)) * (size_t)((NOALLOC_MAX_N + BLOCK - 1) / BLOCK);
 constexpr size_t NOALLOC_STATE = 16 * (size_t)NOALLOC_MAX_N;
 constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD + NOALLOC_PARTIALS + NOALLOC_STATE;
 
@@ -693,8 +778,8 @@ NX_EXPORT int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge
     int rc = noalloc_scratch(&base);
     if (rc) return rc;
     // scratch layout: descriptor at 0; control block at 256, followed (16-byte
-    // aligned, as the workspace carving expects) by the per-block partials;
-    // second state buffer after NOALLOC_HEAD + NOALLOC_PARTIALS
+    // aligned, as the workspace carving expects) by the per-block partials and
+    // block map; second state buffer after NOALLOC_HEAD + NOALLOC_PARTIALS
     nx_erosion_planet *desc = (nx_erosion_planet *)base;
     nx_erosion_ctl *ctl = (nx_erosion_ctl *)(base + 256);
     float *st_tmp = (float *)(base + NOALLOC_HEAD + NOALLOC_PARTIALS);
@@ -705,6 +790,8 @@ NX_EXPORT int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge
     P.edge = edge_dev;
     P.iters = iters;
     P.rain = rain;
+    P.t_start = 0;
+    P.slot = 0;
     cudaStream_t s = (cudaStream_t)stream;
     noalloc_prepare_kernel<<<1, 1, 0, s>>>(P, desc, ctl);
     NX_CHECK_LAUNCH("noalloc_prepare_kernel");

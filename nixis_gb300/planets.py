@@ -164,6 +164,8 @@ class PlanetBatch:
             e.edge = m.edge.data_ptr()
             e.iters = r.erosion_iters
             e.rain = r.rain
+            e.t_start = 0
+            e.slot = j
         self.fb_host, self.er_host = fb, er
         self.fb_dev = _struct_tensor(fb)
         self.er_dev = _struct_tensor(er)

@@ -1,0 +1,456 @@
+"""Serving planet requests with continuous batching.
+
+Requests (seed, divisions, octaves, erosion iterations, insolation) arrive
+over time.  The engine works in ticks; one tick is one erosion launch that
+advances every planet currently eroding by one iteration, each at its own
+iteration count (nx_erosion_tick).  Between ticks, arrived requests are
+admitted as memory frees up:
+
+* state rows come from a fixed arena (first fit, 256-row aligned) holding
+  (h_hi, h_lo, w, s) x 2, raw fBm, heights and insolation per vertex;
+* meshes stay resident, keyed by divisions, evicted least recently used
+  when no admitted planet uses them;
+* admission is first-come first-served against the HBM budget (arena +
+  meshes).
+
+A newly admitted planet's fBm, rescale and initial state run on a side
+stream while the main stream keeps eroding the others; it joins the next
+tick.  A planet that finishes erosion gets its heights (main stream), then
+insolation and the copy of its results to pinned host memory on the side
+stream.  Results are the same bits as the planet generated alone
+(planets.generate_plain).
+
+``serve_plain`` is the comparator: the same stream of requests handled one
+at a time with the plain per-planet path.
+"""
+import ctypes
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _dev
+from . import climate as _climate
+from . import mesh as _mesh
+from . import opensimplex as _osx
+from . import planets as _planets
+from ._lib import ErosionPlanet, FbmPlanet, call, lib
+
+ALIGN = 256
+ROW_BYTES = 16 + 16 + 4 + 4 + 4
+
+
+class RowArena:
+    """First-fit allocator of ALIGN-aligned row ranges in [0, capacity)."""
+
+    def __init__(self, capacity):
+        self.capacity = capacity // ALIGN * ALIGN
+        self.free = [(0, self.capacity)]       # sorted (start, length)
+
+    def alloc(self, n):
+        need = (n + ALIGN - 1) // ALIGN * ALIGN
+        for k, (b, ln) in enumerate(self.free):
+            if ln >= need:
+                if ln == need:
+                    self.free.pop(k)
+                else:
+                    self.free[k] = (b + need, ln - need)
+                return b
+        return None
+
+    def release(self, start, n):
+        need = (n + ALIGN - 1) // ALIGN * ALIGN
+        self.free.append((start, need))
+        self.free.sort()
+        merged = []
+        for b, ln in self.free:
+            if merged and merged[-1][0] + merged[-1][1] == b:
+                merged[-1] = (merged[-1][0], merged[-1][1] + ln)
+            else:
+                merged.append((b, ln))
+        self.free = merged
+
+    @property
+    def used(self):
+        return self.capacity - sum(ln for _, ln in self.free)
+
+
+class ResidentMeshes:
+    """Meshes in HBM with reference counts; unreferenced ones are evicted
+    least recently used when the budget requires it."""
+
+    def __init__(self, budget_bytes):
+        self.budget = budget_bytes
+        self.meshes = {}
+        self.refs = {}
+        self.lru = []
+
+    def bytes_for(self, k):
+        return 0 if k in self.meshes else _planets.mesh_bytes(k)
+
+    def resident_bytes(self):
+        return sum(m.nbytes for m in self.meshes.values())
+
+    def can_fit(self, k):
+        need = self.bytes_for(k)
+        if need == 0:
+            return True
+        free = self.budget - self.resident_bytes()
+        evictable = sum(self.meshes[q].nbytes for q in self.lru if self.refs.get(q, 0) == 0)
+        return need <= free + evictable
+
+    def acquire(self, k, stream=None):
+        if k not in self.meshes:
+            need = _planets.mesh_bytes(k)
+            while self.resident_bytes() + need > self.budget:
+                victim = next((q for q in self.lru if self.refs.get(q, 0) == 0), None)
+                if victim is None:
+                    break
+                self.lru.remove(victim)
+                del self.meshes[victim]
+            self.meshes[k] = _mesh.PlanetMesh(k, stream=stream)
+            self.lru.append(k)
+        else:
+            self.lru.remove(k)
+            self.lru.append(k)
+        self.refs[k] = self.refs.get(k, 0) + 1
+        return self.meshes[k]
+
+    def release(self, k):
+        self.refs[k] -= 1
+
+    # MeshCache interface (planets.generate_plain)
+    def get(self, k, stream=None):
+        m = self.acquire(k, stream)
+        self.release(k)
+        return m
+
+
+@dataclass
+class Ticket:
+    request: _planets.PlanetRequest
+    arrival: float
+    index: int
+    admitted: float = None
+    finished: float = None
+    heights: np.ndarray = None
+    insolation: np.ndarray = None
+    # engine state
+    vbeg: int = 0
+    slot: int = 0
+    t_start: int = 0
+    mesh: object = None
+    host_h: torch.Tensor = None
+    host_i: torch.Tensor = None
+    done_event: object = None
+    ready_event: object = None
+    stage: str = "queued"
+    minmax: torch.Tensor = None
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+
+def _descs_tensor(arr):
+    return torch.from_numpy(np.frombuffer(bytes(arr), np.uint8).copy()).pin_memory()
+
+
+class ServeEngine:
+    """Continuous-batching planet generator over one GPU."""
+
+    def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None):
+        _dev.require_cuda()
+        self.budget = int(hbm_budget)
+        rows = arena_rows if arena_rows is not None else int(self.budget * arena_fraction) // ROW_BYTES
+        self.arena = RowArena(rows)
+        R = self.arena.capacity
+        dev = "cuda"
+        self.st = torch.empty((R, 4), dtype=torch.float32, device=dev)
+        self.st_tmp = torch.empty((R, 4), dtype=torch.float32, device=dev)
+        self.raw = torch.empty(R, dtype=torch.float32, device=dev)
+        self.heights = torch.empty(R, dtype=torch.float32, device=dev)
+        self.inso = torch.empty(R, dtype=torch.float32, device=dev)
+        self.nslots = slots
+        self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(R, slots)), dtype=torch.uint8, device=dev)
+        self.free_slots = list(range(slots))
+        self.meshes = ResidentMeshes(self.budget - R * ROW_BYTES - self.ws.numel())
+        self.main = torch.cuda.Stream()
+        self.side = torch.cuda.Stream()
+        self.desc_dev = torch.empty(slots * ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device=dev)
+        self.chunk = int(lib().nx_fbm_chunk_size())
+        self.tick = 0
+        self.queue = []          # arrived or future tickets, arrival order
+        self.active = []         # admitted, not finished
+        self.eroding_key = None
+        self.eroding = []
+        self._descs_host = None
+        self.done = []
+        self._inflight = []      # events of recent ticks (bounded queue depth)
+        self._schedules = {}
+
+    # ------------------------------------------------------------------
+    def submit(self, request, arrival, index=0):
+        t = Ticket(request, arrival, index)
+        self.queue.append(t)
+        return t
+
+    def _schedule_table(self, r):
+        key = r.schedule_key()
+        if key not in self._schedules:
+            rot, tilts = _climate.annual_schedule(r.axial_tilt, r.days, r.days, r.hours)
+            tab, nre, pairs = _climate._plan(rot, tilts)
+            self._schedules[key] = (torch.from_numpy(tab).cuda(), nre, pairs, len(tilts),
+                                    _climate.SOLAR_CONSTANT / (r.days * r.hours))
+        return self._schedules[key]
+
+    def _admit(self, now):
+        admitted = []
+        while self.queue and self.queue[0].arrival <= now:
+            t = self.queue[0]
+            r = t.request
+            if not self.free_slots:
+                break
+            if not self.meshes.can_fit(r.divisions):
+                break
+            vbeg = self.arena.alloc(r.n_vertices)
+            if vbeg is None:
+                break
+            self.queue.pop(0)
+            t.vbeg = vbeg
+            t.slot = self.free_slots.pop()
+            t.admitted = time.perf_counter()
+            with torch.cuda.stream(self.side):
+                t.mesh = self.meshes.acquire(r.divisions)
+            admitted.append(t)
+        return admitted
+
+    def _launch_new(self, new):
+        """fBm + rescale + initial state of newly admitted planets (side stream)."""
+        s = _dev.stream_handle(self.side)
+        n = len(new)
+        fb = (FbmPlanet * n)()
+        c0 = 0
+        tabs = np.zeros((n, 2, 256), np.int32)
+        for j, t in enumerate(new):
+            tabs[j, 0], tabs[j, 1] = _osx.init(t.request.seed)
+        with torch.cuda.stream(self.side):
+            tab_dev = torch.from_numpy(tabs).pin_memory().to("cuda", non_blocking=True)
+            mm = torch.tensor([[-1, 0]] * n, dtype=torch.int64).to(torch.int32)
+            mm[:, 0] = -1
+            mm_dev = mm.pin_memory().to("cuda", non_blocking=True)
+            for j, t in enumerate(new):
+                r = t.request
+                f = fb[j]
+                f.xyz = t.mesh.xyz.data_ptr()
+                f.n = t.mesh.n
+                f.perm = tab_dev[j, 0].data_ptr()
+                f.pgi = tab_dev[j, 1].data_ptr()
+                f.out = self.raw.data_ptr() + 4 * t.vbeg
+                f.minmax = mm_dev[j].data_ptr()
+                f.chunk0 = c0
+                c0 += (t.mesh.n + self.chunk - 1) // self.chunk
+                sc, st = r.octave_args()
+                call("nx_fbm_planet_fill", ctypes.byref(f), r.octaves, (ctypes.c_double * max(1, len(sc)))(*sc),
+                     (ctypes.c_double * max(1, len(st)))(*st), float(r.radius))
+            fb_dev = _descs_tensor(fb).to("cuda", non_blocking=True)
+            call("nx_fbm_batch", _dev.ptr(fb_dev), ctypes.cast(fb, ctypes.c_void_p), n, None, s)
+            for j, t in enumerate(new):
+                r = t.request
+                self.ws[32 * t.slot: 32 * t.slot + 32].zero_()
+                e = (ErosionPlanet * 1)()
+                e[0].vbeg = 0
+                e[0].n = t.mesh.n
+                e[0].nbr = t.mesh.nbr.data_ptr()
+                e[0].edge = t.mesh.edge.data_ptr()
+                e[0].iters = r.erosion_iters
+                e[0].rain = r.rain
+                e[0].t_start = 0
+                e[0].slot = t.slot
+                e_dev = _descs_tensor(e).to("cuda", non_blocking=True)
+                call("nx_erosion_init_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
+                     ctypes.c_void_p(self.raw.data_ptr() + 4 * t.vbeg), _dev.ptr(mm_dev[j]),
+                     ctypes.c_float(r.elev_lo), ctypes.c_float(r.elev_hi), ctypes.c_float(r.water0),
+                     ctypes.c_void_p(self.st.data_ptr() + 16 * t.vbeg),
+                     ctypes.c_void_p(self.st_tmp.data_ptr() + 16 * t.vbeg), s)
+                t._e_single = (e, e_dev)
+                t.host_h = torch.empty(t.mesh.n, dtype=torch.float32).pin_memory()
+                if r.insolation:
+                    t.host_i = torch.empty(t.mesh.n, dtype=torch.float32).pin_memory()
+                ev = torch.cuda.Event()
+                ev.record(self.side)
+                t.ready_event = ev
+                t._keep = (tab_dev, mm_dev, fb_dev, fb)
+                if r.erosion_iters == 0:
+                    t.stage = "output"
+                else:
+                    t.stage = "waiting"
+
+    def _output(self, t, after_main):
+        """Heights (+ insolation) and the copy to the host for a finished planet."""
+        r = t.request
+        e, e_dev = t._e_single
+        ws = _dev.ptr(self.ws)
+        stream = self.main if after_main else self.side
+        s = _dev.stream_handle(stream)
+        with torch.cuda.stream(stream):
+            if r.erosion_iters > 0:
+                call("nx_erosion_finish", _dev.ptr(e_dev), 1, ws, s)
+            call("nx_erosion_heights_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
+                 ctypes.c_void_p(self.st.data_ptr() + 16 * t.vbeg), ws,
+                 ctypes.c_void_p(self.heights.data_ptr() + 4 * t.vbeg), s)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        self.side.wait_event(ev)
+        ss = _dev.stream_handle(self.side)
+        with torch.cuda.stream(self.side):
+            n = t.mesh.n
+            if r.insolation:
+                tab, nre, pairs, ntilt, scale = self._schedule_table(r)
+                out = self.inso[t.vbeg:t.vbeg + n]
+                call("nx_insolation", _dev.ptr(t.mesh.xyz), n, float(r.radius), _dev.ptr(tab), nre, pairs, ntilt,
+                     _dev.ptr(out), 0, ss)
+                out.mul_(scale)
+                t.host_i.copy_(out, non_blocking=True)
+            t.host_h.copy_(self.heights[t.vbeg:t.vbeg + n], non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(self.side)
+        t.done_event = done
+        t.stage = "copying"
+
+    def _eroding_descs(self):
+        er = [t for t in self.active if t.stage == "eroding"]
+        key = tuple(id(t) for t in er)
+        if key != self.eroding_key:
+            arr = (ErosionPlanet * max(1, len(er)))()
+            for q, t in enumerate(er):
+                m = t.mesh
+                arr[q].vbeg = t.vbeg
+                arr[q].n = m.n
+                arr[q].nbr = m.nbr.data_ptr()
+                arr[q].edge = m.edge.data_ptr()
+                arr[q].iters = t.request.erosion_iters
+                arr[q].rain = t.request.rain
+                arr[q].t_start = t.t_start
+                arr[q].slot = t.slot
+            host = _descs_tensor(arr)
+            with torch.cuda.stream(self.main):
+                self.desc_dev[:host.numel()].copy_(host, non_blocking=True)
+            self._descs_host = (arr, host)
+            self.eroding_key = key
+            return er, True
+        return er, False
+
+    def _step(self, now):
+        new = self._admit(now)
+        if new:
+            self.active.extend(new)
+            self._launch_new(new)
+        # planets whose noise is done join the erosion at this tick
+        for t in self.active:
+            if t.stage == "waiting":
+                self.main.wait_event(t.ready_event)
+                t.stage = "eroding"
+                t.t_start = self.tick
+            elif t.stage == "output":
+                self._output(t, after_main=False)
+        er, remap = self._eroding_descs()
+        if er:
+            arr, _ = self._descs_host
+            call("nx_erosion_tick", _dev.ptr(self.desc_dev), ctypes.cast(arr, ctypes.c_void_p), len(er), self.tick,
+                 _dev.ptr(self.st), _dev.ptr(self.st_tmp), _dev.ptr(self.ws), self.ws.numel(), self.nslots,
+                 1 if remap else 0, _dev.stream_handle(self.main))
+            for t in er:
+                if self.tick - t.t_start == t.request.erosion_iters - 1:
+                    self._output(t, after_main=True)
+            ev = torch.cuda.Event()
+            ev.record(self.main)
+            self._inflight.append(ev)
+            self.tick += 1
+        # bound the work queued ahead of the GPU
+        while len(self._inflight) > 2:
+            self._inflight.pop(0).synchronize()
+        self._collect()
+        return bool(er) or bool(new)
+
+    def _collect(self):
+        still = []
+        for t in self.active:
+            if t.stage == "copying" and t.done_event.query():
+                t.finished = time.perf_counter()
+                t.heights = t.host_h.numpy()
+                t.insolation = t.host_i.numpy() if t.host_i is not None else None
+                self.arena.release(t.vbeg, t.mesh.n)
+                self.free_slots.append(t.slot)
+                self.meshes.release(t.request.divisions)
+                t.stage = "done"
+                t.mesh = None
+                t._keep = None
+                self.done.append(t)
+            else:
+                still.append(t)
+        self.active = still
+
+    # ------------------------------------------------------------------
+    def run(self, stream, realtime=True, t0=None):
+        """Serve (arrival_offset_seconds, request) pairs; returns tickets in
+        request order with latencies (finish - arrival)."""
+        t0 = time.perf_counter() if t0 is None else t0
+        tickets = [self.submit(r, t0 + a, i) for i, (a, r) in enumerate(stream)]
+        if not realtime:
+            for t in tickets:
+                t.arrival = t0
+        while self.queue or self.active:
+            now = time.perf_counter()
+            busy = self._step(now)
+            if not busy and not any(t.stage == "copying" for t in self.active):
+                if self.queue and self.queue[0].arrival > now:
+                    time.sleep(min(self.queue[0].arrival - now, 0.002))
+                elif self.queue and not self.active:
+                    raise MemoryError("request does not fit the HBM budget even alone: %r" % (self.queue[0].request,))
+            elif not busy:
+                time.sleep(0.0002)
+        torch.cuda.synchronize()
+        return tickets
+
+
+def serve_plain(stream, meshes=None, realtime=True, t0=None):
+    """The comparator: requests handled one at a time, in arrival order, with
+    the plain per-planet path; returns (arrival, finish) per request."""
+    meshes = meshes if meshes is not None else ResidentMeshes(80 * 2**30)
+    t0 = time.perf_counter() if t0 is None else t0
+    out = []
+    for a, r in stream:
+        arrival = t0 + a if realtime else t0
+        now = time.perf_counter()
+        if now < arrival:
+            time.sleep(arrival - now)
+        res = _planets.generate_plain(r, meshes, sync=False)
+        h = res.heights.cpu()
+        i = res.insolation.cpu() if res.insolation is not None else None
+        torch.cuda.synchronize()
+        out.append((arrival, time.perf_counter(), h, i))
+    return out
+
+
+def poisson_stream(n=2000, rate=20.0, seed=11, k_lo=50, k_hi=2000, iters_hi=100):
+    """Request stream: gaps exponential(1/rate); divisions log-uniform in
+    [k_lo, k_hi]; octaves uniform in [4, 12]; iterations uniform in
+    [0, iters_hi]; insolation with probability 1/2; seed = request index."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n)
+    ks = np.round(np.exp(rng.uniform(np.log(k_lo), np.log(k_hi), n))).astype(int)
+    octs = rng.integers(4, 13, n)
+    its = rng.integers(0, iters_hi + 1, n)
+    ins = rng.random(n) < 0.5
+    t = np.cumsum(gaps)
+    return [(float(t[i]), _planets.PlanetRequest(seed=i, divisions=int(ks[i]), octaves=int(octs[i]),
+                                                 erosion_iters=int(its[i]), insolation=bool(ins[i])))
+            for i in range(n)]
+
+
+def latency_stats(lat):
+    lat = np.sort(np.asarray(lat))
+    return {"p50_ms": float(1e3 * np.percentile(lat, 50)), "p99_ms": float(1e3 * np.percentile(lat, 99)),
+            "mean_ms": float(1e3 * lat.mean()), "max_ms": float(1e3 * lat.max())}

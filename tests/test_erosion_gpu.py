@@ -216,7 +216,8 @@ def test_batched_planets_equal_planets_alone():
         dst[b:b + n, 0] = torch.from_numpy(hall[b:b + n]).cuda()
         dst[b:b + n, 2] = 1e-3
     arr = (_lib.ErosionPlanet * len(descs))(*[
-        _lib.ErosionPlanet(b, n, nb.data_ptr(), el.data_ptr(), it, 0.0) for (b, n, it), (nb, el) in zip(descs, meshes)])
+        _lib.ErosionPlanet(b, n, nb.data_ptr(), el.data_ptr(), it, 0.0, 0, q)
+        for q, ((b, n, it), (nb, el)) in enumerate(zip(descs, meshes))])
     pd = torch.from_numpy(np.frombuffer(bytes(arr), np.uint8).copy()).cuda()
     ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(N, len(descs))), dtype=torch.uint8, device="cuda")
     _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), len(descs), _dev.stream_handle())
