@@ -232,6 +232,13 @@ int nx_erosion_tick(const nx_erosion_planet *planets_dev, const nx_erosion_plane
                     float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes, int nslots, int remap,
                     void *stream);
 
+/* nticks consecutive ticks t, t+1, ... (one launch each) over the same
+ * planet list; a planet whose iterations end inside the range is skipped
+ * by the later launches and keeps its final state. */
+int nx_erosion_ticks(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets, int t,
+                     int nticks, float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes, int nslots,
+                     int remap, void *stream);
+
 /* After each listed planet's last iteration: record its final scale
  * exponent in its control block's K[0] (read by nx_erosion_store and
  * nx_erosion_heights_batch). */

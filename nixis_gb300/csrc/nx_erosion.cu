@@ -104,17 +104,19 @@ __device__ __forceinline__ double warp_sum(double v)
 // block's planet.  No barrier on the common path: every thread reads the
 // (broadcast) planet descriptor and control words itself, and each warp
 // folds its max into the planet's next slot with a reduction atomic.
-__global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
 {
     const int2 bm = a.blk_map[blockIdx.x];
     const int p = bm.x;
-    const nx_erosion_planet &P = a.planets[p];
+    const nx_erosion_planet P = a.planets[p];
     const int t = a.t - P.t_start;
     if (t < 0 || t >= P.iters) return;        // whole block: planet not stepping now
     nx_erosion_ctl *c = a.ctl + P.slot;
-    const float m = __uint_as_float(((volatile unsigned *)c->maxbits)[t % 3]);
+    // slots read here were written by earlier launches only (this launch
+    // writes the other slots), so ordinary cached loads are safe
+    const float m = __uint_as_float(__ldg(&c->maxbits[t % 3]));
     const int shift = m > RESCALE_ABOVE ? RESCALE_SHIFT : 0;
-    const int K = ((volatile int *)c->K)[t & 1] + shift;
+    const int K = __ldg(&c->K[t & 1]) + shift;
     const float lam = shift ? __int_as_float((127 - shift) << 23) : 1.0f;
     const float rain = scalbnf(P.rain, -K);
     if (bm.y == 0 && threadIdx.x == 0) {
@@ -143,13 +145,6 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
         float sed = si, wat = wi;
         const int nbr[6] = {n01.x, n01.y, n23.x, n23.y, n45.x, n45.y};
         const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
-        float4 o[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const int j = nbr[k];
-            const bool ok = j >= 0 && (int64_t)j < P.n;
-            o[k] = ok ? ist[P.vbeg + j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
         unsigned flow = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
@@ -159,9 +154,10 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
                 c->err = 1;
                 continue;
             }
-            const float wj = __fadd_rn(__fmul_rn(o[k].z, lam), rain);
+            const float4 o = ist[P.vbeg + j];
+            const float wj = __fadd_rn(__fmul_rn(o.z, lam), rain);
             // sign of the slope (erosion.py:230): sign of h_j - h_i
-            const float diff = __fadd_rn(__fsub_rn(__fmul_rn(o[k].x, lam), hh), __fsub_rn(__fmul_rn(o[k].y, lam), hl));
+            const float diff = __fadd_rn(__fsub_rn(__fmul_rn(o.x, lam), hh), __fsub_rn(__fmul_rn(o.y, lam), hl));
             if (diff > 0.0f) {
                 sed = __fadd_rn(sed, __fmul_rn(sol, wj));
                 wat = __fadd_rn(wat, __fmul_rn(wj, dd[k]));
@@ -188,17 +184,24 @@ __global__ void __launch_bounds__(BLOCK) erosion_step_kernel(StepArgs a)
         vmax = fmaxf(fabsf(nh), fmaxf(fabsf(wn), fabsf(sn)));
         if (a.mass) { sh = (double)nh + (double)nl; sw = (double)wn; ss = (double)sn; }
     }
-    // warp max -> the planet's max for the next iteration's rescale decision
-    // (NaN never wins fmaxf; an infinite value still triggers a rescale)
+    // block max -> the planet's max for the next iteration's rescale decision
+    // (one atomic per block; NaN never wins fmaxf; inf still triggers a rescale)
+    __shared__ float s_wmax[BLOCK / 32];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     vmax = warp_max(vmax);
-    if ((threadIdx.x & 31) == 0) atomicMax(&c->maxbits[(t + 1) % 3], __float_as_uint(vmax));
+    if (lane == 0) s_wmax[wid] = vmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float bmx = s_wmax[0];
+        for (int w = 1; w < BLOCK / 32; ++w) bmx = fmaxf(bmx, s_wmax[w]);
+        atomicMax(&c->maxbits[(t + 1) % 3], __float_as_uint(bmx));
+    }
     if (!a.mass) return;
 
     // per-iteration mass sums: block partials, then the planet's last block
     // reduces them in a fixed order (Neumaier), scaled back by 2^K
     __shared__ double s_wsum[BLOCK / 32][3];
     __shared__ bool s_last;
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     sh = warp_sum(sh); sw = warp_sum(sw); ss = warp_sum(ss);
     if (lane == 0) { s_wsum[wid][0] = sh; s_wsum[wid][1] = sw; s_wsum[wid][2] = ss; }
     __syncthreads();
@@ -534,9 +537,21 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
 
 // Serving: one launch advances every listed planet by one iteration, each
 // at its own iteration t - t_start (planets outside [0, iters) are skipped).
+NX_EXPORT int nx_erosion_ticks(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                               int nplanets, int t, int nticks, float *st_dev, float *st_tmp_dev, void *workspace,
+                               size_t ws_bytes, int nslots, int remap, void *stream);
+
 NX_EXPORT int nx_erosion_tick(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
                               int t, float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes, int nslots,
                               int remap, void *stream)
+{
+    return nx_erosion_ticks(planets_dev, planets_host, nplanets, t, 1, st_dev, st_tmp_dev, workspace, ws_bytes, nslots,
+                            remap, stream);
+}
+
+NX_EXPORT int nx_erosion_ticks(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                               int nplanets, int t, int nticks, float *st_dev, float *st_tmp_dev, void *workspace,
+                               size_t ws_bytes, int nslots, int remap, void *stream)
 {
     if (nplanets <= 0) return NX_OK;
     if (!planets_dev || !planets_host || !st_dev || !st_tmp_dev || !workspace || nslots <= 0)
@@ -569,9 +584,12 @@ NX_EXPORT int nx_erosion_tick(const nx_erosion_planet *planets_dev, const nx_ero
     a.mass = nullptr;
     a.mass_np = 0;
     a.flow = nullptr;
-    erosion_step_kernel<<<(unsigned)nblk, BLOCK, 0, s>>>(a);
-    NX_CHECK_LAUNCH("erosion_step_kernel");
-    nx::note_launch(1);
+    for (int q = 0; q < nticks; ++q) {
+        a.t = t + q;
+        erosion_step_kernel<<<(unsigned)nblk, BLOCK, 0, s>>>(a);
+        NX_CHECK_LAUNCH("erosion_step_kernel");
+        nx::note_launch(1);
+    }
     return NX_OK;
 }
 

@@ -3,7 +3,9 @@
 Requests (seed, divisions, octaves, erosion iterations, insolation) arrive
 over time.  The engine works in ticks; one tick is one erosion launch that
 advances every planet currently eroding by one iteration, each at its own
-iteration count (nx_erosion_tick).  Between ticks, arrived requests are
+iteration count (nx_erosion_ticks launches up to max_ticks of them per host
+step, stopping when an eroding planet finishes).  Between steps, arrived
+requests are
 admitted as memory frees up:
 
 * state rows come from a fixed arena (first fit, 256-row aligned) holding
@@ -160,7 +162,7 @@ def _descs_tensor(arr):
 class ServeEngine:
     """Continuous-batching planet generator over one GPU."""
 
-    def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None):
+    def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None, max_ticks=8):
         _dev.require_cuda()
         self.budget = int(hbm_budget)
         rows = arena_rows if arena_rows is not None else int(self.budget * arena_fraction) // ROW_BYTES
@@ -181,6 +183,7 @@ class ServeEngine:
         self.desc_dev = torch.empty(slots * ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device=dev)
         self.chunk = int(lib().nx_fbm_chunk_size())
         self.tick = 0
+        self.max_ticks = max_ticks
         self.queue = []          # arrived or future tickets, arrival order
         self.active = []         # admitted, not finished
         self.eroding_key = None
@@ -357,17 +360,22 @@ class ServeEngine:
                 self._output(t, after_main=False)
         er, remap = self._eroding_descs()
         if er:
+            # advance until the first eroding planet finishes, at most
+            # max_ticks per host step (new arrivals join at step boundaries)
+            left = min(t.t_start + t.request.erosion_iters - self.tick for t in er)
+            n = max(1, min(left, self.max_ticks))
             arr, _ = self._descs_host
-            call("nx_erosion_tick", _dev.ptr(self.desc_dev), ctypes.cast(arr, ctypes.c_void_p), len(er), self.tick,
-                 _dev.ptr(self.st), _dev.ptr(self.st_tmp), _dev.ptr(self.ws), self.ws.numel(), self.nslots,
+            call("nx_erosion_ticks", _dev.ptr(self.desc_dev), ctypes.cast(arr, ctypes.c_void_p), len(er), self.tick,
+                 n, _dev.ptr(self.st), _dev.ptr(self.st_tmp), _dev.ptr(self.ws), self.ws.numel(), self.nslots,
                  1 if remap else 0, _dev.stream_handle(self.main))
+            self.tick += n
             for t in er:
-                if self.tick - t.t_start == t.request.erosion_iters - 1:
+                if self.tick - t.t_start == t.request.erosion_iters:
+                    t.stage = "finishing"
                     self._output(t, after_main=True)
             ev = torch.cuda.Event()
             ev.record(self.main)
             self._inflight.append(ev)
-            self.tick += 1
         # bound the work queued ahead of the GPU
         while len(self._inflight) > 2:
             self._inflight.pop(0).synchronize()
