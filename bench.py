@@ -355,8 +355,10 @@ def bench_ours(args):
     vit = sum(r.n_vertices * r.erosion_iters for r in reqs)
     alg = vit * SAMPLE_ALG_BYTES
     achieved = alg / (ero_ms / 1e3) / 1e9
-    n_launch = sum(1 for t in range(batch.max_iters))
-    roofline = {"bound": "hbm", "kernel": "erosion_step_kernel", "achieved": achieved, "peak": peak,
+    n_launch = batch.erosion_launches()
+    blocked = any(batch.er_host[j].tiling for j in range(np_))
+    ero_kernel = "erosion_tb_kernel" if blocked else "erosion_step_kernel"
+    roofline = {"bound": "hbm", "kernel": ero_kernel, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "alg_bytes_per_vertex_iteration": SAMPLE_ALG_BYTES, "launches": n_launch,
                 "alg_bytes_per_launch": alg / max(n_launch, 1), "avg_launch_ms": ero_ms / max(n_launch, 1),

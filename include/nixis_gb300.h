@@ -161,6 +161,35 @@ int nx_sort_adjacency(const int32_t *adj_in_dev, int32_t *adj_out_dev, int64_t n
 int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, float *edge_dev, int *err_dev,
                     void *stream);
 
+/* Tiling of a mesh for temporally blocked erosion: every vertex belongs to
+ * one tile (a tile_side x tile_side square of its home face's grid); each
+ * tile lists its members, then `rings` rings of neighbours (local numbering),
+ * and, for members and rings 1..rings-1, the six neighbours as local
+ * indices and the six edge lengths. */
+typedef struct nx_tiling {
+    int32_t ntiles;
+    int32_t rings;
+    int32_t nmax;              /* local vertices per tile (capacity) */
+    int32_t cmax;              /* updatable vertices per tile (capacity) */
+    const int32_t *counts;     /* ntiles x (rings + 1): members, then each ring's size */
+    const int32_t *ids;        /* ntiles x nmax global vertex ids */
+    const uint16_t *lnbr;      /* ntiles x cmax x 6 local neighbour indices, 0xFFFF = none */
+    const float *ledge;        /* ntiles x cmax x 6 edge lengths */
+} nx_tiling;
+
+/* Host: sizes of the tiling of divisions k. */
+int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax);
+
+/* Build a tiling from the mesh's neighbour table and edge lengths into
+ * caller buffers sized by nx_tiling_shape (counts int32[ntiles*(rings+1)],
+ * ids int32[ntiles*nmax], lnbr uint16[ntiles*cmax*6], ledge
+ * float[ntiles*cmax*6]).  err_dev (device int[3], caller zeroes it):
+ * [0] bit 0 = a tile exceeded nmax members, bit 1 = a halo or neighbour
+ * problem; [1] largest local vertex count; [2] largest updatable count. */
+int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nbr_dev, const float *edge_dev,
+                    int32_t *counts_dev, int32_t *ids_dev, uint16_t *lnbr_dev, float *ledge_dev, int *err_dev,
+                    void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Erosion (variant 3)                                                 */
 /* ------------------------------------------------------------------ */
@@ -183,6 +212,9 @@ typedef struct nx_erosion_planet {
     float rain;
     int32_t t_start;
     int32_t slot;
+    const nx_tiling *tiling;   /* device copy of the mesh's tiling, or NULL */
+    int32_t ntiles;            /* its ntiles (read on the host) */
+    int32_t maxnl;             /* its largest local vertex count */
 } nx_erosion_planet;
 
 /* Workspace bytes for erosion over n_padded_total state rows (a bound on
@@ -214,8 +246,12 @@ int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, f
                      int iters, float rain, nx_erosion_planet *planet_dev, double *mass_dev, uint16_t *flow_dev,
                      void *workspace, size_t ws_bytes, void *stream);
 
-/* Batched erosion: every planet runs its own iteration count, one launch
- * per iteration over the planets still running.  A planet's state starts
+/* Batched erosion: every planet runs its own iteration count.  If every
+ * planet has a tiling (with tiling->rings = R) and neither mass sums nor
+ * flow bits are requested, iterations run temporally blocked: one launch per
+ * pass of up to R iterations, each block updating one tile in shared
+ * memory; otherwise one launch per iteration over the planets still
+ * running.  Both give the same results.  A planet's state starts
  * in buffer (iters & 1) -- 0: st_dev, 1: st_tmp_dev -- and ends in st_dev.
  * mass_dev (optional): float64[max_iters][nplanets][3].  Call
  * nx_erosion_ctl_init first. */
@@ -243,6 +279,11 @@ int nx_erosion_ticks(const nx_erosion_planet *planets_dev, const nx_erosion_plan
  * exponent in its control block's K[0] (read by nx_erosion_store and
  * nx_erosion_heights_batch). */
 int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
+
+/* Temporal blocking settings: the ring count of the tilings that batches
+ * use (passes have up to that many iterations) and whether batches with
+ * tilings use it (1) or run one iteration per launch (0). */
+int nx_erosion_tb_config(int rings, int enabled);
 
 /* Write one planet's state back as binary64 true values (h_hi + h_lo, w, s
  * times 2^K, K from the workspace's first control block).  w64_dev /

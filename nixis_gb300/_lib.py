@@ -50,6 +50,9 @@ SIGNATURES = {
     "nx_erosion_tick": (_i32, [_p, _p, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_finish": (_i32, [_p, _i32, _p, _p]),
     "nx_erosion_ticks": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
+    "nx_tiling_shape": (_i32, [_i32, _i32, _i32, _p, _p, _p]),
+    "nx_erosion_tb_config": (_i32, [_i32, _i32]),
+    "nx_tiling_build": (_i32, [_i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p]),
 }
 
 NX_MAX_OCTAVES = 32
@@ -74,7 +77,15 @@ class ErosionPlanet(ctypes.Structure):
     """nx_erosion_planet (include/nixis_gb300.h)."""
     _fields_ = [("vbeg", ctypes.c_int64), ("n", ctypes.c_int64), ("nbr", ctypes.c_void_p),
                 ("edge", ctypes.c_void_p), ("iters", ctypes.c_int32), ("rain", ctypes.c_float),
-                ("t_start", ctypes.c_int32), ("slot", ctypes.c_int32)]
+                ("t_start", ctypes.c_int32), ("slot", ctypes.c_int32), ("tiling", ctypes.c_void_p),
+                ("ntiles", ctypes.c_int32), ("maxnl", ctypes.c_int32)]
+
+
+class Tiling(ctypes.Structure):
+    """nx_tiling (include/nixis_gb300.h)."""
+    _fields_ = [("ntiles", ctypes.c_int32), ("rings", ctypes.c_int32), ("nmax", ctypes.c_int32),
+                ("cmax", ctypes.c_int32), ("counts", ctypes.c_void_p), ("ids", ctypes.c_void_p),
+                ("lnbr", ctypes.c_void_p), ("ledge", ctypes.c_void_p)]
 
 _lock = threading.Lock()
 _LIB = None

@@ -78,6 +78,42 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float b)
     lo = __fsub_rn(e, __fsub_rn(hi, s));
 }
 
+// One neighbour's contribution (erosion.py:223-247): the flow choice is the
+// sign of h_j - h_i from the height pairs; returns 1 (higher), 2 (lower), 0.
+__device__ __forceinline__ unsigned erode_accum(float hh, float hl, float hjh, float hjl, float wj, float d, float &sed,
+                                                float &wat)
+{
+    const float diff = __fadd_rn(__fsub_rn(hjh, hh), __fsub_rn(hjl, hl));
+    if (diff > 0.0f) {
+        sed = __fadd_rn(sed, __fmul_rn(c_sol, wj));
+        wat = __fadd_rn(wat, __fmul_rn(wj, d));
+        return 1u;
+    }
+    if (diff < 0.0f) {
+        sed = __fsub_rn(sed, __fmul_rn(c_sol, wj));
+        wat = __fsub_rn(wat, __fmul_rn(wj, d));
+        return 2u;
+    }
+    return 0u;
+}
+
+// erosion.py:262-267: new height pair, sediment and water.
+__device__ __forceinline__ void erode_finish(float hh, float hl, float wi, float si, float sed, float wat, float &nh,
+                                             float &nl, float &wn, float &sn)
+{
+    nh = hh;
+    nl = hl;
+    df_add(nh, nl, -sed);
+    sn = __fadd_rn(si, sed);
+    wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, c_evap)));
+    const float cw = __fmul_rn(c_cap, wn);
+    if (sn > cw) {
+        const float ex = __fsub_rn(sn, cw);
+        df_add(nh, nl, ex);
+        sn = __fsub_rn(sn, ex);
+    }
+}
+
 __device__ __forceinline__ int find_planet(const nx_erosion_planet *P, int np, int64_t v)
 {
     int lo = 0, hi = np - 1;
@@ -133,7 +169,6 @@ __global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
     float vmax = 0.0f;
     double sh = 0.0, sw = 0.0, ss = 0.0;
     if (li < P.n) {
-        const float sol = c_sol, evap = c_evap, cap = c_cap;
         const int2 *nb2 = reinterpret_cast<const int2 *>(P.nbr + 6 * li);
         const float2 *el2 = reinterpret_cast<const float2 *>(P.edge + 6 * li);
         const int2 n01 = nb2[0], n23 = nb2[1], n45 = nb2[2];
@@ -156,29 +191,10 @@ __global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
             }
             const float4 o = ist[P.vbeg + j];
             const float wj = __fadd_rn(__fmul_rn(o.z, lam), rain);
-            // sign of the slope (erosion.py:230): sign of h_j - h_i
-            const float diff = __fadd_rn(__fsub_rn(__fmul_rn(o.x, lam), hh), __fsub_rn(__fmul_rn(o.y, lam), hl));
-            if (diff > 0.0f) {
-                sed = __fadd_rn(sed, __fmul_rn(sol, wj));
-                wat = __fadd_rn(wat, __fmul_rn(wj, dd[k]));
-                flow |= 1u << (2 * k);
-            } else if (diff < 0.0f) {
-                sed = __fsub_rn(sed, __fmul_rn(sol, wj));
-                wat = __fsub_rn(wat, __fmul_rn(wj, dd[k]));
-                flow |= 2u << (2 * k);
-            }
+            flow |= erode_accum(hh, hl, __fmul_rn(o.x, lam), __fmul_rn(o.y, lam), wj, dd[k], sed, wat) << (2 * k);
         }
-        // erosion.py:262-267
-        float nh = hh, nl = hl;
-        df_add(nh, nl, -sed);
-        float sn = __fadd_rn(si, sed);
-        const float wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, evap)));
-        const float cw = __fmul_rn(cap, wn);
-        if (sn > cw) {
-            const float ex = __fsub_rn(sn, cw);
-            df_add(nh, nl, ex);
-            sn = __fsub_rn(sn, ex);
-        }
+        float nh, nl, wn, sn;
+        erode_finish(hh, hl, wi, si, sed, wat, nh, nl, wn, sn);
         ost[i] = make_float4(nh, nl, wn, sn);
         if (a.flow) a.flow[li] = (uint16_t)flow;
         vmax = fmaxf(fabsf(nh), fmaxf(fabsf(wn), fabsf(sn)));
@@ -249,6 +265,184 @@ __global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
         mrow[0] = out[0]; mrow[1] = out[1]; mrow[2] = out[2];
         c->done = 0u;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Temporally blocked erosion: one block per (planet, tile) runs a pass of up
+// to R iterations in shared memory.  It loads the tile and its halo rings
+// (state * lambda), then for m = 0..len-1 updates the members and the rings
+// that the remaining iterations still need (ring set shrinks by one per
+// iteration), and writes the members' final state.  Per vertex the
+// arithmetic is erode_accum / erode_finish in slot order, as in the
+// iteration-at-a-time kernel, so the results are the same.  Global buffers
+// alternate per pass; a planet makes np passes with np = iters (mod 2), so
+// its state starts in buffer (iters & 1) and ends in buffer 0, like the
+// iteration-at-a-time path.
+
+__host__ __device__ __forceinline__ int tb_npass(int iters, int R)
+{
+    if (iters <= 0) return 0;
+    int np = (iters + R - 1) / R;
+    if ((np ^ iters) & 1) ++np;
+    return np;
+}
+
+// Length of pass q: greedy, each later pass keeps at least one iteration.
+__host__ __device__ __forceinline__ int tb_len(int iters, int R, int np, int q)
+{
+    int done = 0;
+    for (int x = 0; x < q; ++x) {
+        int l = iters - done - (np - 1 - x);
+        done += l < R ? l : R;
+    }
+    int l = iters - done - (np - 1 - q);
+    return l < R ? l : R;
+}
+
+struct TbArgs {
+    const nx_erosion_planet *planets;
+    const int2 *blk_map;   // (planet, tile), planets ordered by pass count, descending
+    int pass;
+    int R;
+    int smem_n;            // floats per shared array (>= every tile's local count)
+    float4 *st0;
+    float4 *st1;
+    nx_erosion_ctl *ctl;
+};
+
+constexpr int TB_THREADS = 512;
+
+__global__ void __launch_bounds__(TB_THREADS, 2) erosion_tb_kernel(TbArgs a)
+{
+    extern __shared__ float tsm[];
+    const int2 bm = a.blk_map[blockIdx.x];
+    const nx_erosion_planet P = a.planets[bm.x];
+    const int R = a.R;
+    const int np = tb_npass(P.iters, R);
+    const int q = a.pass;
+    if (q >= np) return;
+    const int len = tb_len(P.iters, R, np, q);
+    const nx_tiling TL = *P.tiling;
+    const int tile = bm.y;
+    const int32_t *cnt = TL.counts + (int64_t)tile * (TL.rings + 1);
+    const int T = cnt[0];
+    int NL = T;
+    for (int r = 1; r <= len; ++r) NL += cnt[r];
+    nx_erosion_ctl *c = a.ctl + P.slot;
+    // rescale per pass: growth is below 16x per iteration, so a max under
+    // 2^(96 - 4R) stays under 2^96 through the pass
+    const float m = __uint_as_float(__ldg(&c->maxbits[q % 3]));
+    const float thr = __int_as_float((127 + 96 - 4 * R) << 23);
+    const int shift = m > thr ? RESCALE_SHIFT : 0;
+    const int K = __ldg(&c->K[q & 1]) + shift;
+    const float lam = shift ? __int_as_float((127 - shift) << 23) : 1.0f;
+    const float rain = scalbnf(P.rain, -K);
+    if (tile == 0 && threadIdx.x == 0) {
+        c->K[(q + 1) & 1] = K;
+        c->maxbits[(q + 2) % 3] = 0u;
+    }
+    if (T == 0) return;
+    const bool par = ((np - q) & 1) != 0;
+    const float4 *__restrict__ ist = par ? a.st1 : a.st0;
+    float4 *__restrict__ ost = par ? a.st0 : a.st1;
+    const int S = a.smem_n;
+    float *b0h = tsm, *b0l = tsm + S, *b0w = tsm + 2 * S, *b0s = tsm + 3 * S;
+    float *b1h = tsm + 4 * S, *b1l = tsm + 5 * S, *b1w = tsm + 6 * S, *b1s = tsm + 7 * S;
+    const int32_t *ids = TL.ids + (int64_t)tile * TL.nmax;
+    for (int l = threadIdx.x; l < NL; l += blockDim.x) {
+        const float4 x = ist[P.vbeg + ids[l]];
+        b0h[l] = __fmul_rn(x.x, lam);
+        b0l[l] = __fmul_rn(x.y, lam);
+        b0w[l] = __fmul_rn(x.z, lam);
+        b0s[l] = __fmul_rn(x.w, lam);
+    }
+    __syncthreads();
+    const uint32_t *lnb = reinterpret_cast<const uint32_t *>(TL.lnbr) + (int64_t)tile * TL.cmax * 3;
+    const float2 *led = reinterpret_cast<const float2 *>(TL.ledge) + (int64_t)tile * TL.cmax * 3;
+    int C = NL - cnt[len];                      // members + rings 1..len-1
+    for (int mi = 0; mi < len; ++mi) {
+        const bool odd = mi & 1;
+        const float *ch = odd ? b1h : b0h, *cl = odd ? b1l : b0l, *cw = odd ? b1w : b0w, *cs = odd ? b1s : b0s;
+        float *nh_ = odd ? b0h : b1h, *nl_ = odd ? b0l : b1l, *nw_ = odd ? b0w : b1w, *ns_ = odd ? b0s : b1s;
+        for (int l = threadIdx.x; l < C; l += blockDim.x) {
+            const uint32_t p01 = lnb[3 * l], p23 = lnb[3 * l + 1], p45 = lnb[3 * l + 2];
+            const float2 d01 = led[3 * l], d23 = led[3 * l + 1], d45 = led[3 * l + 2];
+            const uint32_t nb[6] = {p01 & 0xFFFFu, p01 >> 16, p23 & 0xFFFFu, p23 >> 16, p45 & 0xFFFFu, p45 >> 16};
+            const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
+            const float hh = ch[l], hl = cl[l];
+            const float wi = __fadd_rn(cw[l], rain);
+            const float si = cs[l];
+            float sed = si, wat = wi;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const uint32_t j = nb[k];
+                if (j == 0xFFFFu) continue;
+                erode_accum(hh, hl, ch[j], cl[j], __fadd_rn(cw[j], rain), dd[k], sed, wat);
+            }
+            float nh, nl, wn, sn;
+            erode_finish(hh, hl, wi, si, sed, wat, nh, nl, wn, sn);
+            nh_[l] = nh;
+            nl_[l] = nl;
+            nw_[l] = wn;
+            ns_[l] = sn;
+        }
+        __syncthreads();
+        if (mi + 1 < len) C -= cnt[len - 1 - mi];
+    }
+    const bool fin = len & 1;
+    const float *fh = fin ? b1h : b0h, *fl = fin ? b1l : b0l, *fw = fin ? b1w : b0w, *fs = fin ? b1s : b0s;
+    float vmax = 0.0f;
+    for (int l = threadIdx.x; l < T; l += blockDim.x) {
+        const float4 v = make_float4(fh[l], fl[l], fw[l], fs[l]);
+        ost[P.vbeg + ids[l]] = v;
+        vmax = fmaxf(vmax, fmaxf(fabsf(v.x), fmaxf(fabsf(v.z), fabsf(v.w))));
+    }
+    __shared__ float s_wmax[TB_THREADS / 32];
+    vmax = warp_max(vmax);
+    if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = vmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float bmx = s_wmax[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bmx = fmaxf(bmx, s_wmax[w]);
+        atomicMax(&c->maxbits[(q + 1) % 3], __float_as_uint(bmx));
+    }
+}
+
+// Block map of a temporally blocked run: planets ordered by pass count
+// (descending, then index), each contributing one block per tile.
+__global__ void erosion_tb_map_kernel(const nx_erosion_planet *__restrict__ P, int np, int R, int2 *__restrict__ map)
+{
+    const int p = blockIdx.x;
+    if (p >= np) return;
+    __shared__ int64_t s_b0;
+    const int mine = tb_npass(P[p].iters, R);
+    if (threadIdx.x == 0) {
+        int64_t b0 = 0;
+        for (int q = 0; q < np; ++q) {
+            const int other = tb_npass(P[q].iters, R);
+            if (other > mine || (other == mine && q < p)) b0 += P[q].ntiles;
+        }
+        s_b0 = b0;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < P[p].ntiles; j += blockDim.x) map[s_b0 + j] = make_int2(p, j);
+}
+
+__global__ void erosion_tb_rebase_kernel(const nx_erosion_planet *__restrict__ P, int np, int R,
+                                         nx_erosion_ctl *__restrict__ ctl)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int n = tb_npass(P[p].iters, R);
+    if (n <= 0) return;
+    nx_erosion_ctl &c = ctl[P[p].slot];
+    const unsigned m = c.maxbits[n % 3];
+    const int K = c.K[n & 1];
+    c.maxbits[0] = m;
+    c.maxbits[1] = 0u;
+    c.maxbits[2] = 0u;
+    c.K[0] = K;
+    c.K[1] = K;
 }
 
 // Block map of a launch: planet p owns blocks [sum of earlier planets'
@@ -475,6 +669,19 @@ NX_EXPORT int nx_erosion_load(const double *h64_dev, const double *w64_dev, cons
 
 static int64_t planet_blocks(const nx_erosion_planet &P) { return (P.n + BLOCK - 1) / BLOCK; }
 
+// Temporal blocking: rings of the tilings in use (all planets of a batch
+// share it) and a switch for comparisons.
+static int g_tb_rings = 4;
+static bool g_tb_enabled = true;
+
+NX_EXPORT int nx_erosion_tb_config(int rings, int enabled)
+{
+    if (rings < 1 || rings > 8) return nx::fail(NX_EINVAL, "nx_erosion_tb_config: rings must be in [1, 8]");
+    g_tb_rings = rings;
+    g_tb_enabled = enabled != 0;
+    return NX_OK;
+}
+
 // Batch: planets packed by non-increasing iteration count, so the planets
 // still running at iteration t are a prefix of the block map.
 static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
@@ -496,6 +703,72 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         if (P.iters > max_it) max_it = P.iters;
         if (P.vbeg + P.n > total) total = P.vbeg + P.n;
         nblk += planet_blocks(P);
+    }
+    // temporally blocked when every planet has a tiling and nothing per
+    // iteration (mass sums, flow bits) is requested
+    bool tb = !mass_dev && !flow_dev && g_tb_enabled;
+    int R = 0, maxnl = 0;
+    int64_t ntiles_all = 0;
+    for (int p = 0; p < np && tb; ++p) {
+        const nx_erosion_planet &P = planets_host[p];
+        if (P.iters == 0) {
+            if (P.tiling && P.ntiles > 0) ntiles_all += P.ntiles;
+            continue;
+        }
+        if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0) { tb = false; break; }
+        ntiles_all += P.ntiles;
+        if (P.maxnl > maxnl) maxnl = P.maxnl;
+    }
+    if (maxnl == 0) tb = false;
+    if (tb) {
+        R = g_tb_rings;
+        const size_t smem = 8 * sizeof(float) * (size_t)maxnl;
+        if (smem > 200 * 1024) tb = false;
+    }
+    if (tb) {
+        if (ws_bytes < nx_erosion_workspace_size((ntiles_all > nblk ? ntiles_all : nblk) * BLOCK, np))
+            return nx::fail(NX_EINVAL, "erosion: workspace too small");
+        Workspace w = carve(workspace, np, ntiles_all > nblk ? ntiles_all : nblk);
+        static bool attr_done[64] = {false};
+        int dev = 0;
+        NX_CHECK_CUDA(cudaGetDevice(&dev));
+        if (dev >= 0 && dev < 64 && !attr_done[dev]) {
+            NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            attr_done[dev] = true;
+        }
+        erosion_tb_map_kernel<<<np, 256, 0, s>>>(planets_dev, np, R, w.blk_map);
+        NX_CHECK_LAUNCH("erosion_tb_map_kernel");
+        nx::note_launch(1);
+        int maxpass = 0;
+        for (int p = 0; p < np; ++p) {
+            const int n = tb_npass(planets_host[p].iters, R);
+            if (n > maxpass) maxpass = n;
+        }
+        TbArgs ta;
+        ta.planets = planets_dev;
+        ta.blk_map = w.blk_map;
+        ta.R = R;
+        ta.smem_n = maxnl;
+        ta.st0 = (float4 *)st_dev;
+        ta.st1 = (float4 *)st_tmp;
+        ta.ctl = w.ctl;
+        const size_t smem = 8 * sizeof(float) * (size_t)maxnl;
+        for (int q = 0; q < maxpass; ++q) {
+            int64_t grid = 0;
+            for (int p = 0; p < np; ++p)
+                if (tb_npass(planets_host[p].iters, R) > q) grid += planets_host[p].ntiles;
+            if (grid <= 0) break;
+            ta.pass = q;
+            erosion_tb_kernel<<<(unsigned)grid, TB_THREADS, smem, s>>>(ta);
+            NX_CHECK_LAUNCH("erosion_tb_kernel");
+            nx::note_launch(1);
+        }
+        if (maxpass > 0) {
+            erosion_tb_rebase_kernel<<<(np + 127) / 128, 128, 0, s>>>(planets_dev, np, R, w.ctl);
+            NX_CHECK_LAUNCH("erosion_tb_rebase_kernel");
+            nx::note_launch(1);
+        }
+        return NX_OK;
     }
     if (ws_bytes < nx_erosion_workspace_size(nblk * BLOCK, np)) return nx::fail(NX_EINVAL, "erosion: workspace too small");
     Workspace w = carve(workspace, np, nblk);

@@ -24,6 +24,15 @@ struct IcoTables {
 
 __constant__ IcoTables c_ico;
 
+// Home face of every corner and edge (the lowest-numbered face containing
+// it), used to give every vertex one (face, i, j) grid position for tiling.
+struct IcoHome {
+    int corner_face[12], corner_which[12];        // which: 0 = A, 1 = B, 2 = C of that face
+    int edge_face[30], edge_side[30], edge_fwd[30];  // side: 0 = AB, 1 = AC, 2 = BC
+};
+
+__constant__ IcoHome c_home;
+
 // Point = normalise(w0*A + w1*B + w2*C), sums in the written order, no FMA.
 __device__ __forceinline__ void blend3(const double *A, const double *B, const double *C, double w0, double w1,
                                        double w2, double *out)
@@ -41,6 +50,24 @@ __device__ __forceinline__ void blend2(const double *A, const double *B, double 
     for (int c = 0; c < 3; ++c) p[c] = __dadd_rn(__dmul_rn(w0, A[c]), __dmul_rn(w1, B[c]));
     double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])), __dmul_rn(p[2], p[2])));
     for (int c = 0; c < 3; ++c) out[c] = __ddiv_rn(p[c], r);
+}
+
+// Face-interior offset q -> (face, i, j): rows i = 1..k-2 hold k-1-i points.
+__device__ __forceinline__ void interior_fij(int64_t q, int k, int &f, int &i, int &j)
+{
+    const int64_t npf = (int64_t)(k - 1) * (k - 2) / 2;
+    f = (int)(q / npf);
+    const int64_t off = q - (int64_t)f * npf;
+    const double kk = (double)k;
+    const double disc = (2.0 * kk - 3.0) * (2.0 * kk - 3.0) - 8.0 * (double)off;
+    int ii = (int)floor(((2.0 * kk - 3.0) - sqrt(disc > 0 ? disc : 0.0)) / 2.0) + 1;
+    if (ii < 1) ii = 1;
+    if (ii > k - 2) ii = k - 2;
+    auto start = [&](int a) -> int64_t { return (int64_t)(a - 1) * (k - 1) - (int64_t)(a - 1) * a / 2; };
+    while (ii > 1 && start(ii) > off) --ii;
+    while (ii < k - 2 && start(ii + 1) <= off) ++ii;
+    i = ii;
+    j = (int)(off - start(ii)) + 1;
 }
 
 __global__ void ico_vertices_kernel(int k, int64_t nv, double *__restrict__ xyz)
@@ -261,6 +288,20 @@ int upload_tables(const double *corners, const int *faces, const int *fedge, con
         t.edge[e][1] = edges[2 * e + 1];
     }
     NX_CHECK_CUDA(cudaMemcpyToSymbol(c_ico, &t, sizeof(t)));
+    IcoHome h;
+    for (int c = 0; c < 12; ++c) {
+        h.corner_face[c] = -1;
+        for (int f = 0; f < 20 && h.corner_face[c] < 0; ++f)
+            for (int w = 0; w < 3; ++w)
+                if (t.face[f][w] == c) { h.corner_face[c] = f; h.corner_which[c] = w; break; }
+    }
+    for (int e = 0; e < 30; ++e) {
+        h.edge_face[e] = -1;
+        for (int f = 0; f < 20 && h.edge_face[e] < 0; ++f)
+            for (int sd = 0; sd < 3; ++sd)
+                if (t.fedge[f][sd][0] == e) { h.edge_face[e] = f; h.edge_side[e] = sd; h.edge_fwd[e] = t.fedge[f][sd][1]; break; }
+    }
+    NX_CHECK_CUDA(cudaMemcpyToSymbol(c_home, &h, sizeof(h)));
     if (dev >= 0 && dev < 64) g_tables_ready[dev] = true;
     return NX_OK;
 }
@@ -344,5 +385,240 @@ NX_EXPORT int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int
     edge_len_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, edge_dev, err_dev);
     NX_CHECK_LAUNCH("edge_len_kernel");
     nx::note_launch(1);
+    return NX_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Tiling for temporally blocked erosion.
+//
+// Every vertex gets one grid position (face, i, j) in its home face (corners
+// and edge vertices belong to the lowest-numbered face containing them);
+// tile (f, i / B, j / B) collects it.  For each tile a block then collects
+// the R rings of neighbours around it (breadth first over the neighbour
+// table, with a shared-memory hash set), numbers them locally (members,
+// ring 1, ..., ring R) and stores, for every vertex that a pass can update
+// (members and rings 1..R-1), its six neighbours as local indices and its
+// six edge lengths.
+
+namespace {
+
+__device__ __forceinline__ void home_of(int64_t v, int k, int &f, int &i, int &j)
+{
+    const int64_t ne = (int64_t)30 * (k - 1);
+    if (v < 12) {
+        f = c_home.corner_face[v];
+        const int w = c_home.corner_which[v];
+        i = w == 1 ? k : 0;
+        j = w == 2 ? k : 0;
+    } else if (v < 12 + ne) {
+        const int64_t q = v - 12;
+        const int e = (int)(q / (k - 1));
+        const int t = (int)(q - (int64_t)e * (k - 1)) + 1;
+        f = c_home.edge_face[e];
+        const int pos = c_home.edge_fwd[e] ? t : k - t;
+        const int sd = c_home.edge_side[e];
+        if (sd == 0) { i = pos; j = 0; }
+        else if (sd == 1) { i = 0; j = pos; }
+        else { i = k - pos; j = pos; }
+    } else {
+        interior_fij(v - 12 - ne, k, f, i, j);
+    }
+}
+
+__device__ __forceinline__ int64_t tile_of(int f, int i, int j, int B, int M)
+{
+    const int ti = i / B, tj = j / B;
+    const int64_t tpf = (int64_t)(M + 1) * (M + 2) / 2;
+    return (int64_t)f * tpf + (int64_t)ti * (M + 1) - (int64_t)ti * (ti - 1) / 2 + tj;
+}
+
+__global__ void tile_assign_kernel(int k, int B, int64_t nv, int R, int nmax, int32_t *__restrict__ counts,
+                                   int32_t *__restrict__ ids, int *__restrict__ err)
+{
+    const int M = k / B;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        int f, i, j;
+        home_of(v, k, f, i, j);
+        const int64_t t = tile_of(f, i, j, B, M);
+        const int pos = atomicAdd(&counts[t * (R + 1)], 1);
+        if (pos < nmax) ids[t * nmax + pos] = (int32_t)v;
+        else atomicOr(err, 1);
+    }
+}
+
+constexpr int HASH_BITS = 13;                 // 8192-entry set per tile
+constexpr int HASH_CAP = 1 << HASH_BITS;
+
+__device__ __forceinline__ uint32_t hslot(int32_t v) { return ((uint32_t)v * 2654435761u) >> (32 - HASH_BITS); }
+
+// Insert v (bounded probing); returns its local index, assigning the next
+// one if v is new.  -1 if the set or the list is full.
+__device__ __forceinline__ int hinsert(int32_t *key, int32_t *val, int32_t *list, int *cnt, int nmax, int32_t v)
+{
+    uint32_t h = hslot(v);
+    for (int probe = 0; probe < HASH_CAP; ++probe) {
+        const int32_t old = atomicCAS(&key[h], -1, v);
+        if (old == -1) {
+            const int idx = atomicAdd(cnt, 1);
+            if (idx >= nmax) { val[h] = -1; return -1; }
+            list[idx] = v;
+            val[h] = idx;
+            return idx;
+        }
+        if (old == v) return 0;       // present (its index is read after a barrier)
+        h = (h + 1) & (HASH_CAP - 1);
+    }
+    return -1;
+}
+
+__device__ __forceinline__ int hfind(const int32_t *key, const int32_t *val, int32_t v)
+{
+    uint32_t h = hslot(v);
+    for (int probe = 0; probe < HASH_CAP; ++probe) {
+        const int32_t kk = key[h];
+        if (kk == v) return val[h];
+        if (kk == -1) return -1;
+        h = (h + 1) & (HASH_CAP - 1);
+    }
+    return -1;
+}
+
+__global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restrict__ nbr, const float *__restrict__ edge,
+                                                         int64_t nv, int R, int nmax, int cmax, int32_t *__restrict__ counts,
+                                                         int32_t *__restrict__ ids, uint16_t *__restrict__ lnbr,
+                                                         float *__restrict__ ledge, int *__restrict__ err)
+{
+    extern __shared__ int32_t sh[];
+    int32_t *key = sh;                      // HASH_CAP
+    int32_t *val = key + HASH_CAP;          // HASH_CAP
+    int32_t *list = val + HASH_CAP;         // nmax (padded to a power of two for the sort)
+    __shared__ int s_cnt, s_bad;
+    __shared__ int s_ring[16];
+    const int64_t tile = blockIdx.x;
+    int32_t *tc = counts + tile * (R + 1);
+    int32_t *tid = ids + tile * nmax;
+    int T = tc[0];
+    if (T > nmax) T = nmax;
+    int P2 = 1;
+    while (P2 < T) P2 <<= 1;
+    for (int q = threadIdx.x; q < HASH_CAP; q += blockDim.x) key[q] = -1;
+    for (int q = threadIdx.x; q < P2; q += blockDim.x) list[q] = q < T ? tid[q] : 0x7FFFFFFF;
+    if (threadIdx.x == 0) { s_cnt = 0; s_bad = 0; }
+    __syncthreads();
+    // members in ascending id order (row segments -> coalesced accesses)
+    for (int size = 2; size <= P2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int q = threadIdx.x; q < P2; q += blockDim.x) {
+                const int o = q ^ stride;
+                if (o > q) {
+                    const bool up = (q & size) == 0;
+                    const int32_t a = list[q], b = list[o];
+                    if ((a > b) == up) { list[q] = b; list[o] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    for (int q = threadIdx.x; q < T; q += blockDim.x) {
+        // members take local indices 0..T-1 in sorted order
+        const int32_t v = list[q];
+        uint32_t h = hslot(v);
+        for (int probe = 0; probe < HASH_CAP; ++probe) {
+            if (atomicCAS(&key[h], -1, v) == -1) { val[h] = q; break; }
+            h = (h + 1) & (HASH_CAP - 1);
+        }
+    }
+    if (threadIdx.x == 0) s_cnt = T;
+    __syncthreads();
+    int beg = 0, end = T;
+    for (int r = 1; r <= R; ++r) {
+        const int nwork = (end - beg) * 6;
+        for (int w = threadIdx.x; w < nwork; w += blockDim.x) {
+            const int32_t v = list[beg + w / 6];
+            const int32_t j = nbr[6 * (int64_t)v + (w % 6)];
+            if (j < 0) continue;
+            if ((int64_t)j >= nv) { s_bad = 1; continue; }
+            if (hinsert(key, val, list, &s_cnt, nmax, j) < 0) s_bad = 1;
+        }
+        __syncthreads();
+        beg = end;
+        end = min(s_cnt, nmax);
+        if (threadIdx.x == 0) s_ring[r] = end - beg;
+        __syncthreads();
+    }
+    const int NL = end;
+    int C0 = T;
+    for (int r = 1; r < R; ++r) C0 += s_ring[r];
+    if (C0 > cmax) { if (threadIdx.x == 0) s_bad = 1; C0 = cmax; }
+    __syncthreads();
+    for (int q = threadIdx.x; q < NL; q += blockDim.x) tid[q] = list[q];
+    for (int w = threadIdx.x; w < C0 * 6; w += blockDim.x) {
+        const int q = w / 6, sl = w % 6;
+        const int32_t v = list[q];
+        const int32_t j = nbr[6 * (int64_t)v + sl];
+        int loc = -1;
+        if (j >= 0) {
+            loc = hfind(key, val, j);
+            if (loc < 0) s_bad = 1;
+        }
+        lnbr[((int64_t)tile * cmax + q) * 6 + sl] = loc < 0 ? (uint16_t)0xFFFF : (uint16_t)loc;
+        ledge[((int64_t)tile * cmax + q) * 6 + sl] = edge[6 * (int64_t)v + sl];
+    }
+    if (threadIdx.x == 0) {
+        tc[0] = T;
+        for (int r = 1; r <= R; ++r) tc[r] = s_ring[r];
+        atomicMax(&err[1], NL);
+        atomicMax(&err[2], C0);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_bad) atomicOr(err, 2);
+}
+
+}  // namespace
+
+NX_EXPORT int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax)
+{
+    if (k < 1 || tile_side < 2 || rings < 1 || rings > 8 || !ntiles || !nmax || !cmax)
+        return nx::fail(NX_EINVAL, "nx_tiling_shape: bad arguments");
+    const int M = k / tile_side;
+    const int64_t nt = (int64_t)20 * (M + 1) * (M + 2) / 2;
+    // ring r of a tile of side B has about 4B + 8r vertices; twice that for slack
+    const int64_t B = tile_side;
+    int64_t halo = 0;
+    for (int r = 1; r <= rings; ++r) halo += 2 * (4 * B + 8 * r) + 64;
+    int64_t nm = B * B + 2 * B + halo, cm = B * B + 2 * B + halo;
+    if (nm > 4096) return nx::fail(NX_EINVAL, "nx_tiling_shape: tile too large (%lld local vertices)", (long long)nm);
+    if (nt > 0x7FFFFFFF) return nx::fail(NX_EINVAL, "nx_tiling_shape: too many tiles");
+    *ntiles = (int32_t)nt;
+    *nmax = (int32_t)nm;
+    *cmax = (int32_t)cm;
+    return NX_OK;
+}
+
+NX_EXPORT int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nbr_dev, const float *edge_dev,
+                              int32_t *counts_dev, int32_t *ids_dev, uint16_t *lnbr_dev, float *ledge_dev, int *err_dev,
+                              void *stream)
+{
+    int32_t nt = 0, nmax = 0, cmax = 0;
+    int rc = nx_tiling_shape(k, tile_side, rings, &nt, &nmax, &cmax);
+    if (rc) return rc;
+    if (!nbr_dev || !edge_dev || !counts_dev || !ids_dev || !lnbr_dev || !ledge_dev || !err_dev)
+        return nx::fail(NX_EINVAL, "nx_tiling_build: null pointer");
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !g_tables_ready[dev]) return nx::fail(NX_EINVAL, "nx_tiling_build: call nx_icosphere_tables first");
+    const int64_t nv = (int64_t)10 * k * k + 2;
+    cudaStream_t s = (cudaStream_t)stream;
+    NX_CHECK_CUDA(cudaMemsetAsync(counts_dev, 0, sizeof(int32_t) * (size_t)nt * (rings + 1), s));
+    tile_assign_kernel<<<grid1d(nv), 256, 0, s>>>(k, tile_side, nv, rings, nmax, counts_dev, ids_dev, err_dev);
+    NX_CHECK_LAUNCH("tile_assign_kernel");
+    int P2 = 1;
+    while (P2 < nmax) P2 <<= 1;
+    const size_t smem = sizeof(int32_t) * (2 * (size_t)HASH_CAP + (size_t)(P2 > nmax ? P2 : nmax));
+    NX_CHECK_CUDA(cudaFuncSetAttribute(tile_rings_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    tile_rings_kernel<<<nt, 512, smem, s>>>(nbr_dev, edge_dev, nv, rings, nmax, cmax, counts_dev, ids_dev, lnbr_dev,
+                                            ledge_dev, err_dev);
+    NX_CHECK_LAUNCH("tile_rings_kernel");
+    nx::note_launch(2);
     return NX_OK;
 }

@@ -18,6 +18,11 @@ from ._lib import call, lib
 _tables_done = set()
 _lock = threading.Lock()
 
+# temporally blocked erosion: tiles are TILE_SIDE x TILE_SIDE squares of a
+# face grid with TILE_RINGS halo rings (passes of up to TILE_RINGS iterations)
+TILE_SIDE = 40
+TILE_RINGS = 4
+
 
 def _ensure_tables():
     dev = torch.cuda.current_device()
@@ -121,10 +126,48 @@ class PlanetMesh:
         self.edge, err = edge_lengths(xyz, nbr, stream=stream)
         if int(err.item()):
             raise RuntimeError("mesh adjacency produced an invalid neighbour id")
+        self._tilings = {}
+
+    def tiling(self, tile_side=TILE_SIDE, rings=TILE_RINGS, stream=None):
+        """The mesh's tiling for temporally blocked erosion (built once)."""
+        key = (tile_side, rings)
+        if key not in self._tilings:
+            self._tilings[key] = MeshTiling(self, tile_side, rings, stream)
+        return self._tilings[key]
 
     @property
     def nbytes(self):
-        return self.xyz.numel() * 8 + self.nbr.numel() * 4 + self.edge.numel() * 4
+        return (self.xyz.numel() * 8 + self.nbr.numel() * 4 + self.edge.numel() * 4 +
+                sum(t.nbytes for t in self._tilings.values()))
+
+
+class MeshTiling:
+    """Tiles of a mesh with their halo rings (nx_tiling), resident in HBM."""
+
+    def __init__(self, mesh, tile_side=TILE_SIDE, rings=TILE_RINGS, stream=None):
+        nt, nm, cm = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        call("nx_tiling_shape", mesh.k, tile_side, rings, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm))
+        self.ntiles, self.nmax, self.cmax, self.rings = nt.value, nm.value, cm.value, rings
+        dev = "cuda"
+        self.counts = torch.zeros(self.ntiles * (rings + 1), dtype=torch.int32, device=dev)
+        self.ids = torch.empty(self.ntiles * self.nmax, dtype=torch.int32, device=dev)
+        self.lnbr = torch.empty(self.ntiles * self.cmax * 6, dtype=torch.int16, device=dev)
+        self.ledge = torch.empty(self.ntiles * self.cmax * 6, dtype=torch.float32, device=dev)
+        err = torch.zeros(3, dtype=torch.int32, device=dev)
+        call("nx_tiling_build", mesh.k, tile_side, rings, _dev.ptr(mesh.nbr), _dev.ptr(mesh.edge), _dev.ptr(self.counts),
+             _dev.ptr(self.ids), _dev.ptr(self.lnbr), _dev.ptr(self.ledge), _dev.ptr(err), _dev.stream_handle(stream))
+        e = err.cpu().numpy()
+        if e[0]:
+            raise RuntimeError(f"tiling of divisions {mesh.k} failed (flags {int(e[0])})")
+        self.maxnl, self.maxc = int(e[1]), int(e[2])
+        from ._lib import Tiling
+        t = Tiling(self.ntiles, rings, self.nmax, self.cmax, self.counts.data_ptr(), self.ids.data_ptr(),
+                   self.lnbr.data_ptr(), self.ledge.data_ptr())
+        self.dev = torch.from_numpy(np.frombuffer(bytes(t), np.uint8).copy()).cuda()
+
+    @property
+    def nbytes(self):
+        return self.counts.numel() * 4 + self.ids.numel() * 4 + self.lnbr.numel() * 2 + self.ledge.numel() * 4
 
 
 class MeshCache:

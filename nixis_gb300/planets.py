@@ -95,7 +95,7 @@ def _struct_tensor(arr):
 class PlanetBatch:
     """A fixed set of planets, packed for batched execution."""
 
-    def __init__(self, requests, meshes=None, stream=None):
+    def __init__(self, requests, meshes=None, stream=None, blocked=True):
         _dev.require_cuda()
         if not requests:
             raise ValueError("empty batch")
@@ -166,10 +166,20 @@ class PlanetBatch:
             e.rain = r.rain
             e.t_start = 0
             e.slot = j
+            if blocked and r.erosion_iters > 0:
+                tl = m.tiling(stream=stream)
+                e.tiling = tl.dev.data_ptr()
+                e.ntiles = tl.ntiles
+                e.maxnl = tl.maxnl
         self.fb_host, self.er_host = fb, er
         self.fb_dev = _struct_tensor(fb)
         self.er_dev = _struct_tensor(er)
-        self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(N, np_)), dtype=torch.uint8, device=dev)
+        rows = N
+        if blocked:
+            # the block map of a blocked run has one entry per tile
+            nt = sum(self.meshes.get(r.divisions).tiling().ntiles for r in requests if r.erosion_iters > 0)
+            rows = max(rows, nt * ALIGN)
+        self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(rows, np_)), dtype=torch.uint8, device=dev)
         self.max_iters = max(r.erosion_iters for r in requests)
         # insolation groups by schedule
         self.inso_groups = []
@@ -229,8 +239,17 @@ class PlanetBatch:
         else:
             self.launch()
 
+    def erosion_launches(self):
+        """Erosion launches per run: passes of the blocked path, or iterations."""
+        if any(self.er_host[j].tiling for j in range(len(self.requests))):
+            R = _mesh.TILE_RINGS
+            return max(_tb_npass(r.erosion_iters, R) for r in self.requests)
+        return self.max_iters
+
     def kernels_per_run(self):
-        return 4 + self.max_iters + (1 if self.max_iters > 0 else 0) + len(self.inso_groups)
+        blocked = any(self.er_host[j].tiling for j in range(len(self.requests)))
+        extra = (2 if self.max_iters > 0 else 0)       # block map + rebase
+        return 3 + self.erosion_launches() + extra + len(self.inso_groups)
 
     def results(self):
         """PlanetResult per request, in request order (views into the batch)."""
@@ -248,6 +267,16 @@ class PlanetBatch:
                 ins = self.inso[b:b + n] * sc
             out.append(PlanetResult(r, self.heights[b:b + n], ins, int(K[pos[i]])))
         return out
+
+
+def _tb_npass(iters, R):
+    """Passes of a temporally blocked run: ceil(iters/R), made = iters mod 2."""
+    if iters <= 0:
+        return 0
+    n = (iters + R - 1) // R
+    if (n ^ iters) & 1:
+        n += 1
+    return n
 
 
 def generate_batched(requests, meshes=None):

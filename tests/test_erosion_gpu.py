@@ -236,3 +236,76 @@ def test_bad_neighbour_id_is_reported_not_faulted():
     bad[20, 3] = len(pts) + 5
     with pytest.raises(IndexError):
         erosion.erosion_iteration3(pts, bad, g["ero_k6_smooth_h0"].copy(), np.full(len(pts), 1e-3), np.zeros(len(pts)))
+
+
+def test_tiling_covers_every_vertex_once_with_valid_rings():
+    from nixis_gb300 import mesh
+    for k in (3, 17, 100):
+        m = mesh.PlanetMesh(k)
+        t = m.tiling()
+        R = t.rings
+        cnt = t.counts.view(t.ntiles, R + 1).cpu().numpy()
+        ids = t.ids.view(t.ntiles, t.nmax).cpu().numpy()
+        members = np.concatenate([ids[i, :cnt[i, 0]] for i in range(t.ntiles)])
+        assert np.array_equal(np.sort(members), np.arange(m.n))
+        nbr = m.nbr.cpu().numpy()
+        for i in range(0, t.ntiles, max(1, t.ntiles // 7)):
+            T = cnt[i, 0]
+            loc = ids[i, :cnt[i].sum()]
+            assert len(set(loc.tolist())) == len(loc)
+            # ring r = vertices at graph distance r from the members
+            seen = set(loc[:T].tolist())
+            front = set(seen)
+            off = T
+            for r in range(1, R + 1):
+                nxt = {int(j) for v in front for j in nbr[v] if j >= 0} - seen
+                assert nxt == set(loc[off:off + cnt[i, r]].tolist()), (k, i, r)
+                seen |= nxt
+                front = nxt
+                off += cnt[i, r]
+
+
+@pytest.mark.parametrize("rain", [0.0, 0.3 / 320])
+def test_temporally_blocked_batch_equals_iteration_at_a_time(rain):
+    from nixis_gb300 import mesh, planets, _lib
+    from nixis_gb300.planets import PlanetRequest
+    reqs = [PlanetRequest(seed=s, divisions=k, octaves=6, erosion_iters=it, rain=rain)
+            for s, (k, it) in enumerate([(3, 9), (40, 33), (57, 1), (100, 20), (23, 7), (90, 2), (64, 0), (12, 4)])]
+    cache = mesh.MeshCache()
+    a = planets.PlanetBatch(reqs, cache, blocked=True)
+    a.run()
+    b = planets.PlanetBatch(reqs, cache, blocked=False)
+    b.run()
+    torch.cuda.synchronize()
+    for r, x, y in zip(reqs, a.results(), b.results()):
+        assert torch.equal(x.heights, y.heights), r
+    # and the plain single-planet path
+    for r, x in zip(reqs, a.results()):
+        assert torch.equal(x.heights, planets.generate_plain(r, cache).heights), r
+
+
+def test_temporally_blocked_long_run_rescales_like_iteration_at_a_time():
+    """170 and 150 iterations: both paths rescale (at different iterations:
+    per pass vs per iteration) and hold the same true values."""
+    from nixis_gb300 import mesh, planets
+    from nixis_gb300.planets import PlanetRequest
+    reqs = [PlanetRequest(seed=1, divisions=30, octaves=5, erosion_iters=170),
+            PlanetRequest(seed=2, divisions=7, octaves=5, erosion_iters=150)]
+    cache = mesh.MeshCache()
+    out = []
+    for blocked in (True, False):
+        bt = planets.PlanetBatch(reqs, cache, blocked=blocked)
+        bt.run()
+        torch.cuda.synchronize()
+        st = bt.st.double()
+        vals = []
+        for i, res in enumerate(bt.results()):
+            assert res.scale_exponent > 0
+            b, n = bt.vbeg[i], reqs[i].n_vertices
+            x = st[b:b + n]
+            true = torch.stack([x[:, 0] + x[:, 1], x[:, 2], x[:, 3]]) * 2.0 ** res.scale_exponent
+            assert torch.isfinite(true).all()
+            vals.append(true)
+        out.append(vals)
+    for x, y in zip(*out):
+        assert torch.equal(x, y)
