@@ -79,22 +79,18 @@ __device__ __forceinline__ void df_add(float &hi, float &lo, float b)
 }
 
 // One neighbour's contribution (erosion.py:223-247): the flow choice is the
-// sign of h_j - h_i from the height pairs; returns 1 (higher), 2 (lower), 0.
+// sign of h_j - h_i from the height pairs.  Branch free: with g = +1, -1 or
+// 0, fma(g, t, x) is exactly x + t, x - t or x (t*g is exact).  Returns the
+// flow code: 1 higher, 2 lower, 0 equal.
 __device__ __forceinline__ unsigned erode_accum(float hh, float hl, float hjh, float hjl, float wj, float d, float &sed,
                                                 float &wat)
 {
     const float diff = __fadd_rn(__fsub_rn(hjh, hh), __fsub_rn(hjl, hl));
-    if (diff > 0.0f) {
-        sed = __fadd_rn(sed, __fmul_rn(c_sol, wj));
-        wat = __fadd_rn(wat, __fmul_rn(wj, d));
-        return 1u;
-    }
-    if (diff < 0.0f) {
-        sed = __fsub_rn(sed, __fmul_rn(c_sol, wj));
-        wat = __fsub_rn(wat, __fmul_rn(wj, d));
-        return 2u;
-    }
-    return 0u;
+    const bool up = diff > 0.0f, dn = diff < 0.0f;
+    const float g = up ? 1.0f : (dn ? -1.0f : 0.0f);
+    sed = __fmaf_rn(g, __fmul_rn(c_sol, wj), sed);
+    wat = __fmaf_rn(g, __fmul_rn(wj, d), wat);
+    return up ? 1u : (dn ? 2u : 0u);
 }
 
 // erosion.py:262-267: new height pair, sediment and water.
@@ -312,9 +308,9 @@ struct TbArgs {
 
 constexpr int TB_THREADS = 512;
 
-__global__ void __launch_bounds__(TB_THREADS, 2) erosion_tb_kernel(TbArgs a)
+__global__ void __launch_bounds__(TB_THREADS, 3) erosion_tb_kernel(TbArgs a)
 {
-    extern __shared__ float tsm[];
+    extern __shared__ float4 tsm4[];
     const int2 bm = a.blk_map[blockIdx.x];
     const nx_erosion_planet P = a.planets[bm.x];
     const int R = a.R;
@@ -345,55 +341,46 @@ __global__ void __launch_bounds__(TB_THREADS, 2) erosion_tb_kernel(TbArgs a)
     const bool par = ((np - q) & 1) != 0;
     const float4 *__restrict__ ist = par ? a.st1 : a.st0;
     float4 *__restrict__ ost = par ? a.st0 : a.st1;
-    const int S = a.smem_n;
-    float *b0h = tsm, *b0l = tsm + S, *b0w = tsm + 2 * S, *b0s = tsm + 3 * S;
-    float *b1h = tsm + 4 * S, *b1l = tsm + 5 * S, *b1w = tsm + 6 * S, *b1s = tsm + 7 * S;
+    float4 *buf0 = tsm4, *buf1 = tsm4 + a.smem_n;     // rows (h_hi, h_lo, w, s)
     const int32_t *ids = TL.ids + (int64_t)tile * TL.nmax;
     for (int l = threadIdx.x; l < NL; l += blockDim.x) {
         const float4 x = ist[P.vbeg + ids[l]];
-        b0h[l] = __fmul_rn(x.x, lam);
-        b0l[l] = __fmul_rn(x.y, lam);
-        b0w[l] = __fmul_rn(x.z, lam);
-        b0s[l] = __fmul_rn(x.w, lam);
+        buf0[l] = make_float4(__fmul_rn(x.x, lam), __fmul_rn(x.y, lam), __fmul_rn(x.z, lam), __fmul_rn(x.w, lam));
     }
     __syncthreads();
     const uint32_t *lnb = reinterpret_cast<const uint32_t *>(TL.lnbr) + (int64_t)tile * TL.cmax * 3;
     const float2 *led = reinterpret_cast<const float2 *>(TL.ledge) + (int64_t)tile * TL.cmax * 3;
     int C = NL - cnt[len];                      // members + rings 1..len-1
     for (int mi = 0; mi < len; ++mi) {
-        const bool odd = mi & 1;
-        const float *ch = odd ? b1h : b0h, *cl = odd ? b1l : b0l, *cw = odd ? b1w : b0w, *cs = odd ? b1s : b0s;
-        float *nh_ = odd ? b0h : b1h, *nl_ = odd ? b0l : b1l, *nw_ = odd ? b0w : b1w, *ns_ = odd ? b0s : b1s;
+        const float4 *cur = (mi & 1) ? buf1 : buf0;
+        float4 *nxt = (mi & 1) ? buf0 : buf1;
         for (int l = threadIdx.x; l < C; l += blockDim.x) {
-            const uint32_t p01 = lnb[3 * l], p23 = lnb[3 * l + 1], p45 = lnb[3 * l + 2];
-            const float2 d01 = led[3 * l], d23 = led[3 * l + 1], d45 = led[3 * l + 2];
+            const uint32_t p01 = __ldg(lnb + 3 * l), p23 = __ldg(lnb + 3 * l + 1), p45 = __ldg(lnb + 3 * l + 2);
+            const float2 d01 = __ldg(led + 3 * l), d23 = __ldg(led + 3 * l + 1), d45 = __ldg(led + 3 * l + 2);
+            const float4 me = cur[l];
+            const float wi = __fadd_rn(me.z, rain);
+            float sed = me.w, wat = wi;
             const uint32_t nb[6] = {p01 & 0xFFFFu, p01 >> 16, p23 & 0xFFFFu, p23 >> 16, p45 & 0xFFFFu, p45 >> 16};
             const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
-            const float hh = ch[l], hl = cl[l];
-            const float wi = __fadd_rn(cw[l], rain);
-            const float si = cs[l];
-            float sed = si, wat = wi;
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
-                const uint32_t j = nb[k];
-                if (j == 0xFFFFu) continue;
-                erode_accum(hh, hl, ch[j], cl[j], __fadd_rn(cw[j], rain), dd[k], sed, wat);
+                // a missing neighbour (pentagon slot) is stored as the vertex
+                // itself: equal heights contribute nothing, as the reference's
+                // skip of -1
+                const float4 o = cur[nb[k]];
+                erode_accum(me.x, me.y, o.x, o.y, __fadd_rn(o.z, rain), dd[k], sed, wat);
             }
             float nh, nl, wn, sn;
-            erode_finish(hh, hl, wi, si, sed, wat, nh, nl, wn, sn);
-            nh_[l] = nh;
-            nl_[l] = nl;
-            nw_[l] = wn;
-            ns_[l] = sn;
+            erode_finish(me.x, me.y, wi, me.w, sed, wat, nh, nl, wn, sn);
+            nxt[l] = make_float4(nh, nl, wn, sn);
         }
         __syncthreads();
         if (mi + 1 < len) C -= cnt[len - 1 - mi];
     }
-    const bool fin = len & 1;
-    const float *fh = fin ? b1h : b0h, *fl = fin ? b1l : b0l, *fw = fin ? b1w : b0w, *fs = fin ? b1s : b0s;
+    const float4 *fin = (len & 1) ? buf1 : buf0;
     float vmax = 0.0f;
     for (int l = threadIdx.x; l < T; l += blockDim.x) {
-        const float4 v = make_float4(fh[l], fl[l], fw[l], fs[l]);
+        const float4 v = fin[l];
         ost[P.vbeg + ids[l]] = v;
         vmax = fmaxf(vmax, fmaxf(fabsf(v.x), fmaxf(fabsf(v.z), fabsf(v.w))));
     }
@@ -722,7 +709,7 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     if (maxnl == 0) tb = false;
     if (tb) {
         R = g_tb_rings;
-        const size_t smem = 8 * sizeof(float) * (size_t)maxnl;
+        const size_t smem = 2 * sizeof(float4) * (size_t)maxnl;
         if (smem > 200 * 1024) tb = false;
     }
     if (tb) {
@@ -752,7 +739,7 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         ta.st0 = (float4 *)st_dev;
         ta.st1 = (float4 *)st_tmp;
         ta.ctl = w.ctl;
-        const size_t smem = 8 * sizeof(float) * (size_t)maxnl;
+        const size_t smem = 2 * sizeof(float4) * (size_t)maxnl;
         for (int q = 0; q < maxpass; ++q) {
             int64_t grid = 0;
             for (int p = 0; p < np; ++p)

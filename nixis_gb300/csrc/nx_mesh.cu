@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
     extern __shared__ int32_t sh[];
     int32_t *key = sh;                      // HASH_CAP
     int32_t *val = key + HASH_CAP;          // HASH_CAP
-    int32_t *list = val + HASH_CAP;         // nmax (padded to a power of two for the sort)
+    int32_t *list = val + HASH_CAP;         // local vertices; list + nmax: sort scratch
     __shared__ int s_cnt, s_bad;
     __shared__ int s_ring[16];
     const int64_t tile = blockIdx.x;
@@ -547,6 +547,44 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
         __syncthreads();
     }
     const int NL = end;
+    // each ring in ascending id order too (neighbouring vertices get nearby
+    // local indices: fewer shared-memory bank conflicts in the erosion pass),
+    // then the hash values follow the new positions
+    {
+        int32_t *scr = list + nmax;        // scratch of nmax entries
+        int rb = T;
+        for (int r = 1; r <= R; ++r) {
+            const int re = rb + s_ring[r];
+            const int ln = re - rb;
+            int p2 = 1;
+            while (p2 < ln) p2 <<= 1;
+            for (int q = threadIdx.x; q < p2; q += blockDim.x) scr[q] = q < ln ? list[rb + q] : 0x7FFFFFFF;
+            __syncthreads();
+            for (int size = 2; size <= p2; size <<= 1)
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int q = threadIdx.x; q < p2; q += blockDim.x) {
+                        const int o = q ^ stride;
+                        if (o > q) {
+                            const bool upw = (q & size) == 0;
+                            const int32_t x = scr[q], y = scr[o];
+                            if ((x > y) == upw) { scr[q] = y; scr[o] = x; }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (int q = threadIdx.x; q < ln; q += blockDim.x) {
+                const int32_t v = scr[q];
+                list[rb + q] = v;
+                uint32_t h = hslot(v);
+                for (int probe = 0; probe < HASH_CAP; ++probe) {
+                    if (key[h] == v) { val[h] = rb + q; break; }
+                    h = (h + 1) & (HASH_CAP - 1);
+                }
+            }
+            __syncthreads();
+            rb = re;
+        }
+    }
     int C0 = T;
     for (int r = 1; r < R; ++r) C0 += s_ring[r];
     if (C0 > cmax) { if (threadIdx.x == 0) s_bad = 1; C0 = cmax; }
@@ -556,12 +594,14 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
         const int q = w / 6, sl = w % 6;
         const int32_t v = list[q];
         const int32_t j = nbr[6 * (int64_t)v + sl];
-        int loc = -1;
+        // a missing neighbour (-1, pentagon slot) points at the vertex itself:
+        // the erosion update then sees equal heights and adds nothing
+        int loc = q;
         if (j >= 0) {
             loc = hfind(key, val, j);
-            if (loc < 0) s_bad = 1;
+            if (loc < 0) { s_bad = 1; loc = q; }
         }
-        lnbr[((int64_t)tile * cmax + q) * 6 + sl] = loc < 0 ? (uint16_t)0xFFFF : (uint16_t)loc;
+        lnbr[((int64_t)tile * cmax + q) * 6 + sl] = (uint16_t)loc;
         ledge[((int64_t)tile * cmax + q) * 6 + sl] = edge[6 * (int64_t)v + sl];
     }
     if (threadIdx.x == 0) {
@@ -614,7 +654,8 @@ NX_EXPORT int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nb
     NX_CHECK_LAUNCH("tile_assign_kernel");
     int P2 = 1;
     while (P2 < nmax) P2 <<= 1;
-    const size_t smem = sizeof(int32_t) * (2 * (size_t)HASH_CAP + (size_t)(P2 > nmax ? P2 : nmax));
+    // hash keys + values, the local list (padded for sorting) and a scratch
+    const size_t smem = sizeof(int32_t) * (2 * (size_t)HASH_CAP + 2 * (size_t)P2);
     NX_CHECK_CUDA(cudaFuncSetAttribute(tile_rings_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     tile_rings_kernel<<<nt, 512, smem, s>>>(nbr_dev, edge_dev, nv, rings, nmax, cmax, counts_dev, ids_dev, lnbr_dev,
                                             ledge_dev, err_dev);
