@@ -320,9 +320,38 @@ __device__ __forceinline__ float contrib(uint32_t w, float dx, float dy, float d
     return (a2 * a2) * dot;
 }
 
-struct SlotTrace {
-    int32_t *p;   // 9 slots x [x, y, z, packed gradient, used]
-};
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__device__ __forceinline__ float gcomp(uint32_t w, uint32_t sel)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel));
+}
+
+// Two lattice contributions at once in paired binary32 arithmetic (one
+// FFMA2/FMUL2/FADD2 does both): acc += attn^4 * (grad . d) for slots a and
+// b; ON (1 or 0) masks slots outside the region.  -attn = |d|^2 - 2 is
+// clamped at 0 before squaring, so only attn > 0 counts.
+__device__ __forceinline__ float2 contrib2(uint32_t wa, uint32_t wb, float2 DX, float2 DY, float2 DZ, float2 ON,
+                                           float2 acc)
+{
+    float2 sq = __fmul2_rn(DZ, DZ);
+    sq = __ffma2_rn(DY, DY, sq);
+    sq = __ffma2_rn(DX, DX, sq);
+    float2 na = __fadd2_rn(sq, f2(-2.0f, -2.0f));
+    na = f2(fminf(na.x, 0.0f), fminf(na.y, 0.0f));
+    na = __fmul2_rn(na, ON);
+    const float2 a2 = __fmul2_rn(na, na);
+    const float2 a4 = __fmul2_rn(a2, a2);
+    const float2 nb = f2(-GBIAS, -GBIAS);
+    const float2 gx = __fadd2_rn(f2(gcomp(wa, 0x7442), gcomp(wb, 0x7442)), nb);
+    const float2 gy = __fadd2_rn(f2(gcomp(wa, 0x7443), gcomp(wb, 0x7443)), nb);
+    const float2 gz = __fadd2_rn(f2(__uint_as_float((wa & 0x7Fu) | 0x4B000000u),
+                                    __uint_as_float((wb & 0x7Fu) | 0x4B000000u)), nb);
+    float2 dot = __fmul2_rn(gz, DZ);
+    dot = __ffma2_rn(gy, DY, dot);
+    dot = __ffma2_rn(gx, DX, dot);
+    return __ffma2_rn(a4, dot, acc);
+}
 
 // noise3d(x*s) * 103 for one vertex and octave.
 template <bool TRACE>
@@ -345,19 +374,12 @@ __device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float y
     const float dx0 = c.dx0, dy0 = c.dy0, dz0 = c.dz0;
     // slot 0: (0,0,0) in region 0, (1,1,1) in region 1
     uint32_t w0 = lk(lb, r == 1 ? (int)h11 + z1 : (int)h00 + z0);
-    float k0 = r == 1 ? 1.0f + 1.0f : 0.0f;   // o + sum(o)/3 with o = (1,1,1): 1 + 1
-    float v = contrib(w0, dx0 - k0, dy0 - k0, dz0 - k0, on0);
-    // mixed corners
+    const float k0 = r == 1 ? 1.0f + 1.0f : 0.0f;   // o + sum(o)/3 with o = (1,1,1): 1 + 1
+    // mixed corners; displacement d = d0 - o - sum(o)/3
     const float c1 = 1.0f + THIRD, c2 = 2.0f * THIRD, c3 = 1.0f + 2.0f * THIRD;
     uint32_t w100 = lk(lb, (int)h10 + z0), w010 = lk(lb, (int)h01 + z0), w001 = lk(lb, (int)h00 + z1);
     uint32_t w110 = lk(lb, (int)h11 + z0), w101 = lk(lb, (int)h10 + z1), w011 = lk(lb, (int)h01 + z1);
-    v += contrib(w100, dx0 - c1, dy0 - THIRD, dz0 - THIRD, onA);
-    v += contrib(w010, dx0 - THIRD, dy0 - c1, dz0 - THIRD, onA);
-    v += contrib(w001, dx0 - THIRD, dy0 - THIRD, dz0 - c1, onA);
-    v += contrib(w110, dx0 - c3, dy0 - c3, dz0 - c2, onB);
-    v += contrib(w101, dx0 - c3, dy0 - c2, dz0 - c3, onB);
-    v += contrib(w011, dx0 - c2, dy0 - c3, dz0 - c3, onB);
-    // extra points: d = d0 - o - sum(o)/3
+    // extra points
     const Decision &D = c.D;
     float s0 = ((D.e0x + D.e0y) + D.e0z) * THIRD, s1 = ((D.e1x + D.e1y) + D.e1z) * THIRD;
     int ox0 = __float_as_int(D.e0x + MAGIC) << 7, oy0 = __float_as_int(D.e0y + MAGIC) << 7,
@@ -366,8 +388,18 @@ __device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float y
         oz1 = __float_as_int(D.e1z + MAGIC) << 7;
     uint32_t we0 = lk(lb, (int)lk(lb, (int)lk(lb, c.xb7 + ox0) + c.yb7 + oy0) + c.zb7 + oz0);
     uint32_t we1 = lk(lb, (int)lk(lb, (int)lk(lb, c.xb7 + ox1) + c.yb7 + oy1) + c.zb7 + oz1);
-    v += contrib(we0, dx0 - (D.e0x + s0), dy0 - (D.e0y + s0), dz0 - (D.e0z + s0), true);
-    v += contrib(we1, dx0 - (D.e1x + s1), dy0 - (D.e1y + s1), dz0 - (D.e1z + s1), true);
+    const float2 X0 = f2(dx0, dx0), Y0 = f2(dy0, dy0), Z0 = f2(dz0, dz0);
+    const float fon0 = on0 ? 1.0f : 0.0f, fA = onA ? 1.0f : 0.0f, fB = onB ? 1.0f : 0.0f;
+    float2 acc = f2(0.0f, 0.0f);
+    acc = contrib2(w0, w100, __fadd2_rn(X0, f2(-k0, -c1)), __fadd2_rn(Y0, f2(-k0, -THIRD)),
+                   __fadd2_rn(Z0, f2(-k0, -THIRD)), f2(fon0, fA), acc);
+    acc = contrib2(w010, w001, __fadd2_rn(X0, f2(-THIRD, -THIRD)), __fadd2_rn(Y0, f2(-c1, -THIRD)),
+                   __fadd2_rn(Z0, f2(-THIRD, -c1)), f2(fA, fA), acc);
+    acc = contrib2(w110, w101, __fadd2_rn(X0, f2(-c3, -c3)), __fadd2_rn(Y0, f2(-c3, -c2)),
+                   __fadd2_rn(Z0, f2(-c2, -c3)), f2(fB, fB), acc);
+    acc = contrib2(w011, we0, __fadd2_rn(X0, f2(-c2, -(D.e0x + s0))), __fadd2_rn(Y0, f2(-c3, -(D.e0y + s0))),
+                   __fadd2_rn(Z0, f2(-c3, -(D.e0z + s0))), f2(fB, 1.0f), acc);
+    float v = (acc.x + acc.y) + contrib(we1, dx0 - (D.e1x + s1), dy0 - (D.e1y + s1), dz0 - (D.e1z + s1), true);
     if (TRACE) {
         tr[0] = c.xsb; tr[1] = c.ysb; tr[2] = c.zsb; tr[3] = r;
         tr[4] = c.xsb + (int)D.e0x; tr[5] = c.ysb + (int)D.e0y; tr[6] = c.zsb + (int)D.e0z;
