@@ -30,7 +30,8 @@ sys.path.insert(0, ROOT)
 N_PLANETS = 64
 METRIC = "batched planets/s (64 planets, divisions 100-800, 4-12 octaves, 0-100 erosion iterations)"
 UNIT = "planets/s"
-SAMPLE_ALG_BYTES = 72      # erosion: algorithmic bytes per vertex-iteration (state 12+12, neighbours 24, edges 24)
+SAMPLE_ALG_BYTES = 96      # erosion: algorithmic bytes per vertex-iteration (state in 24 + out 24: h, w, s as
+                           # binary32 pairs; neighbour ids 24, edge lengths 24)
 
 
 def workload(name="batch64"):
@@ -286,6 +287,22 @@ def bench_ours(args):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     reqs = workload(args.workload)
     npl = len(reqs)
+    # blocked-erosion setting: autotuned on this device (before anything is timed)
+    from nixis_gb300 import autotune
+    tune_t0 = time.perf_counter()
+    if args.tb or args.profile:
+        # profiler runs launch nothing but the batch: a given or the default setting
+        tb = autotune.TbConfig(*(int(x) for x in args.tb.split("/"))) if args.tb else autotune.DEFAULT
+        autotune.use(tb)
+        tune_info = {"setting": f"{tb.tile_side}/{tb.rings}/{tb.threads}", "source": "given" if args.tb else "default"}
+    else:
+        tb, timings = autotune.tune(save=False)
+        tune_info = {"setting": f"{tb.tile_side}/{tb.rings}/{tb.threads}", "source": "autotuned",
+                     "candidates_ms": timings, "seconds": round(time.perf_counter() - tune_t0, 2)}
+    if args.tune_only:
+        if rank == 0:
+            print(json.dumps({"autotune": tune_info}))
+        return
     cache = mesh.MeshCache()
     for r in reqs:
         cache.get(r.divisions)
@@ -343,7 +360,7 @@ def bench_ours(args):
     ev[1].record(stream)
     call("nx_erosion_init_batch", _dev.ptr(batch.er_dev), ctypes.cast(batch.er_host, ctypes.c_void_p), np_,
          _dev.ptr(batch.raw), _dev.ptr(batch.minmax), ctypes.c_float(-8000.0), ctypes.c_float(8000.0),
-         ctypes.c_float(1e-3), _dev.ptr(batch.st), _dev.ptr(batch.st_tmp), s)
+         ctypes.c_double(1e-3), _dev.ptr(batch.st), _dev.ptr(batch.st_tmp), s)
     call("nx_erosion_ctl_init", _dev.ptr(batch.ws), batch.ws.numel(), np_, s)
     ev[2].record(stream)
     call("nx_erosion_batch", _dev.ptr(batch.er_dev), ctypes.cast(batch.er_host, ctypes.c_void_p), np_,
@@ -406,6 +423,13 @@ def bench_ours(args):
            "h2d_bytes_per_step": int(batch.tables.numel() * 4), "d2h_bytes_per_step": int(batch.heights.numel() * 4),
            "note": "request tables in, all heights out to pinned host memory, per step"}
 
+    launches = batch.kernels_per_run() * args.steps
+    serving = None
+    if rank == 0 and world == 1 and args.serve_requests > 0:
+        del batch
+        torch.cuda.empty_cache()
+        serving = run_serving(args.serve_requests)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = run_cpu_baseline(reqs, budget_s=args.cpu_budget)
@@ -415,11 +439,192 @@ def bench_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(reqs),
                 "plain_per_planet": plain, "ratio_vs_plain": value / (plain["value"] * world),
-                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "gpu_launches": batch.kernels_per_run() * args.steps}
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "blocked_erosion": tune_info,
+                "serving": serving,
+                "gpu_launches": launches}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# serving: continuous batching against the plain per-planet path
+
+def run_serving(n_requests, hbm_budget=120 * 2**30):
+    """The first n requests of the serving stream (Poisson arrivals at 20
+    req/s, seed 11, divisions log-uniform in [50, 2000], octaves U[4,12],
+    erosion iterations U[0,100], insolation for half), served (a) as they
+    arrive and (b) all at once, by the engine and by the plain per-planet
+    path; every engine result is checked bit for bit against the plain
+    path's.  Meshes are built on demand by both (resident, LRU under the
+    budget)."""
+    import torch
+    from nixis_gb300 import serve
+    stream = serve.poisson_stream(2000)[:n_requests]
+    out = {"requests": len(stream), "arrival_rate_per_s": 20.0, "hbm_budget_gb": hbm_budget / 2**30}
+    eng_meshes = None
+    for mode, realtime in (("arrivals", True), ("all_at_once", False)):
+        eng = serve.ServeEngine(hbm_budget=hbm_budget)
+        if eng_meshes is not None:
+            eng.meshes = eng_meshes          # meshes stay resident between the two runs
+            eng.meshes.tb = eng.tb
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tk = eng.run(stream, realtime=realtime, t0=t0)
+        span = time.perf_counter() - t0
+        eng_meshes = eng.meshes
+        pm = serve.ResidentMeshes(hbm_budget // 2)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        plain = serve.serve_plain(stream, meshes=pm, realtime=realtime, t0=t1)
+        span_p = time.perf_counter() - t1
+        same = all(np.array_equal(t.heights, p[2].numpy()) and
+                   (t.insolation is None or np.array_equal(t.insolation, p[3].numpy())) for t, p in zip(tk, plain))
+        lat_e = serve.latency_stats([t.latency for t in tk])
+        lat_p = serve.latency_stats([f - a for a, f, _, _ in plain])
+        out[mode] = {"engine": dict(lat_e, planets_per_s=len(tk) / span, seconds=span),
+                     "plain": dict(lat_p, planets_per_s=len(plain) / span_p, seconds=span_p),
+                     "p99_ratio_plain_over_engine": lat_p["p99_ms"] / lat_e["p99_ms"],
+                     "results_equal_plain": bool(same)}
+        del eng
+    return out
+
+
+def bench_serve(args):
+    from nixis_gb300 import autotune
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    tb, _ = autotune.tune(save=False)
+    res = run_serving(args.serve)
+    res["blocked_erosion"] = f"{tb.tile_side}/{tb.rings}/{tb.threads}"
+    print(json.dumps({"serving": res}))
+
+
+# ---------------------------------------------------------------------------
+# single-planet configurations (supplementary lines)
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _time(fn, reps=3):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        a, b = _events()
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        best = ms if best is None else min(best, ms)
+    return best
+
+
+def bench_single(name):
+    """c1: divisions 250, 8 octaves, seed 0, metres (float64);
+    c2: divisions 1000, 12 octaves, seed 1, then 50 erosion iterations from
+        water 1e-3, sediment 0 (errors per field vs binary64 at 1/10/50);
+    c3: divisions 2500, 12 octaves, seed 2, 200 erosion iterations, and
+        mean annual insolation over 365 days x 24 hours."""
+    import torch
+    from oracle import oracle as O
+    from nixis_gb300 import mesh, terrain, erosion, climate, planets
+    k, octs, seed = {"c1": (250, 8, 0), "c2": (1000, 12, 1), "c3": (2500, 12, 2)}[name]
+    m = mesh.PlanetMesh(k)
+    n = m.n
+    perm, pgi = O.init(seed)
+    sc, st = terrain._octave_args(octs, 1.0, 1.0, 2.0, 0.5, 1.0)
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    fbm_ms = _time(lambda: terrain.fbm(m.xyz, perm, pgi, sc, st, 1.0, out=out))
+    _, nfb = terrain.fbm(m.xyz, perm, pgi, sc, st, 1.0, out=out, count_fallbacks=True)
+    h = out.cpu().numpy()
+    line = {"config": name, "divisions": k, "vertices": n, "octaves": octs, "seed": seed,
+            "fbm_ms": fbm_ms, "vertex_octaves_per_s": n * octs / (fbm_ms / 1e3),
+            "fbm_tflops_at_160": n * octs * 160 / (fbm_ms / 1e3) / 1e12,
+            "binary64_decision_rate": nfb / (n * octs)}
+    pts = m.xyz.cpu().numpy()
+    t0 = time.perf_counter()
+    ref = O.sample_octaves(pts, None, perm, pgi, octs, 1.0, 1.0, 2.0, 0.5, 1.0)
+    line["cpu_fbm_s"] = time.perf_counter() - t0
+    r = ref.max() - ref.min()
+    line["fbm_max_err_over_range"] = float(np.abs(h - ref).max() / r)
+    line["fbm_rms_err_over_range"] = float(np.sqrt(np.mean((h - ref) ** 2)) / r)
+    hm = O.rescale(ref, -8000.0, 8000.0)
+    hg = O.rescale(h, -8000.0, 8000.0)
+    line["elevation_max_err_m"] = float(np.abs(hg - hm).max())
+    if name == "c1":
+        print(json.dumps(line))
+        return
+    iters = 50 if name == "c2" else 200
+    nbr = m.nbr.cpu().numpy()
+    hm_t = torch.from_numpy(hm).cuda()
+    w0 = torch.full((n,), 1e-3, dtype=torch.float64, device="cuda")
+    run = erosion.ErosionRun(m.xyz, m.nbr, m.edge)
+    checkpoints = [1, 10, 50] if name == "c2" else [1, 10, 50, 100, 140, 150, 200]
+    # binary32-pair state vs binary64 reference, per field, at checkpoints
+    errs = {}
+    if name == "c2":
+        run.load(hm_t, w0)
+        hw, ww, sw = hm.copy(), np.full(n, 1e-3), np.zeros(n)
+        done = 0
+        hd = torch.empty(n, dtype=torch.float64, device="cuda")
+        wd, sd = torch.empty_like(hd), torch.empty_like(hd)
+        for cp in checkpoints:
+            run.steps(cp - done)
+            for _ in range(cp - done):
+                O.erosion_iteration3(pts, nbr, hw, ww, sw)
+            done = cp
+            run.store(hd, wd, sd)
+            g = [hd.cpu().numpy(), wd.cpu().numpy(), sd.cpu().numpy()]
+            errs[cp] = {f: {"max_abs_over_max": float(np.abs(a - b).max() / np.abs(b).max()),
+                            "rms_over_max": float(np.sqrt(np.mean((a - b) ** 2)) / np.abs(b).max())}
+                        for f, a, b in zip("hws", g, (hw, ww, sw))}
+            # flow choices (sign of h_n - h_i per slot) that differ from binary64's
+            jj = np.where(nbr < 0, np.arange(n)[:, None], nbr)
+            errs[cp]["flow_choice_flips"] = int((np.sign(g[0][jj] - g[0][:, None]) !=
+                                                 np.sign(hw[jj] - hw[:, None])).sum())
+        line["erosion_errors"] = errs
+    # timing: one planet's erosion, blocked (batch of one) and iteration at a time (CUDA graph)
+    req = planets.PlanetRequest(seed=seed, divisions=k, octaves=octs, erosion_iters=iters)
+    cache = mesh.MeshCache()
+    cache._m[k] = m
+    cache._order.append(k)
+    for blocked in (True, False):
+        bt = planets.PlanetBatch([req], cache, blocked=blocked)
+        bt.capture()
+        ms = _time(lambda: bt.run())
+        ero = ms - fbm_ms
+        line["planet_ms_blocked" if blocked else "planet_ms_iteration_kernel"] = ms
+        line["erosion_gvi_per_s_blocked" if blocked else "erosion_gvi_per_s_iteration_kernel"] = n * iters / (ero / 1e3) / 1e9
+        res = bt.results()[0]
+        line["scale_exponent"] = res.scale_exponent
+        del bt
+    # mass sums (compensated, per iteration) and where plain binary32 would overflow
+    run.load(hm_t, w0)
+    mass, _ = run.steps(iters, mass=True)
+    ms_ = mass.cpu().numpy()
+    line["mass_sum_h_plus_s_first_last"] = [float(ms_[0, 0] + ms_[0, 2]), float(ms_[-1, 0] + ms_[-1, 2])]
+    line["scale_exponent_after"] = run.scale_exponent()
+    over = [i + 1 for i in range(iters) if abs(ms_[i, 1]) / n > 3.4e38]
+    line["first_iteration_mean_water_above_binary32_max"] = over[0] if over else None
+    if name == "c3":
+        xs = m.xyz
+        ins_ms = _time(lambda: climate.annual_insolation(xs, 1.0), reps=2)
+        samples = n * 365 * 24
+        line["insolation_ms"] = ins_ms
+        line["insolation_samples_per_s"] = samples / (ins_ms / 1e3)
+        line["insolation_tflops_at_6"] = samples * 6 / (ins_ms / 1e3) / 1e12
+        rng = np.random.default_rng(0)
+        idx = rng.choice(n, 100000, replace=False)
+        got = climate.annual_insolation(xs, 1.0).cpu().numpy()[idx]
+        ref_i = O.annual_insolation(pts[idx], 1.0)
+        line["insolation_max_err_over_max"] = float(np.abs(got - ref_i).max() / np.abs(ref_i).max())
+        line["mean_toa_wm2_range"] = [float(1361 * got.min() / 8760), float(1361 * got.max() / 8760)]
+    print(json.dumps(line))
 
 
 def main():
@@ -433,7 +638,18 @@ def main():
     ap.add_argument("--workload", choices=["batch64", "small"], default="batch64")
     ap.add_argument("--eager", action="store_true", help="launch without a CUDA graph (for profilers)")
     ap.add_argument("--profile", action="store_true", help="build the batch, run it once eagerly, exit (ncu)")
+    ap.add_argument("--single", choices=["c1", "c2", "c3"], help="a single-planet configuration (supplementary line)")
+    ap.add_argument("--tb", help="blocked-erosion setting side/rings/threads instead of autotuning (e.g. 40/4/512)")
+    ap.add_argument("--tune-only", action="store_true", help="run the autotuner, print its table, exit")
+    ap.add_argument("--serve", type=int, default=0, help="serving comparison on the first N stream requests, exit")
+    ap.add_argument("--serve-requests", type=int, default=200, help="stream requests in the default line's serving leg")
     args = ap.parse_args()
+    if args.single:
+        bench_single(args.single)
+        return
+    if args.serve:
+        bench_serve(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

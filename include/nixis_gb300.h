@@ -156,7 +156,8 @@ int nx_build_adjacency(const int32_t *tris_dev, int64_t nt, int64_t nv, int32_t 
 int nx_sort_adjacency(const int32_t *adj_in_dev, int32_t *adj_out_dev, int64_t nv, void *stream);
 
 /* Per-slot neighbour distance |v_i - v_j| in binary64 (erosion.calc_distance,
- * erosion.py:38-40) rounded to binary32: edge_dev float[nv*6], 0 for -1 slots.
+ * erosion.py:38-40) split into a pair hi + lo of binary32s: edge_dev
+ * float[nv*6*2], (hi, lo) per slot, 0 for -1 slots.
  * err_dev (optional) gets bit 0 for an out-of-range neighbour id. */
 int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, float *edge_dev, int *err_dev,
                     void *stream);
@@ -174,7 +175,7 @@ typedef struct nx_tiling {
     const int32_t *counts;     /* ntiles x (rings + 1): members, then each ring's size */
     const int32_t *ids;        /* ntiles x nmax global vertex ids */
     const uint16_t *lnbr;      /* ntiles x cmax x 6 local neighbour indices, 0xFFFF = none */
-    const float *ledge;        /* ntiles x cmax x 6 edge lengths */
+    const float *ledge;        /* ntiles x cmax x 6 edge lengths, (hi, lo) pairs */
 } nx_tiling;
 
 /* Host: sizes of the tiling of divisions k. */
@@ -183,7 +184,7 @@ int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *n
 /* Build a tiling from the mesh's neighbour table and edge lengths into
  * caller buffers sized by nx_tiling_shape (counts int32[ntiles*(rings+1)],
  * ids int32[ntiles*nmax], lnbr uint16[ntiles*cmax*6], ledge
- * float[ntiles*cmax*6]).  err_dev (device int[3], caller zeroes it):
+ * float[ntiles*cmax*6*2]).  err_dev (device int[3], caller zeroes it):
  * [0] bit 0 = a tile exceeded nmax members, bit 1 = a halo or neighbour
  * problem; [1] largest local vertex count; [2] largest updatable count. */
 int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nbr_dev, const float *edge_dev,
@@ -195,8 +196,8 @@ int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nbr_dev, con
 /* ------------------------------------------------------------------ */
 
 /* One planet of an erosion launch.  Its state occupies rows [vbeg, vbeg+n)
- * of the state buffers; nbr (n,6) local neighbour ids and edge (n,6)
- * per-slot lengths are its mesh (device pointers, shared by planets of
+ * of the state buffers; nbr (n,6) local neighbour ids and edge (n,6,2)
+ * per-slot lengths (pairs, as nx_edge_lengths writes them) are its mesh (device pointers, shared by planets of
  * equal divisions).  `rain` is added to every water value before each
  * iteration (erode_terrain3 adds 0.3/320, erosion.py:182-183; 0 gives bare
  * erosion_iteration3 steps).  Its iteration t runs at global step
@@ -225,12 +226,13 @@ size_t nx_erosion_workspace_size(int64_t n_padded_total, int nplanets);
 /* Zero the per-planet control words (scale exponent 0) of a workspace. */
 int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream);
 
-/* Erosion state: float4 per vertex (h_hi, h_lo, w, s): water and sediment
- * binary32, height as an unevaluated sum h_hi + h_lo of binary32s; values
- * are true values * 2^-K for the planet's scale exponent K (below). */
+/* Erosion state: a row of 8 floats per vertex, (h_hi, h_lo, w_hi, w_lo,
+ * s_hi, s_lo, 0, 0): height, water and sediment each an unevaluated sum
+ * hi + lo of binary32s; values are true values * 2^-K for the planet's
+ * scale exponent K (below). */
 
 /* Load binary64 fields (the reference's r_buff/heights, wat, sed; w/s may
- * be NULL for zeros) into the state st_dev float[4n], choosing a
+ * be NULL for zeros) into the state st_dev float[8n], choosing a
  * power-of-two scale so every value fits. */
 int nx_erosion_load(const double *h64_dev, const double *w64_dev, const double *s64_dev, int64_t n, float *st_dev,
                     void *workspace, size_t ws_bytes, void *stream);
@@ -275,26 +277,47 @@ int nx_erosion_ticks(const nx_erosion_planet *planets_dev, const nx_erosion_plan
                      int nticks, float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes, int nslots,
                      int remap, void *stream);
 
+/* Serving, temporally blocked: npasses launches over the same planet list,
+ * launch q advancing every listed planet by one pass of up to R iterations
+ * (R = the rings of nx_erosion_tb_config), planet p at its own pass
+ * pass + q - t_start (planets outside [0, nx_erosion_npass(iters)) skip).
+ * Every planet needs a tiling with R rings (a tiling with fewer sets err = 2
+ * in its control block and leaves the state).  Same results as
+ * nx_erosion_ticks; call nx_erosion_finish after a planet's last pass.
+ * remap = 1 rebuilds the launch's block map (whenever the list changed). */
+int nx_erosion_passes(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
+                      int pass, int npasses, float *st_dev, float *st_tmp_dev, void *workspace, size_t ws_bytes,
+                      int nslots, int remap, void *stream);
+
+/* Number of passes a temporally blocked run of `iters` iterations makes
+ * (iters rounded up to passes of R, plus one if needed so that the count has
+ * the parity of iters: a run ends in the buffer it started from iff iters
+ * is even, as with one launch per iteration). */
+int nx_erosion_npass(int iters);
+
 /* After each listed planet's last iteration: record its final scale
  * exponent in its control block's K[0] (read by nx_erosion_store and
  * nx_erosion_heights_batch). */
 int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
 
-/* Temporal blocking settings: the ring count of the tilings that batches
- * use (passes have up to that many iterations) and whether batches with
- * tilings use it (1) or run one iteration per launch (0). */
-int nx_erosion_tb_config(int rings, int enabled);
+/* Temporal blocking settings (process wide, default 4 rings, 512 threads,
+ * enabled): the ring count of the tilings that batches use (passes have up
+ * to that many iterations), threads per block of the blocked kernel (256,
+ * 512 or 1024), and whether batches with tilings use it (1) or run one
+ * iteration per launch (0).  The autotuner (nixis_gb300.autotune) picks
+ * rings, threads and the tile side per device. */
+int nx_erosion_tb_config(int rings, int threads, int enabled);
 
-/* Write one planet's state back as binary64 true values (h_hi + h_lo, w, s
- * times 2^K, K from the workspace's first control block).  w64_dev /
+/* Write one planet's state back as binary64 true values (hi + lo of each
+ * field times 2^K, K from the workspace's first control block).  w64_dev /
  * s64_dev may be NULL. */
 int nx_erosion_store(const float *st_dev, int64_t n, const void *workspace, double *h64_dev, double *w64_dev,
                      double *s64_dev, void *stream);
 
 /* Layout of a workspace's per-planet control block (32 bytes, planet p at
  * byte 32*p): after a run, K[0] is the planet's scale exponent (stored
- * value = true value * 2^-K[0]) and err != 0 flags a neighbour id outside
- * the planet's range. */
+ * value = true value * 2^-K[0]) and err = 1 flags a neighbour id outside
+ * the planet's range, err = 2 a tiling with fewer rings than a pass. */
 typedef struct nx_erosion_ctl {
     uint32_t maxbits[3];
     int32_t K[2];
@@ -305,10 +328,11 @@ typedef struct nx_erosion_ctl {
 
 /* Initial state of a batch from raw fBm sums (nx_fbm_batch output rows
  * and min/max keys, 2 per planet): h = util.rescale(raw, elev_lo, elev_hi)
- * (util.py:110-140), w = water0, s = 0, written to buffer (iters & 1). */
+ * (util.py:110-140), w = water0 (as a pair), s = 0, written to buffer
+ * (iters & 1). */
 int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
                           int nplanets, const float *raw_dev, const uint32_t *minmax_dev, float elev_lo,
-                          float elev_hi, float water0, float *st_dev, float *st_tmp_dev, void *stream);
+                          float elev_hi, double water0, float *st_dev, float *st_tmp_dev, void *stream);
 
 /* Heights of every planet of a finished batch into out_dev (packed rows):
  * (h_hi + h_lo) * 2^K, binary32. */
@@ -324,9 +348,9 @@ int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_eros
  * `iters` iterations like nx_erosion_steps on one planet of at most
  * NX_NOALLOC_MAX_VERTICES vertices (larger n returns NX_EINVAL) without
  * allocating: its scratch (second state buffer, control block, partial
- * sums) is a fixed array inside the library, about 4.2 MB, which every GPU
+ * sums) is a fixed array inside the library, about 8.4 MB, which every GPU
  * that loads the library keeps until the process exits.  The caller passes
- * the mesh, the state st_dev (float4 rows as in nx_erosion_load, true
+ * the mesh, the state st_dev (8-float rows as in nx_erosion_load, true
  * values with scale exponent 0, magnitudes below 2^96) and the outputs:
  * the state is updated in place, mass_dev (optional) as in
  * nx_erosion_steps, status_dev (optional, device int32[2]) gets the final

@@ -43,15 +43,17 @@ SIGNATURES = {
     "nx_fbm_planet_fill": (_i32, [_p, _i32, _p, _p, _d]),
     "nx_fbm_chunk_size": (_i32, []),
     "nx_fbm_batch": (_i32, [_p, _p, _i32, _p, _p]),
-    "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_float, _p, _p,
+    "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_double, _p, _p,
                                      _p]),
     "nx_erosion_heights_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p]),
     "nx_erosion_steps_noalloc": (_i32, [_p, _p, _i64, _p, _i32, ctypes.c_float, _p, _p, _p]),
     "nx_erosion_tick": (_i32, [_p, _p, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_finish": (_i32, [_p, _i32, _p, _p]),
     "nx_erosion_ticks": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
+    "nx_erosion_passes": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
+    "nx_erosion_npass": (_i32, [_i32]),
     "nx_tiling_shape": (_i32, [_i32, _i32, _i32, _p, _p, _p]),
-    "nx_erosion_tb_config": (_i32, [_i32, _i32]),
+    "nx_erosion_tb_config": (_i32, [_i32, _i32, _i32]),
     "nx_tiling_build": (_i32, [_i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p]),
 }
 

@@ -1,0 +1,195 @@
+"""Autotuner for the temporally blocked erosion kernel.
+
+Three knobs set how the blocked erosion maps onto the GPU: the tile side
+(tiles are side x side squares of a face grid; bigger tiles waste less work
+on halo rings but need more shared memory per block), the rings per pass
+(iterations done in shared memory between trips to HBM; more rings mean
+fewer trips but wider halos) and the threads per block.  ``tune`` times
+every candidate on a synthetic planet, checks that all of them give the
+same heights bit for bit (they run the same per-vertex arithmetic), keeps
+the fastest and caches it per device in a JSON file
+(``$NIXIS_GB300_CACHE`` or ``~/.cache/nixis_gb300/autotune.json``).
+``current`` returns the cached choice for the current device, or the
+defaults when this device was never tuned.
+"""
+import ctypes
+import json
+import os
+from dataclasses import asdict, dataclass
+
+import torch
+
+from . import _dev
+from ._lib import NxError, call, lib
+
+SMEM_LIMIT = 200 * 1024          # dynamic shared memory the blocked kernel may use
+ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
+SIDES = (32, 40, 48, 56)
+RINGS = (2, 3, 4, 5)
+THREADS = (256, 512, 1024)
+
+
+@dataclass(frozen=True)
+class TbConfig:
+    tile_side: int = 40
+    rings: int = 4
+    threads: int = 512
+
+
+DEFAULT = TbConfig()
+_current = {}
+
+
+def cache_path():
+    d = os.environ.get("NIXIS_GB300_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "nixis_gb300")
+    return os.path.join(d, "autotune.json")
+
+
+def device_key(index=None):
+    """Device name, SM count and library version: a tuning result is reused
+    only on the same kind of GPU with the same kernels."""
+    i = torch.cuda.current_device() if index is None else index
+    p = torch.cuda.get_device_properties(i)
+    return f"{p.name}|sm{p.multi_processor_count}|cc{p.major}.{p.minor}|lib{lib().nx_version()}"
+
+
+def _load(path):
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d if isinstance(d, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(path, table):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + f".{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def lookup(key, path=None):
+    """The cached configuration for a device key, or None."""
+    e = _load(path or cache_path()).get(key)
+    if not isinstance(e, dict):
+        return None
+    try:
+        return TbConfig(int(e["tile_side"]), int(e["rings"]), int(e["threads"]))
+    except (KeyError, TypeError, ValueError):
+        return None
+
+
+def store(key, cfg, timings=None, path=None):
+    path = path or cache_path()
+    table = _load(path)
+    entry = asdict(cfg)
+    if timings is not None:
+        entry["timings_ms"] = timings
+    table[key] = entry
+    _save(path, table)
+
+
+def current():
+    """The configuration in use on the current device (tuned, cached or default)."""
+    _dev.require_cuda()
+    dev = torch.cuda.current_device()
+    if dev not in _current:
+        _current[dev] = lookup(device_key(dev)) or DEFAULT
+    return _current[dev]
+
+
+def apply(cfg):
+    """Make cfg the blocked kernel's setting (process wide)."""
+    call("nx_erosion_tb_config", int(cfg.rings), int(cfg.threads), 1)
+
+
+def use(cfg):
+    """Use cfg on the current device from now on (without tuning)."""
+    _dev.require_cuda()
+    _current[torch.cuda.current_device()] = cfg
+    apply(cfg)
+
+
+def candidates(mesh):
+    """Every (side, rings, threads) whose tiles fit the shared-memory limit."""
+    out = []
+    for side in SIDES:
+        for rings in RINGS:
+            nt, nm, cm = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+            try:
+                call("nx_tiling_shape", mesh.k, side, rings, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm))
+            except NxError:
+                continue                         # more local vertices than a tile may hold
+            if nm.value * ROW_SMEM > SMEM_LIMIT:
+                continue
+            for threads in THREADS:
+                out.append(TbConfig(side, rings, threads))
+    return out
+
+
+def tune(divisions=400, iters=24, reps=3, configs=None, save=True, verbose=False):
+    """Time the candidates on one synthetic planet (12-octave terrain,
+    `iters` erosion iterations); returns (best config, {config: ms}).  Every
+    candidate must reproduce the first one's heights bit for bit."""
+    from . import mesh as _mesh
+    from . import planets as _planets
+    _dev.require_cuda()
+    cache = _mesh.MeshCache()
+    m = cache.get(divisions)
+    req = _planets.PlanetRequest(seed=12345, divisions=divisions, octaves=12, erosion_iters=iters)
+    configs = list(configs) if configs is not None else candidates(m)
+    timings, ref, best = {}, None, None
+    configs.sort(key=lambda c: (c.tile_side, c.rings, c.threads))
+    for cfg in configs:
+        for key in [k for k in m._tilings if k != (cfg.tile_side, cfg.rings)]:
+            del m._tilings[key]                  # one tiling resident at a time
+        tl = m.tiling(cfg.tile_side, cfg.rings)
+        if tl.maxnl * ROW_SMEM > SMEM_LIMIT:
+            continue
+        bt = _planets.PlanetBatch([req], cache, tb=cfg)
+        bt.launch()
+        torch.cuda.synchronize()
+        h = bt.heights[:m.n].clone()
+        if ref is None:
+            ref = h
+        elif not torch.equal(h, ref):
+            raise RuntimeError(f"autotune: {cfg} changed the results")
+        ms = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            bt.launch()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        t = min(ms)
+        timings[f"{cfg.tile_side}/{cfg.rings}/{cfg.threads}"] = round(t, 4)
+        if verbose:
+            print(f"autotune {cfg}: {t:.3f} ms", flush=True)
+        if best is None or t < best[1]:
+            best = (cfg, t)
+        del bt
+    if best is None:
+        raise RuntimeError("autotune: no candidate fits")
+    cfg = best[0]
+    use(cfg)
+    if save:
+        store(device_key(), cfg, timings)
+    return cfg, timings
+
+
+def ensure_tuned(**kw):
+    """The cached configuration for this device, tuning first if there is none."""
+    _dev.require_cuda()
+    cfg = lookup(device_key())
+    if cfg is None:
+        cfg, _ = tune(**kw)
+    else:
+        use(cfg)
+    return cfg
+
+
+__all__ = ["TbConfig", "DEFAULT", "current", "use", "apply", "tune", "ensure_tuned", "candidates", "lookup", "store",
+           "device_key", "cache_path"]

@@ -1,14 +1,17 @@
 // nx_erosion.cu -- erosion variant 3 (erosion.py:172-279) for sm_103a.
 //
-// State per vertex: float4 (h_hi, h_lo, w, s), double buffered (the
-// reference reads old arrays and writes copies, erosion.py:199-201,
-// 274-277).  Water and sediment are binary32; the height is an unevaluated
-// pair hi + lo of binary32s (about 48 significant bits) so that the small
-// per-iteration height changes the binary64 reference makes (1e-8 m on
-// heights of 1e3 m in early iterations) are kept, and the sign of
-// h_n - h_i -- the flow choice -- follows binary64 instead of tying.
-// Neighbour slots are the reference's (n,6) int32 table; edge lengths are
-// precomputed per slot in binary64 and rounded.
+// State per vertex: a row of 8 binary32s, (h_hi, h_lo, w_hi, w_lo) and
+// (s_hi, s_lo, 0, 0), double buffered (the reference reads old arrays and
+// writes copies, erosion.py:199-201, 274-277).  Height, water and sediment
+// are each an unevaluated pair hi + lo of binary32s (about 48 significant
+// bits).  Pairs keep the small per-iteration changes the binary64 reference
+// makes, and they keep the flow choice -- the sign of h_n - h_i -- on the
+// binary64 trajectory: with binary32 water and sediment the heights, which
+// become sums of eroded amounts, drift by ~1e-6 relative within tens of
+// iterations, enough to flip near-ties and move whole regions off the
+// reference's path.  Neighbour slots are the reference's (n,6) int32 table;
+// edge lengths are precomputed per slot in binary64 and kept as pairs too
+// (rounded to binary32 they alone move a 100-iteration run by ~1e-4).
 //
 // Overflow: under the reference's update, water and sediment grow about 2x
 // per iteration, past binary32's range after ~140 iterations.  The update is
@@ -39,10 +42,12 @@ constexpr int BLOCK = 256;
 constexpr float RESCALE_ABOVE = 7.9228163e28f;   // 2^96
 constexpr int RESCALE_SHIFT = 64;
 
-// erosion.py:205-207, rounded to binary32
-__device__ __constant__ float c_sol = (float)(0.01 / 320);
-__device__ __constant__ float c_evap = (float)(0.1 / 320);
-__device__ __constant__ float c_cap = (float)(0.2 / 320);
+// erosion.py:205-207 (solubility, 1 - evaporation, capacity) as pairs
+// hi + lo of the binary64 values
+constexpr double SOL = 0.01 / 320, ONE_M_EVAP = 1.0 - 0.1 / 320, CAP = 0.2 / 320;
+constexpr float SOL_H = (float)SOL, SOL_L = (float)(SOL - (double)SOL_H);
+constexpr float OE_H = (float)ONE_M_EVAP, OE_L = (float)(ONE_M_EVAP - (double)OE_H);
+constexpr float CAP_H = (float)CAP, CAP_L = (float)(CAP - (double)CAP_H);
 
 }  // namespace
 
@@ -58,7 +63,7 @@ struct StepArgs {
     const nx_erosion_planet *planets;
     const int2 *blk_map;   // per block of the launch: (planet index, block within the planet)
     int t;                 // global step; a planet's iteration is t - t_start
-    float4 *st0;
+    float4 *st0;           // rows of two float4s
     float4 *st1;
     nx_erosion_ctl *ctl;
     double *partials;      // [block][3] (mass sums only)
@@ -67,46 +72,97 @@ struct StepArgs {
     uint16_t *flow;        // optional: per vertex 2 bits per slot (1: neighbour higher, 2: lower)
 };
 
-// (hi, lo) + b with b binary32: two-sum, then renormalise (no FMA).
-__device__ __forceinline__ void df_add(float &hi, float &lo, float b)
+// Unevaluated pair hi + lo of binary32s.
+struct Pair {
+    float h, l;
+};
+
+// Knuth's two-sum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 {
-    float s = __fadd_rn(hi, b);
-    float bb = __fsub_rn(s, hi);
-    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-    e = __fadd_rn(e, lo);
-    hi = __fadd_rn(s, e);
-    lo = __fsub_rn(e, __fsub_rn(hi, s));
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// One neighbour's contribution (erosion.py:223-247): the flow choice is the
-// sign of h_j - h_i from the height pairs.  Branch free: with g = +1, -1 or
-// 0, fma(g, t, x) is exactly x + t, x - t or x (t*g is exact).  Returns the
-// flow code: 1 higher, 2 lower, 0 equal.
-__device__ __forceinline__ unsigned erode_accum(float hh, float hl, float hjh, float hjl, float wj, float d, float &sed,
-                                                float &wat)
+// pair + pair, renormalised
+__device__ __forceinline__ Pair padd(Pair a, Pair b)
 {
-    const float diff = __fadd_rn(__fsub_rn(hjh, hh), __fsub_rn(hjl, hl));
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    Pair r;
+    r.h = __fadd_rn(s, e);
+    r.l = __fsub_rn(e, __fsub_rn(r.h, s));
+    return r;
+}
+
+// pair * (ch + cl), not renormalised
+__device__ __forceinline__ Pair pmul(Pair a, float ch, float cl)
+{
+    Pair r;
+    r.h = __fmul_rn(a.h, ch);
+    float e = __fmaf_rn(a.h, ch, -r.h);
+    e = __fmaf_rn(a.h, cl, e);
+    r.l = __fmaf_rn(a.l, ch, e);
+    return r;
+}
+
+// (wh + wl) + r for binary32 rain r, not renormalised
+__device__ __forceinline__ Pair prain(float wh, float wl, float r)
+{
+    float s, e;
+    two_sum(wh, r, s, e);
+    return Pair{s, __fadd_rn(wl, e)};
+}
+
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// One neighbour's contribution (erosion.py:223-247).  o = (h_hi, h_lo,
+// w_hi, w_lo) of the neighbour, its water including this iteration's rain;
+// (dh, dl) the edge length pair.  The flow choice is the sign g (+1, -1, 0)
+// of h_j - h_i from the height pairs; then, as two-sums in paired binary32
+// lanes (FADD2), S += g*w_j (lane x) and W += g*w_j*d (lane y); A holds the
+// lanes' hi parts, L their lo parts.  Returns the flow code: 1 higher,
+// 2 lower, 0 equal.
+__device__ __forceinline__ unsigned erode_accum(float hh, float hl, float4 o, float dh, float dl, float2 &A, float2 &L)
+{
+    const float diff = __fadd_rn(__fsub_rn(o.x, hh), __fsub_rn(o.y, hl));
     const bool up = diff > 0.0f, dn = diff < 0.0f;
     const float g = up ? 1.0f : (dn ? -1.0f : 0.0f);
-    sed = __fmaf_rn(g, __fmul_rn(c_sol, wj), sed);
-    wat = __fmaf_rn(g, __fmul_rn(wj, d), wat);
+    const float xh = __fmul_rn(g, o.z), xl = __fmul_rn(g, o.w);
+    const float p = __fmul_rn(xh, dh);
+    float pe = __fmaf_rn(xh, dh, -p);
+    pe = __fmaf_rn(xh, dl, pe);
+    pe = __fmaf_rn(xl, dh, pe);
+    const float2 B = make_float2(xh, p);
+    const float2 s = __fadd2_rn(A, B);
+    const float2 bb = __fadd2_rn(s, neg2(A));
+    const float2 e = __fadd2_rn(__fadd2_rn(A, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(B, neg2(bb)));
+    L = __fadd2_rn(L, __fadd2_rn(e, make_float2(xl, pe)));
+    A = s;
     return up ? 1u : (dn ? 2u : 0u);
 }
 
-// erosion.py:262-267: new height pair, sediment and water.
-__device__ __forceinline__ void erode_finish(float hh, float hl, float wi, float si, float sed, float wat, float &nh,
-                                             float &nl, float &wn, float &sn)
+// erosion.py:261-267 from the accumulated S and W: sed = s + sol*S,
+// h -= sed, s += sed, w = w_i + W*(1 - evap), then the capacity test.
+// wi is the vertex's water including this iteration's rain.
+__device__ __forceinline__ void erode_finish(Pair hi, Pair wi, Pair si, float2 A, float2 L, Pair &hn, Pair &wn,
+                                             Pair &sn)
 {
-    nh = hh;
-    nl = hl;
-    df_add(nh, nl, -sed);
-    sn = __fadd_rn(si, sed);
-    wn = __fadd_rn(wi, __fsub_rn(wat, __fmul_rn(wat, c_evap)));
-    const float cw = __fmul_rn(c_cap, wn);
-    if (sn > cw) {
-        const float ex = __fsub_rn(sn, cw);
-        df_add(nh, nl, ex);
-        sn = __fsub_rn(sn, ex);
+    const Pair S{A.x, L.x}, W{A.y, L.y};
+    const Pair sed = padd(si, pmul(S, SOL_H, SOL_L));
+    hn = padd(hi, Pair{-sed.h, -sed.l});
+    sn = padd(si, sed);
+    wn = padd(wi, pmul(W, OE_H, OE_L));
+    const Pair c = pmul(wn, CAP_H, CAP_L);
+    Pair cw;
+    cw.h = __fadd_rn(c.h, c.l);
+    cw.l = __fsub_rn(c.l, __fsub_rn(cw.h, c.h));
+    if (__fadd_rn(__fsub_rn(sn.h, cw.h), __fsub_rn(sn.l, cw.l)) > 0.0f) {
+        const Pair ex = padd(sn, Pair{-cw.h, -cw.l});
+        hn = padd(hn, ex);
+        sn = cw;
     }
 }
 
@@ -136,7 +192,7 @@ __device__ __forceinline__ double warp_sum(double v)
 // block's planet.  No barrier on the common path: every thread reads the
 // (broadcast) planet descriptor and control words itself, and each warp
 // folds its max into the planet's next slot with a reduction atomic.
-__global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(BLOCK, 4) erosion_step_kernel(StepArgs a)
 {
     const int2 bm = a.blk_map[blockIdx.x];
     const int p = bm.x;
@@ -166,16 +222,17 @@ __global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
     double sh = 0.0, sw = 0.0, ss = 0.0;
     if (li < P.n) {
         const int2 *nb2 = reinterpret_cast<const int2 *>(P.nbr + 6 * li);
-        const float2 *el2 = reinterpret_cast<const float2 *>(P.edge + 6 * li);
+        const float4 *el4 = reinterpret_cast<const float4 *>(P.edge + 12 * li);
         const int2 n01 = nb2[0], n23 = nb2[1], n45 = nb2[2];
-        const float4 me = ist[i];
-        const float2 d01 = el2[0], d23 = el2[1], d45 = el2[2];
-        const float hh = __fmul_rn(me.x, lam), hl = __fmul_rn(me.y, lam);
-        const float wi = __fadd_rn(__fmul_rn(me.z, lam), rain);
-        const float si = __fmul_rn(me.w, lam);
-        float sed = si, wat = wi;
+        const float4 me = ist[2 * i], mb = ist[2 * i + 1];
+        const float4 d01 = el4[0], d23 = el4[1], d45 = el4[2];   // (hi, lo) per slot
+        const Pair hi{__fmul_rn(me.x, lam), __fmul_rn(me.y, lam)};
+        const Pair wi = prain(__fmul_rn(me.z, lam), __fmul_rn(me.w, lam), rain);
+        const Pair si{__fmul_rn(mb.x, lam), __fmul_rn(mb.y, lam)};
+        float2 A = make_float2(0.0f, wi.h), L = make_float2(0.0f, wi.l);
         const int nbr[6] = {n01.x, n01.y, n23.x, n23.y, n45.x, n45.y};
-        const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
+        const float dh[6] = {d01.x, d01.z, d23.x, d23.z, d45.x, d45.z};
+        const float dl[6] = {d01.y, d01.w, d23.y, d23.w, d45.y, d45.w};
         unsigned flow = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
@@ -185,16 +242,22 @@ __global__ void __launch_bounds__(BLOCK, 6) erosion_step_kernel(StepArgs a)
                 c->err = 1;
                 continue;
             }
-            const float4 o = ist[P.vbeg + j];
-            const float wj = __fadd_rn(__fmul_rn(o.z, lam), rain);
-            flow |= erode_accum(hh, hl, __fmul_rn(o.x, lam), __fmul_rn(o.y, lam), wj, dd[k], sed, wat) << (2 * k);
+            const float4 o = ist[2 * (P.vbeg + j)];
+            const Pair wj = prain(__fmul_rn(o.z, lam), __fmul_rn(o.w, lam), rain);
+            const float4 os = make_float4(__fmul_rn(o.x, lam), __fmul_rn(o.y, lam), wj.h, wj.l);
+            flow |= erode_accum(hi.h, hi.l, os, dh[k], dl[k], A, L) << (2 * k);
         }
-        float nh, nl, wn, sn;
-        erode_finish(hh, hl, wi, si, sed, wat, nh, nl, wn, sn);
-        ost[i] = make_float4(nh, nl, wn, sn);
+        Pair hn, wn, sn;
+        erode_finish(hi, wi, si, A, L, hn, wn, sn);
+        ost[2 * i] = make_float4(hn.h, hn.l, wn.h, wn.l);
+        ost[2 * i + 1] = make_float4(sn.h, sn.l, 0.0f, 0.0f);
         if (a.flow) a.flow[li] = (uint16_t)flow;
-        vmax = fmaxf(fabsf(nh), fmaxf(fabsf(wn), fabsf(sn)));
-        if (a.mass) { sh = (double)nh + (double)nl; sw = (double)wn; ss = (double)sn; }
+        vmax = fmaxf(fabsf(hn.h), fmaxf(fabsf(wn.h), fabsf(sn.h)));
+        if (a.mass) {
+            sh = (double)hn.h + (double)hn.l;
+            sw = (double)wn.h + (double)wn.l;
+            ss = (double)sn.h + (double)sn.l;
+        }
     }
     // block max -> the planet's max for the next iteration's rescale decision
     // (one atomic per block; NaN never wins fmaxf; inf still triggers a rescale)
@@ -298,7 +361,7 @@ __host__ __device__ __forceinline__ int tb_len(int iters, int R, int np, int q)
 struct TbArgs {
     const nx_erosion_planet *planets;
     const int2 *blk_map;   // (planet, tile), planets ordered by pass count, descending
-    int pass;
+    int pass;              // global pass; a planet's pass is pass - t_start
     int R;
     int smem_n;            // floats per shared array (>= every tile's local count)
     float4 *st0;
@@ -306,25 +369,36 @@ struct TbArgs {
     nx_erosion_ctl *ctl;
 };
 
-constexpr int TB_THREADS = 512;
+// Threads per block of the blocked kernel: 256, 512 or 1024 (autotuned),
+// sized for 1024 resident threads per SM (64 registers each).
 
-__global__ void __launch_bounds__(TB_THREADS, 3) erosion_tb_kernel(TbArgs a)
+// Shared memory of a pass for tiles of up to n local vertices: rows
+// (h_hi, h_lo, w_hi, w_lo) twice (read and write side) and (s_hi, s_lo)
+// once (a vertex's sediment is read and written only by its own thread).
+__host__ __device__ __forceinline__ size_t tb_smem_bytes(int n) { return (2 * sizeof(float4) + sizeof(float2)) * (size_t)n; }
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) erosion_tb_kernel(TbArgs a)
 {
     extern __shared__ float4 tsm4[];
     const int2 bm = a.blk_map[blockIdx.x];
     const nx_erosion_planet P = a.planets[bm.x];
     const int R = a.R;
     const int np = tb_npass(P.iters, R);
-    const int q = a.pass;
-    if (q >= np) return;
+    const int q = a.pass - P.t_start;            // the planet's own pass
+    if (q < 0 || q >= np) return;
     const int len = tb_len(P.iters, R, np, q);
     const nx_tiling TL = *P.tiling;
+    nx_erosion_ctl *c = a.ctl + P.slot;
+    if (TL.rings < len) {                        // tiling made for shorter passes
+        if (threadIdx.x == 0) c->err = 2;
+        return;
+    }
     const int tile = bm.y;
     const int32_t *cnt = TL.counts + (int64_t)tile * (TL.rings + 1);
     const int T = cnt[0];
     int NL = T;
     for (int r = 1; r <= len; ++r) NL += cnt[r];
-    nx_erosion_ctl *c = a.ctl + P.slot;
     // rescale per pass: growth is below 16x per iteration, so a max under
     // 2^(96 - 4R) stays under 2^96 through the pass
     const float m = __uint_as_float(__ldg(&c->maxbits[q % 3]));
@@ -341,50 +415,63 @@ __global__ void __launch_bounds__(TB_THREADS, 3) erosion_tb_kernel(TbArgs a)
     const bool par = ((np - q) & 1) != 0;
     const float4 *__restrict__ ist = par ? a.st1 : a.st0;
     float4 *__restrict__ ost = par ? a.st0 : a.st1;
-    float4 *buf0 = tsm4, *buf1 = tsm4 + a.smem_n;     // rows (h_hi, h_lo, w, s)
+    // rows (h_hi, h_lo, w_hi, w_lo), the water including the rain of the
+    // iteration about to read it; sediment pairs apart
+    float4 *buf0 = tsm4, *buf1 = tsm4 + a.smem_n;
+    float2 *sed = reinterpret_cast<float2 *>(tsm4 + 2 * a.smem_n);
     const int32_t *ids = TL.ids + (int64_t)tile * TL.nmax;
     for (int l = threadIdx.x; l < NL; l += blockDim.x) {
-        const float4 x = ist[P.vbeg + ids[l]];
-        buf0[l] = make_float4(__fmul_rn(x.x, lam), __fmul_rn(x.y, lam), __fmul_rn(x.z, lam), __fmul_rn(x.w, lam));
+        const int64_t row = P.vbeg + ids[l];
+        const float4 x = ist[2 * row];
+        const float4 y = ist[2 * row + 1];
+        const Pair wr = prain(__fmul_rn(x.z, lam), __fmul_rn(x.w, lam), rain);
+        buf0[l] = make_float4(__fmul_rn(x.x, lam), __fmul_rn(x.y, lam), wr.h, wr.l);
+        sed[l] = make_float2(__fmul_rn(y.x, lam), __fmul_rn(y.y, lam));
     }
     __syncthreads();
     const uint32_t *lnb = reinterpret_cast<const uint32_t *>(TL.lnbr) + (int64_t)tile * TL.cmax * 3;
-    const float2 *led = reinterpret_cast<const float2 *>(TL.ledge) + (int64_t)tile * TL.cmax * 3;
+    const float4 *led = reinterpret_cast<const float4 *>(TL.ledge) + (int64_t)tile * TL.cmax * 3;
     int C = NL - cnt[len];                      // members + rings 1..len-1
     for (int mi = 0; mi < len; ++mi) {
         const float4 *cur = (mi & 1) ? buf1 : buf0;
         float4 *nxt = (mi & 1) ? buf0 : buf1;
+        const bool more = mi + 1 < len;          // rain for the next iteration in the pass
         for (int l = threadIdx.x; l < C; l += blockDim.x) {
             const uint32_t p01 = __ldg(lnb + 3 * l), p23 = __ldg(lnb + 3 * l + 1), p45 = __ldg(lnb + 3 * l + 2);
-            const float2 d01 = __ldg(led + 3 * l), d23 = __ldg(led + 3 * l + 1), d45 = __ldg(led + 3 * l + 2);
+            const float4 d01 = __ldg(led + 3 * l), d23 = __ldg(led + 3 * l + 1), d45 = __ldg(led + 3 * l + 2);
             const float4 me = cur[l];
-            const float wi = __fadd_rn(me.z, rain);
-            float sed = me.w, wat = wi;
+            const float2 ms = sed[l];
+            float2 A = make_float2(0.0f, me.z), L = make_float2(0.0f, me.w);
             const uint32_t nb[6] = {p01 & 0xFFFFu, p01 >> 16, p23 & 0xFFFFu, p23 >> 16, p45 & 0xFFFFu, p45 >> 16};
-            const float dd[6] = {d01.x, d01.y, d23.x, d23.y, d45.x, d45.y};
+            const float dh[6] = {d01.x, d01.z, d23.x, d23.z, d45.x, d45.z};
+            const float dl[6] = {d01.y, d01.w, d23.y, d23.w, d45.y, d45.w};
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
                 // a missing neighbour (pentagon slot) is stored as the vertex
                 // itself: equal heights contribute nothing, as the reference's
                 // skip of -1
-                const float4 o = cur[nb[k]];
-                erode_accum(me.x, me.y, o.x, o.y, __fadd_rn(o.z, rain), dd[k], sed, wat);
+                erode_accum(me.x, me.y, cur[nb[k]], dh[k], dl[k], A, L);
             }
-            float nh, nl, wn, sn;
-            erode_finish(me.x, me.y, wi, me.w, sed, wat, nh, nl, wn, sn);
-            nxt[l] = make_float4(nh, nl, wn, sn);
+            Pair hn, wn, sn;
+            erode_finish(Pair{me.x, me.y}, Pair{me.z, me.w}, Pair{ms.x, ms.y}, A, L, hn, wn, sn);
+            const Pair wr = more ? prain(wn.h, wn.l, rain) : wn;
+            nxt[l] = make_float4(hn.h, hn.l, wr.h, wr.l);
+            sed[l] = make_float2(sn.h, sn.l);
         }
         __syncthreads();
-        if (mi + 1 < len) C -= cnt[len - 1 - mi];
+        if (more) C -= cnt[len - 1 - mi];
     }
     const float4 *fin = (len & 1) ? buf1 : buf0;
     float vmax = 0.0f;
     for (int l = threadIdx.x; l < T; l += blockDim.x) {
         const float4 v = fin[l];
-        ost[P.vbeg + ids[l]] = v;
-        vmax = fmaxf(vmax, fmaxf(fabsf(v.x), fmaxf(fabsf(v.z), fabsf(v.w))));
+        const float2 sv = sed[l];
+        const int64_t row = P.vbeg + ids[l];
+        ost[2 * row] = v;
+        ost[2 * row + 1] = make_float4(sv.x, sv.y, 0.0f, 0.0f);
+        vmax = fmaxf(vmax, fmaxf(fabsf(v.x), fmaxf(fabsf(v.z), fabsf(sv.x))));
     }
-    __shared__ float s_wmax[TB_THREADS / 32];
+    __shared__ float s_wmax[THREADS / 32];
     vmax = warp_max(vmax);
     if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = vmax;
     __syncthreads();
@@ -491,12 +578,10 @@ __global__ void erosion_load64_kernel(const double *__restrict__ h, const double
     int K = 0;
     if (m > 0x1p64) K = ilogb(m) - 64;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double hv = ldexp(h[i], -K);
-        float hh = (float)hv;
-        float hl = (float)(hv - (double)hh);
-        float wv = w ? (float)ldexp(w[i], -K) : 0.0f;
-        float sv = s ? (float)ldexp(s[i], -K) : 0.0f;
-        st[i] = make_float4(hh, hl, wv, sv);
+        const double hv = ldexp(h[i], -K), wv = w ? ldexp(w[i], -K) : 0.0, sv = s ? ldexp(s[i], -K) : 0.0;
+        const float hh = (float)hv, wh = (float)wv, sh = (float)sv;
+        st[2 * i] = make_float4(hh, (float)(hv - (double)hh), wh, (float)(wv - (double)wh));
+        st[2 * i + 1] = make_float4(sh, (float)(sv - (double)sh), 0.0f, 0.0f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         float mf = (float)ldexp(m, -K);
@@ -515,10 +600,10 @@ __global__ void erosion_store64_kernel(const float4 *__restrict__ st, int64_t n,
 {
     const int K = ctl->K[0];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float4 v = st[i];
+        const float4 v = st[2 * i], b = st[2 * i + 1];
         h[i] = ldexp((double)v.x + (double)v.y, K);
-        if (w) w[i] = ldexp((double)v.z, K);
-        if (so) so[i] = ldexp((double)v.w, K);
+        if (w) w[i] = ldexp((double)v.z + (double)v.w, K);
+        if (so) so[i] = ldexp((double)b.x + (double)b.y, K);
     }
 }
 
@@ -534,12 +619,12 @@ __device__ __forceinline__ int block_planet(const nx_erosion_planet *P, int np, 
 }
 
 // util.rescale (util.py:110-140) of the raw fBm sums to [lo, hi], and the
-// initial state (h, 0, water0, 0) in the buffer the planet's first
-// iteration reads: B[iters & 1].
+// initial state (h, 0, water0 as a pair | 0, 0, 0, 0) in the buffer the
+// planet's first iteration reads: B[iters & 1].
 __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_planet *__restrict__ P, int np,
                                                            const float *__restrict__ raw,
                                                            const uint32_t *__restrict__ minmax, float lo, float hi,
-                                                           float water0, float4 *__restrict__ st0,
+                                                           float w0h, float w0l, float4 *__restrict__ st0,
                                                            float4 *__restrict__ st1, int64_t total)
 {
     for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
@@ -553,7 +638,8 @@ __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_plan
         // ((x - min) * ((hi - lo) / (max - min))) + lo, unfused
         const float h = __fadd_rn(__fmul_rn(__fsub_rn(raw[row], mn), sc), lo);
         float4 *dst = (P[p].iters & 1) ? st1 : st0;
-        dst[row] = make_float4(h, 0.0f, water0, 0.0f);
+        dst[2 * row] = make_float4(h, 0.0f, w0h, w0l);
+        dst[2 * row + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
@@ -569,7 +655,7 @@ __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_p
         const int64_t row = blk * 256 + threadIdx.x;
         const int64_t i = row - P[p].vbeg;
         if (i < 0 || i >= P[p].n) continue;
-        float4 v = st[row];
+        const float4 v = st[2 * row];
         out[row] = (float)ldexp((double)v.x + (double)v.y, ctl[P[p].slot].K[0]);
     }
 }
@@ -659,13 +745,45 @@ static int64_t planet_blocks(const nx_erosion_planet &P) { return (P.n + BLOCK -
 // Temporal blocking: rings of the tilings in use (all planets of a batch
 // share it) and a switch for comparisons.
 static int g_tb_rings = 4;
+static int g_tb_threads = 512;
 static bool g_tb_enabled = true;
 
-NX_EXPORT int nx_erosion_tb_config(int rings, int enabled)
+NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int enabled)
 {
     if (rings < 1 || rings > 8) return nx::fail(NX_EINVAL, "nx_erosion_tb_config: rings must be in [1, 8]");
+    if (threads != 256 && threads != 512 && threads != 1024)
+        return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads must be 256, 512 or 1024");
     g_tb_rings = rings;
+    g_tb_threads = threads;
     g_tb_enabled = enabled != 0;
+    return NX_OK;
+}
+
+static cudaError_t launch_tb(int64_t grid, size_t smem, cudaStream_t s, const TbArgs &ta)
+{
+    switch (g_tb_threads) {
+    case 256: erosion_tb_kernel<256><<<(unsigned)grid, 256, smem, s>>>(ta); break;
+    case 1024: erosion_tb_kernel<1024><<<(unsigned)grid, 1024, smem, s>>>(ta); break;
+    default: erosion_tb_kernel<512><<<(unsigned)grid, 512, smem, s>>>(ta); break;
+    }
+    return cudaGetLastError();
+}
+
+// Shared-memory limit of the blocked kernel, set once per device.
+static int tb_prepare()
+{
+    static std::mutex mu;
+    static bool done[64] = {false};
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return nx::fail(NX_EINVAL, "erosion: device id %d out of range", dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!done[dev]) {
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        done[dev] = true;
+    }
     return NX_OK;
 }
 
@@ -709,20 +827,14 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     if (maxnl == 0) tb = false;
     if (tb) {
         R = g_tb_rings;
-        const size_t smem = 2 * sizeof(float4) * (size_t)maxnl;
-        if (smem > 200 * 1024) tb = false;
+        if (tb_smem_bytes(maxnl) > 200 * 1024) tb = false;
     }
     if (tb) {
         if (ws_bytes < nx_erosion_workspace_size((ntiles_all > nblk ? ntiles_all : nblk) * BLOCK, np))
             return nx::fail(NX_EINVAL, "erosion: workspace too small");
         Workspace w = carve(workspace, np, ntiles_all > nblk ? ntiles_all : nblk);
-        static bool attr_done[64] = {false};
-        int dev = 0;
-        NX_CHECK_CUDA(cudaGetDevice(&dev));
-        if (dev >= 0 && dev < 64 && !attr_done[dev]) {
-            NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-            attr_done[dev] = true;
-        }
+        int rc = tb_prepare();
+        if (rc) return rc;
         erosion_tb_map_kernel<<<np, 256, 0, s>>>(planets_dev, np, R, w.blk_map);
         NX_CHECK_LAUNCH("erosion_tb_map_kernel");
         nx::note_launch(1);
@@ -739,15 +851,14 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         ta.st0 = (float4 *)st_dev;
         ta.st1 = (float4 *)st_tmp;
         ta.ctl = w.ctl;
-        const size_t smem = 2 * sizeof(float4) * (size_t)maxnl;
+        const size_t smem = tb_smem_bytes(maxnl);
         for (int q = 0; q < maxpass; ++q) {
             int64_t grid = 0;
             for (int p = 0; p < np; ++p)
                 if (tb_npass(planets_host[p].iters, R) > q) grid += planets_host[p].ntiles;
             if (grid <= 0) break;
             ta.pass = q;
-            erosion_tb_kernel<<<(unsigned)grid, TB_THREADS, smem, s>>>(ta);
-            NX_CHECK_LAUNCH("erosion_tb_kernel");
+            NX_CHECK_CUDA(launch_tb(grid, smem, s, ta));
             nx::note_launch(1);
         }
         if (maxpass > 0) {
@@ -853,6 +964,59 @@ NX_EXPORT int nx_erosion_ticks(const nx_erosion_planet *planets_dev, const nx_er
     return NX_OK;
 }
 
+// Serving, temporally blocked: each launch advances every listed planet by
+// one pass (up to R iterations), planet p at its own pass
+// pass - t_start; planets outside [0, npass) skip.
+NX_EXPORT int nx_erosion_passes(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                                int nplanets, int pass, int npasses, float *st_dev, float *st_tmp_dev, void *workspace,
+                                size_t ws_bytes, int nslots, int remap, void *stream)
+{
+    if (nplanets <= 0 || npasses <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !st_dev || !st_tmp_dev || !workspace || nslots <= 0)
+        return nx::fail(NX_EINVAL, "nx_erosion_passes: bad arguments");
+    int64_t ntiles = 0;
+    int maxnl = 0;
+    for (int p = 0; p < nplanets; ++p) {
+        const nx_erosion_planet &P = planets_host[p];
+        if (P.vbeg < 0 || P.n < 0 || P.iters < 0 || P.slot < 0 || P.slot >= nslots || (P.n > 0 && (!P.nbr || !P.edge)))
+            return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d: bad descriptor", p);
+        if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0)
+            return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d has no tiling", p);
+        ntiles += P.ntiles;
+        if (P.maxnl > maxnl) maxnl = P.maxnl;
+    }
+    if (tb_smem_bytes(maxnl) > 200 * 1024) return nx::fail(NX_EINVAL, "nx_erosion_passes: tiles too large");
+    if (ws_bytes < nx_erosion_workspace_size(ntiles * BLOCK, nslots))
+        return nx::fail(NX_EINVAL, "nx_erosion_passes: workspace too small");
+    int rc = tb_prepare();
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    Workspace w = carve(workspace, nslots, ntiles);
+    const int R = g_tb_rings;
+    if (remap) {
+        erosion_tb_map_kernel<<<nplanets, 256, 0, s>>>(planets_dev, nplanets, R, w.blk_map);
+        NX_CHECK_LAUNCH("erosion_tb_map_kernel");
+        nx::note_launch(1);
+    }
+    TbArgs ta;
+    ta.planets = planets_dev;
+    ta.blk_map = w.blk_map;
+    ta.R = R;
+    ta.smem_n = maxnl;
+    ta.st0 = (float4 *)st_dev;
+    ta.st1 = (float4 *)st_tmp_dev;
+    ta.ctl = w.ctl;
+    for (int q = 0; q < npasses; ++q) {
+        ta.pass = pass + q;
+        NX_CHECK_CUDA(launch_tb(ntiles, tb_smem_bytes(maxnl), s, ta));
+        nx::note_launch(1);
+    }
+    return NX_OK;
+}
+
+// Passes a planet of `iters` iterations makes (temporally blocked runs).
+NX_EXPORT int nx_erosion_npass(int iters) { return tb_npass(iters, g_tb_rings); }
+
 // After a planet's last iteration: its final scale exponent into K[0].
 NX_EXPORT int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream)
 {
@@ -884,7 +1048,7 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
     NX_CHECK_CUDA(cudaMemcpyAsync(planet_dev, &P, sizeof(P), cudaMemcpyHostToDevice, s));
     // state enters in buffer 0; with an odd count the first iteration reads buffer 1
     if (iters & 1)
-        NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp_dev, st_dev, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp_dev, st_dev, 2 * sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, s));
     return run_batch(planet_dev, &P, 1, st_dev, st_tmp_dev, mass_dev, flow_dev, workspace, ws_bytes, s);
 }
 
@@ -940,7 +1104,7 @@ static int check_packed(const nx_erosion_planet *ph, int np, int64_t *total)
 
 NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
                                     int nplanets, const float *raw_dev, const uint32_t *minmax_dev, float elev_lo,
-                                    float elev_hi, float water0, float *st_dev, float *st_tmp_dev, void *stream)
+                                    float elev_hi, double water0, float *st_dev, float *st_tmp_dev, void *stream)
 {
     if (nplanets <= 0) return NX_OK;
     if (!planets_dev || !planets_host || !raw_dev || !minmax_dev || !st_dev || !st_tmp_dev)
@@ -949,8 +1113,9 @@ NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const 
     int rc = check_packed(planets_host, nplanets, &total);
     if (rc) return rc;
     if (total == 0) return NX_OK;
+    const float w0h = (float)water0, w0l = (float)(water0 - (double)w0h);
     erosion_init_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(planets_dev, nplanets, raw_dev, minmax_dev,
-                                                                         elev_lo, elev_hi, water0, (float4 *)st_dev,
+                                                                         elev_lo, elev_hi, w0h, w0l, (float4 *)st_dev,
                                                                          (float4 *)st_tmp_dev, total);
     NX_CHECK_LAUNCH("erosion_init_kernel");
     nx::note_launch(1);
@@ -994,7 +1159,7 @@ namespace {
 constexpr int64_t NOALLOC_MAX_N = NX_NOALLOC_MAX_VERTICES;
 constexpr size_t NOALLOC_HEAD = 512;    // descriptor (40 B) + control block (32 B), padded
 constexpr size_t NOALLOC_PARTIALS = (3 * sizeof(double) + sizeof(int2)) * (size_t)((NOALLOC_MAX_N + BLOCK - 1) / BLOCK);
-constexpr size_t NOALLOC_STATE = 16 * (size_t)NOALLOC_MAX_N;
+constexpr size_t NOALLOC_STATE = 32 * (size_t)NOALLOC_MAX_N;
 constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD + NOALLOC_PARTIALS + NOALLOC_STATE;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
@@ -1075,7 +1240,7 @@ NX_EXPORT int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge
     NX_CHECK_LAUNCH("noalloc_prepare_kernel");
     nx::note_launch(1);
     if (iters & 1)
-        NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp, st_dev, 16 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp, st_dev, 32 * (size_t)n, cudaMemcpyDeviceToDevice, s));
     size_t ws_bytes = nx_erosion_workspace_size(n, 1);
     static_assert(256 + sizeof(nx_erosion_ctl) + 16 + NOALLOC_PARTIALS <= NOALLOC_HEAD + NOALLOC_PARTIALS,
                   "partials fit before the second state buffer");

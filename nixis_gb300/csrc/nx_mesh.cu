@@ -239,23 +239,25 @@ __global__ void adj_sort_kernel(int64_t nv, const int32_t *__restrict__ in, int3
     }
 }
 
-// erosion.py:38-40 in binary64 (squares by multiplication), rounded to binary32.
+// erosion.py:38-40 in binary64 (squares by multiplication), split into a
+// pair hi + lo of binary32s: el[2q] = hi, el[2q+1] = lo.
 __global__ void edge_len_kernel(const double *__restrict__ xyz, const int32_t *__restrict__ nbr, int64_t nv,
-                                float *__restrict__ el, int *__restrict__ err)
+                                float2 *__restrict__ el, int *__restrict__ err)
 {
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 6 * nv; q += (int64_t)gridDim.x * blockDim.x) {
         int64_t v = q / 6;
         int32_t j = nbr[q];
-        float d = 0.0f;
+        double d = 0.0;
         if (j >= 0 && (int64_t)j < nv) {
             double dx = __dsub_rn(xyz[3 * v], xyz[3 * (int64_t)j]);
             double dy = __dsub_rn(xyz[3 * v + 1], xyz[3 * (int64_t)j + 1]);
             double dz = __dsub_rn(xyz[3 * v + 2], xyz[3 * (int64_t)j + 2]);
-            d = (float)__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
         } else if (j != -1 && err) {
             atomicOr(err, 1);
         }
-        el[q] = d;
+        const float hi = (float)d;
+        el[q] = make_float2(hi, (float)(d - (double)hi));
     }
 }
 
@@ -382,7 +384,7 @@ NX_EXPORT int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int
     if (nv < 0) return nx::fail(NX_EINVAL, "nx_edge_lengths: nv < 0");
     if (nv == 0) return NX_OK;
     if (!xyz_dev || !nbr_dev || !edge_dev) return nx::fail(NX_EINVAL, "nx_edge_lengths: null pointer");
-    edge_len_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, edge_dev, err_dev);
+    edge_len_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, (float2 *)edge_dev, err_dev);
     NX_CHECK_LAUNCH("edge_len_kernel");
     nx::note_launch(1);
     return NX_OK;
@@ -602,7 +604,8 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
             if (loc < 0) { s_bad = 1; loc = q; }
         }
         lnbr[((int64_t)tile * cmax + q) * 6 + sl] = (uint16_t)loc;
-        ledge[((int64_t)tile * cmax + q) * 6 + sl] = edge[6 * (int64_t)v + sl];
+        reinterpret_cast<float2 *>(ledge)[((int64_t)tile * cmax + q) * 6 + sl] =
+            reinterpret_cast<const float2 *>(edge)[6 * (int64_t)v + sl];
     }
     if (threadIdx.x == 0) {
         tc[0] = T;

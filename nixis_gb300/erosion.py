@@ -1,8 +1,8 @@
 """Drop-in for the reference's erosion module, variant 3 (the one nixis.py
 calls, nixis.py:410), plus the steepest-descent rule of find_lowest.
 
-State on the GPU is binary32 with a per-planet power-of-two scale (exact,
-see csrc/nx_erosion.cu); results are returned in the reference's float64
+State on the GPU is binary32 pairs (hi + lo) with a per-planet power-of-two
+scale (exact, see csrc/nx_erosion.cu); results are returned in the reference's float64
 arrays, updated in place like the reference.
 """
 import numpy as np
@@ -19,7 +19,7 @@ CAPACITY = 0.2 / 320        # erosion.py:207
 
 
 class ErosionRun:
-    """Resident binary32 erosion state of one planet.
+    """Resident erosion state of one planet (binary32 pairs).
 
     verts float64 (N,3) and neighbors int32 (N,6) as CUDA tensors (or
     numpy); fields are loaded from float64 heights / water / sediment."""
@@ -36,7 +36,7 @@ class ErosionRun:
                 raise IndexError("neighbors holds an id outside [-1, N)")
         self.edge = edge
         n = self.n
-        self.st = torch.empty((n, 4), dtype=torch.float32, device="cuda")    # (h_hi, h_lo, w, s)
+        self.st = torch.empty((n, 8), dtype=torch.float32, device="cuda")    # (h, w, s as hi/lo pairs, 0, 0)
         self.st_tmp = torch.empty_like(self.st)
         self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
         self.planet = torch.zeros(8, dtype=torch.int64, device="cuda")   # one nx_erosion_planet (40 B)

@@ -96,13 +96,14 @@ def sort_adjacency(adj, stream=None):
 
 
 def edge_lengths(xyz, nbr, stream=None):
-    """float32 (N,6) per-slot neighbour distances (binary64, rounded)."""
+    """float32 (N,6,2) per-slot neighbour distances (binary64, split into
+    (hi, lo) pairs)."""
     x = _dev.to_device(xyz, np.float64, name="verts")
     nb = _dev.to_device(nbr, np.int32, name="neighbors")
     n = x.shape[0]
     if nb.shape != (n, 6):
         raise ValueError("neighbors must have shape (N, 6)")
-    el = torch.empty((n, 6), dtype=torch.float32, device="cuda")
+    el = torch.empty((n, 6, 2), dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     call("nx_edge_lengths", _dev.ptr(x), _dev.ptr(nb), n, _dev.ptr(el), _dev.ptr(err), _dev.stream_handle(stream))
     return el, err
@@ -110,7 +111,8 @@ def edge_lengths(xyz, nbr, stream=None):
 
 class PlanetMesh:
     """A subdivision's resident mesh: xyz float64 (N,3), nbr int32 (N,6),
-    edge float32 (N,6); triangles are dropped after the adjacency is built."""
+    edge float32 (N,6,2) pairs; triangles are dropped after the adjacency is
+    built."""
 
     def __init__(self, divisions, stream=None):
         self.k = ico.check_divisions(divisions)
@@ -152,7 +154,7 @@ class MeshTiling:
         self.counts = torch.zeros(self.ntiles * (rings + 1), dtype=torch.int32, device=dev)
         self.ids = torch.empty(self.ntiles * self.nmax, dtype=torch.int32, device=dev)
         self.lnbr = torch.empty(self.ntiles * self.cmax * 6, dtype=torch.int16, device=dev)
-        self.ledge = torch.empty(self.ntiles * self.cmax * 6, dtype=torch.float32, device=dev)
+        self.ledge = torch.empty(self.ntiles * self.cmax * 12, dtype=torch.float32, device=dev)
         err = torch.zeros(3, dtype=torch.int32, device=dev)
         call("nx_tiling_build", mesh.k, tile_side, rings, _dev.ptr(mesh.nbr), _dev.ptr(mesh.edge), _dev.ptr(self.counts),
              _dev.ptr(self.ids), _dev.ptr(self.lnbr), _dev.ptr(self.ledge), _dev.ptr(err), _dev.stream_handle(stream))

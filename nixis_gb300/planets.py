@@ -23,6 +23,7 @@ import numpy as np
 import torch
 
 from . import _dev
+from . import autotune as _autotune
 from . import climate as _climate
 from . import mesh as _mesh
 from . import opensimplex as _osx
@@ -74,9 +75,27 @@ class PlanetRequest:
         return n * (4 + 16 + 16 + 4 + (4 if self.insolation else 0))
 
 
-def mesh_bytes(divisions):
+def _tiling_shape(divisions, tb):
+    nt, nm, cm = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    call("nx_tiling_shape", int(divisions), tb.tile_side, tb.rings, ctypes.byref(nt), ctypes.byref(nm),
+         ctypes.byref(cm))
+    return nt.value, nm.value, cm.value
+
+
+def tile_count(divisions, tb):
+    """Tiles of the temporally blocked erosion's tiling of a mesh."""
+    return _tiling_shape(divisions, tb)[0]
+
+
+def mesh_bytes(divisions, tb=None):
+    """HBM of a resident mesh: vertices, neighbours, edge lengths and (with
+    a blocked-erosion setting tb) the tiling for it."""
     n = 10 * divisions * divisions + 2
-    return n * (24 + 24 + 24)
+    b = n * (24 + 24 + 48)
+    if tb is not None:
+        nt, nm, cm = _tiling_shape(divisions, tb)
+        b += nt * ((tb.rings + 1) * 4 + nm * 4 + cm * 6 * (2 + 8))
+    return b
 
 
 @dataclass
@@ -95,7 +114,7 @@ def _struct_tensor(arr):
 class PlanetBatch:
     """A fixed set of planets, packed for batched execution."""
 
-    def __init__(self, requests, meshes=None, stream=None, blocked=True):
+    def __init__(self, requests, meshes=None, stream=None, blocked=True, tb=None):
         _dev.require_cuda()
         if not requests:
             raise ValueError("empty batch")
@@ -107,6 +126,9 @@ class PlanetBatch:
         self.requests = list(requests)
         self.meshes = meshes if meshes is not None else _mesh.MeshCache()
         self.stream = stream
+        self.blocked = blocked
+        # blocked erosion setting (tile side, rings, threads): autotuned or given
+        self.tb = (tb or _autotune.current()) if blocked else None
         np_ = len(requests)
         # pack in order of descending iteration count (stable)
         self.order = sorted(range(np_), key=lambda i: -requests[i].erosion_iters)
@@ -120,8 +142,8 @@ class PlanetBatch:
         N = off
         dev = "cuda"
         self.raw = torch.empty(N, dtype=torch.float32, device=dev)
-        self.st = torch.empty((N, 4), dtype=torch.float32, device=dev)
-        self.st_tmp = torch.empty((N, 4), dtype=torch.float32, device=dev)
+        self.st = torch.empty((N, 8), dtype=torch.float32, device=dev)
+        self.st_tmp = torch.empty((N, 8), dtype=torch.float32, device=dev)
         self.heights = torch.empty(N, dtype=torch.float32, device=dev)
         self.any_inso = any(r.insolation for r in requests)
         self.inso = torch.empty(N, dtype=torch.float32, device=dev) if self.any_inso else None
@@ -167,7 +189,7 @@ class PlanetBatch:
             e.t_start = 0
             e.slot = j
             if blocked and r.erosion_iters > 0:
-                tl = m.tiling(stream=stream)
+                tl = m.tiling(self.tb.tile_side, self.tb.rings, stream=stream)
                 e.tiling = tl.dev.data_ptr()
                 e.ntiles = tl.ntiles
                 e.maxnl = tl.maxnl
@@ -177,7 +199,8 @@ class PlanetBatch:
         rows = N
         if blocked:
             # the block map of a blocked run has one entry per tile
-            nt = sum(self.meshes.get(r.divisions).tiling().ntiles for r in requests if r.erosion_iters > 0)
+            nt = sum(self.meshes.get(r.divisions).tiling(self.tb.tile_side, self.tb.rings).ntiles
+                     for r in requests if r.erosion_iters > 0)
             rows = max(rows, nt * ALIGN)
         self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(rows, np_)), dtype=torch.uint8, device=dev)
         self.max_iters = max(r.erosion_iters for r in requests)
@@ -212,9 +235,11 @@ class PlanetBatch:
         call("nx_fbm_batch", _dev.ptr(self.fb_dev), ctypes.cast(self.fb_host, ctypes.c_void_p), np_, None, s)
         call("nx_erosion_init_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
              _dev.ptr(self.raw), _dev.ptr(self.minmax), ctypes.c_float(self.requests[0].elev_lo),
-             ctypes.c_float(self.requests[0].elev_hi), ctypes.c_float(self.requests[0].water0), _dev.ptr(self.st),
+             ctypes.c_float(self.requests[0].elev_hi), ctypes.c_double(self.requests[0].water0), _dev.ptr(self.st),
              _dev.ptr(self.st_tmp), s)
         call("nx_erosion_ctl_init", _dev.ptr(self.ws), self.ws.numel(), np_, s)
+        if self.blocked:
+            _autotune.apply(self.tb)
         call("nx_erosion_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
              _dev.ptr(self.st), _dev.ptr(self.st_tmp), None, _dev.ptr(self.ws), self.ws.numel(), s)
         call("nx_erosion_heights_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
@@ -242,8 +267,7 @@ class PlanetBatch:
     def erosion_launches(self):
         """Erosion launches per run: passes of the blocked path, or iterations."""
         if any(self.er_host[j].tiling for j in range(len(self.requests))):
-            R = _mesh.TILE_RINGS
-            return max(_tb_npass(r.erosion_iters, R) for r in self.requests)
+            return max(_tb_npass(r.erosion_iters, self.tb.rings) for r in self.requests)
         return self.max_iters
 
     def kernels_per_run(self):
@@ -298,8 +322,8 @@ class _PlainWork:
         if n > self.n:
             self.raw = torch.empty(n, dtype=torch.float32, device="cuda")
             self.hm = torch.empty(n, dtype=torch.float64, device="cuda")
-            self.st = torch.empty((n, 4), dtype=torch.float32, device="cuda")
-            self.st_tmp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+            self.st = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+            self.st_tmp = torch.empty((n, 8), dtype=torch.float32, device="cuda")
             self.inso = torch.empty(n, dtype=torch.float32, device="cuda")
             self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
             self.planet = torch.zeros(8, dtype=torch.int64, device="cuda")

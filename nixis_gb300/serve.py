@@ -2,14 +2,15 @@
 
 Requests (seed, divisions, octaves, erosion iterations, insolation) arrive
 over time.  The engine works in ticks; one tick is one erosion launch that
-advances every planet currently eroding by one iteration, each at its own
-iteration count (nx_erosion_ticks launches up to max_ticks of them per host
-step, stopping when an eroding planet finishes).  Between steps, arrived
-requests are
-admitted as memory frees up:
+advances every planet currently eroding by one temporally blocked pass (up
+to 4 iterations in shared memory, nx_erosion_passes), each planet at its own
+pass count; with blocked=False a tick is one iteration (nx_erosion_ticks).
+Up to max_ticks ticks are launched per host step, stopping when an eroding
+planet finishes.  Between steps, arrived requests are admitted as memory
+frees up:
 
 * state rows come from a fixed arena (first fit, 256-row aligned) holding
-  (h_hi, h_lo, w, s) x 2, raw fBm, heights and insolation per vertex;
+  two 8-float state rows, raw fBm, heights and insolation per vertex;
 * meshes stay resident, keyed by divisions, evicted least recently used
   when no admitted planet uses them;
 * admission is first-come first-served against the HBM budget (arena +
@@ -33,6 +34,7 @@ import numpy as np
 import torch
 
 from . import _dev
+from . import autotune as _autotune
 from . import climate as _climate
 from . import mesh as _mesh
 from . import opensimplex as _osx
@@ -40,7 +42,7 @@ from . import planets as _planets
 from ._lib import ErosionPlanet, FbmPlanet, call, lib
 
 ALIGN = 256
-ROW_BYTES = 16 + 16 + 4 + 4 + 4
+ROW_BYTES = 32 + 32 + 4 + 4 + 4
 
 
 class RowArena:
@@ -82,14 +84,15 @@ class ResidentMeshes:
     """Meshes in HBM with reference counts; unreferenced ones are evicted
     least recently used when the budget requires it."""
 
-    def __init__(self, budget_bytes):
+    def __init__(self, budget_bytes, tb=None):
         self.budget = budget_bytes
+        self.tb = tb                 # blocked-erosion setting whose tilings count against the budget
         self.meshes = {}
         self.refs = {}
         self.lru = []
 
     def bytes_for(self, k):
-        return 0 if k in self.meshes else _planets.mesh_bytes(k)
+        return 0 if k in self.meshes else _planets.mesh_bytes(k, self.tb)
 
     def resident_bytes(self):
         return sum(m.nbytes for m in self.meshes.values())
@@ -104,7 +107,7 @@ class ResidentMeshes:
 
     def acquire(self, k, stream=None):
         if k not in self.meshes:
-            need = _planets.mesh_bytes(k)
+            need = _planets.mesh_bytes(k, self.tb)
             while self.resident_bytes() + need > self.budget:
                 victim = next((q for q in self.lru if self.refs.get(q, 0) == 0), None)
                 if victim is None:
@@ -143,6 +146,8 @@ class Ticket:
     slot: int = 0
     t_start: int = 0
     mesh: object = None
+    tiling: object = None
+    tiles: int = 0
     host_h: torch.Tensor = None
     host_i: torch.Tensor = None
     done_event: object = None
@@ -162,22 +167,29 @@ def _descs_tensor(arr):
 class ServeEngine:
     """Continuous-batching planet generator over one GPU."""
 
-    def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None, max_ticks=8):
+    def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None, max_ticks=8,
+                 blocked=True):
         _dev.require_cuda()
         self.budget = int(hbm_budget)
         rows = arena_rows if arena_rows is not None else int(self.budget * arena_fraction) // ROW_BYTES
         self.arena = RowArena(rows)
         R = self.arena.capacity
         dev = "cuda"
-        self.st = torch.empty((R, 4), dtype=torch.float32, device=dev)
-        self.st_tmp = torch.empty((R, 4), dtype=torch.float32, device=dev)
+        self.st = torch.empty((R, 8), dtype=torch.float32, device=dev)
+        self.st_tmp = torch.empty((R, 8), dtype=torch.float32, device=dev)
         self.raw = torch.empty(R, dtype=torch.float32, device=dev)
         self.heights = torch.empty(R, dtype=torch.float32, device=dev)
         self.inso = torch.empty(R, dtype=torch.float32, device=dev)
         self.nslots = slots
-        self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(R, slots)), dtype=torch.uint8, device=dev)
+        # block map and partials for R rows, or for the tiles of the planets
+        # in them (at most 2 x 256 per row for meshes of divisions >= 16)
+        self.ws_rows = 2 * R
+        self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(self.ws_rows, slots)), dtype=torch.uint8, device=dev)
+        self.blocked = blocked
+        self.tb = _autotune.current() if blocked else None
+        self.tiles_admitted = 0
         self.free_slots = list(range(slots))
-        self.meshes = ResidentMeshes(self.budget - R * ROW_BYTES - self.ws.numel())
+        self.meshes = ResidentMeshes(self.budget - R * ROW_BYTES - self.ws.numel(), self.tb)
         self.main = torch.cuda.Stream()
         self.side = torch.cuda.Stream()
         self.desc_dev = torch.empty(slots * ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device=dev)
@@ -217,15 +229,24 @@ class ServeEngine:
                 break
             if not self.meshes.can_fit(r.divisions):
                 break
+            tiles = 0
+            if self.blocked and r.erosion_iters > 0:
+                tiles = _planets.tile_count(r.divisions, self.tb)
+                if (self.tiles_admitted + tiles) * 256 > self.ws_rows:
+                    break
             vbeg = self.arena.alloc(r.n_vertices)
             if vbeg is None:
                 break
+            self.tiles_admitted += tiles
+            t.tiles = tiles
             self.queue.pop(0)
             t.vbeg = vbeg
             t.slot = self.free_slots.pop()
             t.admitted = time.perf_counter()
             with torch.cuda.stream(self.side):
                 t.mesh = self.meshes.acquire(r.divisions)
+                t.tiling = (t.mesh.tiling(self.tb.tile_side, self.tb.rings, stream=self.side)
+                            if self.blocked and r.erosion_iters > 0 else None)
             admitted.append(t)
         return admitted
 
@@ -274,9 +295,9 @@ class ServeEngine:
                 e_dev = _descs_tensor(e).to("cuda", non_blocking=True)
                 call("nx_erosion_init_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
                      ctypes.c_void_p(self.raw.data_ptr() + 4 * t.vbeg), _dev.ptr(mm_dev[j]),
-                     ctypes.c_float(r.elev_lo), ctypes.c_float(r.elev_hi), ctypes.c_float(r.water0),
-                     ctypes.c_void_p(self.st.data_ptr() + 16 * t.vbeg),
-                     ctypes.c_void_p(self.st_tmp.data_ptr() + 16 * t.vbeg), s)
+                     ctypes.c_float(r.elev_lo), ctypes.c_float(r.elev_hi), ctypes.c_double(r.water0),
+                     ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg),
+                     ctypes.c_void_p(self.st_tmp.data_ptr() + 32 * t.vbeg), s)
                 t._e_single = (e, e_dev)
                 t.host_h = torch.empty(t.mesh.n, dtype=torch.float32).pin_memory()
                 if r.insolation:
@@ -301,7 +322,7 @@ class ServeEngine:
             if r.erosion_iters > 0:
                 call("nx_erosion_finish", _dev.ptr(e_dev), 1, ws, s)
             call("nx_erosion_heights_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
-                 ctypes.c_void_p(self.st.data_ptr() + 16 * t.vbeg), ws,
+                 ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg), ws,
                  ctypes.c_void_p(self.heights.data_ptr() + 4 * t.vbeg), s)
         ev = torch.cuda.Event()
         ev.record(stream)
@@ -337,6 +358,10 @@ class ServeEngine:
                 arr[q].rain = t.request.rain
                 arr[q].t_start = t.t_start
                 arr[q].slot = t.slot
+                if t.tiling is not None:
+                    arr[q].tiling = t.tiling.dev.data_ptr()
+                    arr[q].ntiles = t.tiling.ntiles
+                    arr[q].maxnl = t.tiling.maxnl
             host = _descs_tensor(arr)
             with torch.cuda.stream(self.main):
                 self.desc_dev[:host.numel()].copy_(host, non_blocking=True)
@@ -362,15 +387,18 @@ class ServeEngine:
         if er:
             # advance until the first eroding planet finishes, at most
             # max_ticks per host step (new arrivals join at step boundaries)
-            left = min(t.t_start + t.request.erosion_iters - self.tick for t in er)
+            blocked = self.blocked
+            left = min(t.t_start + self._ticks_of(t, blocked) - self.tick for t in er)
             n = max(1, min(left, self.max_ticks))
             arr, _ = self._descs_host
-            call("nx_erosion_ticks", _dev.ptr(self.desc_dev), ctypes.cast(arr, ctypes.c_void_p), len(er), self.tick,
-                 n, _dev.ptr(self.st), _dev.ptr(self.st_tmp), _dev.ptr(self.ws), self.ws.numel(), self.nslots,
-                 1 if remap else 0, _dev.stream_handle(self.main))
+            if blocked:
+                _autotune.apply(self.tb)
+            call("nx_erosion_passes" if blocked else "nx_erosion_ticks", _dev.ptr(self.desc_dev),
+                 ctypes.cast(arr, ctypes.c_void_p), len(er), self.tick, n, _dev.ptr(self.st), _dev.ptr(self.st_tmp),
+                 _dev.ptr(self.ws), self.ws.numel(), self.nslots, 1 if remap else 0, _dev.stream_handle(self.main))
             self.tick += n
             for t in er:
-                if self.tick - t.t_start == t.request.erosion_iters:
+                if self.tick - t.t_start == self._ticks_of(t, blocked):
                     t.stage = "finishing"
                     self._output(t, after_main=True)
             ev = torch.cuda.Event()
@@ -382,6 +410,10 @@ class ServeEngine:
         self._collect()
         return bool(er) or bool(new)
 
+    def _ticks_of(self, t, blocked):
+        it = t.request.erosion_iters
+        return int(lib().nx_erosion_npass(it)) if blocked else it
+
     def _collect(self):
         still = []
         for t in self.active:
@@ -392,8 +424,10 @@ class ServeEngine:
                 self.arena.release(t.vbeg, t.mesh.n)
                 self.free_slots.append(t.slot)
                 self.meshes.release(t.request.divisions)
+                self.tiles_admitted -= t.tiles
                 t.stage = "done"
                 t.mesh = None
+                t.tiling = None
                 t._keep = None
                 self.done.append(t)
             else:

@@ -447,52 +447,124 @@ NXO_API int nxo_erode_terrain3(const double *xyz, const int32_t *nbr, int64_t n,
 }
 
 /*
- * The same update evaluated with the GPU kernel's arithmetic: water and
- * sediment in binary32, the height as an unevaluated pair hi + lo of
- * binary32s, the slope sign taken from (hj_hi - hi_hi) + (hj_lo - hi_lo),
- * and the edge length supplied per neighbour slot (edge_len[6*i+k],
- * computed once in binary64 and rounded).  State rows are (h_hi, h_lo, w, s).
- * Used to check the kernel operation for operation (bit for bit).
+ * The same update evaluated with the GPU kernel's arithmetic, operation for
+ * operation, so the kernel can be checked bit for bit.  Height, water and
+ * sediment are unevaluated pairs hi + lo of binary32s (about 48 significant
+ * bits); edge lengths are supplied per neighbour slot as pairs too
+ * (edge_len[12*i+2k] + edge_len[12*i+2k+1], computed once in binary64).  State rows are 8
+ * floats: (h_hi, h_lo, w_hi, w_lo, s_hi, s_lo, 0, 0).  `rain` (binary32) is
+ * added to every vertex's water before the update, as erode_terrain3 does
+ * (erosion.py:182-184).
+ *
+ * Per neighbour j in slot order the flow sign g (+1, -1, 0) is the sign of
+ * (hj_hi - hi_hi) + (hj_lo - hi_lo); the update accumulates S = sum g*w_j
+ * and W = w_i + sum g*w_j*d_j (erosion.py:238-247) in pairs, then
+ * sed_amt = s_i + sol*S, h -= sed_amt, s += sed_amt,
+ * w = w_i + W*(1 - evap), and the capacity test moves s - cap*w to h
+ * (erosion.py:261-267).  sol, 1 - evap and cap are binary64 constants
+ * split into pairs.
  */
-static void df_add(float *hi, float *lo, float b)
+typedef struct { float h, l; } nxo_pair;
+
+/* Knuth's two-sum: s + e == a + b exactly. */
+static void two_sum(float a, float b, float *s, float *e)
 {
-    float s = *hi + b;
-    float bb = s - *hi;
-    float e = (*hi - (s - bb)) + (b - bb);
-    e = e + *lo;
-    float h2 = s + e;
-    *lo = e - (h2 - s);
-    *hi = h2;
+    float x = a + b;
+    float bb = x - a;
+    *e = (a - (x - bb)) + (b - bb);
+    *s = x;
 }
 
-NXO_API void nxo_erosion_iteration3_f32(const float *edge_len, const int32_t *nbr, int64_t n,
-                                        const float *st, float *out)
+/* pair + pair, renormalised */
+static nxo_pair padd(nxo_pair a, nxo_pair b)
 {
-    const float sol = (float)SOLUBILITY, evap = (float)EVAPORATION, cap = (float)CAPACITY;
+    float s, e;
+    two_sum(a.h, b.h, &s, &e);
+    e = e + (a.l + b.l);
+    nxo_pair r;
+    r.h = s + e;
+    r.l = e - (r.h - s);
+    return r;
+}
+
+/* pair * (ch + cl), not renormalised */
+static nxo_pair pmul(nxo_pair a, float ch, float cl)
+{
+    nxo_pair r;
+    r.h = a.h * ch;
+    float e = fmaf(a.h, ch, -r.h);
+    e = fmaf(a.h, cl, e);
+    r.l = fmaf(a.l, ch, e);
+    return r;
+}
+
+/* (wh + wl) + r with r binary32, not renormalised */
+static nxo_pair prain(float wh, float wl, float r)
+{
+    float s, e;
+    two_sum(wh, r, &s, &e);
+    nxo_pair x = {s, wl + e};
+    return x;
+}
+
+static void split_const(double c, float *h, float *l)
+{
+    *h = (float)c;
+    *l = (float)(c - (double)*h);
+}
+
+NXO_API void nxo_erosion_iteration3_pair(const float *edge_len, const int32_t *nbr, int64_t n, const float *st,
+                                         float rain, float *out)
+{
+    float sol_h, sol_l, oe_h, oe_l, cap_h, cap_l;
+    split_const(SOLUBILITY, &sol_h, &sol_l);
+    split_const(1.0 - EVAPORATION, &oe_h, &oe_l);
+    split_const(CAPACITY, &cap_h, &cap_l);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
-        const float hh = st[4 * i], hl = st[4 * i + 1], wi = st[4 * i + 2], si = st[4 * i + 3];
-        float sed_amt = si, wat_amt = wi;
+        const float *me = st + 8 * i;
+        const nxo_pair hi = {me[0], me[1]}, si = {me[4], me[5]};
+        const nxo_pair wi = prain(me[2], me[3], rain);
+        float Sh = 0.0f, Sl = 0.0f, Wh = wi.h, Wl = wi.l;
         for (int k = 0; k < 6; ++k) {
             int32_t j = nbr[6 * i + k];
             if (j == -1) continue;
-            float d = edge_len[6 * i + k];
-            const float *o = st + 4 * (int64_t)j;
-            float diff = (o[0] - hh) + (o[1] - hl);
-            if (diff > 0) { sed_amt += sol * o[2]; wat_amt += o[2] * d; }
-            else if (diff < 0) { sed_amt -= sol * o[2]; wat_amt -= o[2] * d; }
+            const float dh = edge_len[12 * i + 2 * k], dl = edge_len[12 * i + 2 * k + 1];
+            const float *o = st + 8 * (int64_t)j;
+            const float diff = (o[0] - hi.h) + (o[1] - hi.l);
+            const float g = diff > 0 ? 1.0f : (diff < 0 ? -1.0f : 0.0f);
+            const nxo_pair wj = prain(o[2], o[3], rain);
+            const float xh = g * wj.h, xl = g * wj.l;
+            const float p = xh * dh;
+            float pe = fmaf(xh, dh, -p);
+            pe = fmaf(xh, dl, pe);
+            pe = fmaf(xl, dh, pe);
+            float s, e;
+            two_sum(Sh, xh, &s, &e);
+            Sl = Sl + (e + xl);
+            Sh = s;
+            two_sum(Wh, p, &s, &e);
+            Wl = Wl + (e + pe);
+            Wh = s;
         }
-        float nh = hh, nl = hl;
-        df_add(&nh, &nl, -sed_amt);
-        float sn = si + sed_amt;
-        float wn = wi + (wat_amt - wat_amt * evap);
-        float cw = cap * wn;
-        if (sn > cw) {
-            float ex = sn - cw;
-            df_add(&nh, &nl, ex);
-            sn -= ex;
+        const nxo_pair S = {Sh, Sl}, W = {Wh, Wl};
+        const nxo_pair sed = padd(si, pmul(S, sol_h, sol_l));
+        const nxo_pair nsed = {-sed.h, -sed.l};
+        nxo_pair hn = padd(hi, nsed);
+        nxo_pair sn = padd(si, sed);
+        const nxo_pair wn = padd(wi, pmul(W, oe_h, oe_l));
+        const nxo_pair c = pmul(wn, cap_h, cap_l);
+        nxo_pair cw;
+        cw.h = c.h + c.l;
+        cw.l = c.l - (cw.h - c.h);
+        if ((sn.h - cw.h) + (sn.l - cw.l) > 0) {
+            const nxo_pair ncw = {-cw.h, -cw.l};
+            const nxo_pair ex = padd(sn, ncw);
+            hn = padd(hn, ex);
+            sn = cw;
         }
-        out[4 * i] = nh; out[4 * i + 1] = nl; out[4 * i + 2] = wn; out[4 * i + 3] = sn;
+        float *q = out + 8 * i;
+        q[0] = hn.h; q[1] = hn.l; q[2] = wn.h; q[3] = wn.l; q[4] = sn.h; q[5] = sn.l; q[6] = 0.0f; q[7] = 0.0f;
     }
 }
 

@@ -46,7 +46,7 @@ def lib():
             "nxo_make_bool_elevation_mask": (None, [_p, _i64, _d, _p]),
             "nxo_erosion_iteration3": (_i32, [_p, _p, _i64, _p, _p, _p]),
             "nxo_erode_terrain3": (_i32, [_p, _p, _i64, _p, _i32]),
-            "nxo_erosion_iteration3_f32": (None, [_p, _p, _i64, _p, _p]),
+            "nxo_erosion_iteration3_pair": (None, [_p, _p, _i64, _p, ctypes.c_float, _p]),
             "nxo_find_lowest": (_i32, [_i64, _p, _p]),
             "nxo_day2deg": (_d, [_d, _d]),
             "nxo_calculate_seasonal_tilt": (_d, [_d, _d]),
@@ -151,15 +151,27 @@ def erode_terrain3(nodes, neighbors, heights, num_iter=1):
         raise MemoryError("oracle erode_terrain3: allocation failed")
 
 
-def erosion_iteration3_f32(edge_len, neighbors, st):
-    """The update with the GPU kernel's arithmetic on rows (h_hi, h_lo, w, s)
-    (float32 (N,4)); returns the new rows."""
+def erosion_iteration3_pair(edge_len, neighbors, st, rain=0.0):
+    """The update with the GPU kernel's arithmetic on rows (h_hi, h_lo,
+    w_hi, w_lo, s_hi, s_lo, 0, 0) (float32 (N,8)) with edge lengths as
+    (hi, lo) pairs (float32 (N,6,2)); returns the new rows."""
     el = _c(edge_len, np.float32)
     nbr = _c(neighbors, np.int32)
     st = _c(st, np.float32)
     out = np.empty_like(st)
-    lib().nxo_erosion_iteration3_f32(_ptr(el), _ptr(nbr), len(nbr), _ptr(st), _ptr(out))
+    lib().nxo_erosion_iteration3_pair(_ptr(el), _ptr(nbr), len(nbr), _ptr(st), float(np.float32(rain)), _ptr(out))
     return out
+
+
+def pair_rows(h, w, s):
+    """float64 fields -> (N,8) float32 state rows (each field split into a
+    binary32 pair, as the GPU loads them)."""
+    st = np.zeros((len(h), 8), np.float32)
+    for c, v in ((0, h), (2, w), (4, s)):
+        v = np.asarray(v, np.float64)
+        st[:, c] = v.astype(np.float32)
+        st[:, c + 1] = (v - st[:, c].astype(np.float64)).astype(np.float32)
+    return st
 
 
 def split_heights(h):

@@ -90,12 +90,15 @@ def icosphere(k, with_tris=True):
 
 def edge_lengths(pts, adj):
     """Per-slot neighbour distance, binary64 with erosion.py:38-40's formula,
-    rounded to binary32; 0 where the slot is -1."""
-    out = np.zeros(adj.shape, np.float32)
+    split into a binary32 pair (hi, lo): float32 (N, 6, 2); 0 where the slot
+    is -1."""
+    out = np.zeros(adj.shape + (2,), np.float32)
     valid = adj >= 0
     for k in range(6):
         j = np.where(valid[:, k], adj[:, k], 0)
         d = pts - pts[j]
-        dist = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2])
-        out[:, k] = np.where(valid[:, k], dist, 0.0).astype(np.float32)
+        dist = np.where(valid[:, k], np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]), 0.0)
+        hi = dist.astype(np.float32)
+        out[:, k, 0] = hi
+        out[:, k, 1] = (dist - hi.astype(np.float64)).astype(np.float32)
     return out

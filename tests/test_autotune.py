@@ -1,0 +1,43 @@
+"""The blocked-erosion autotuner: its per-device cache (CPU) and a small
+tuning run whose candidates must all give the same heights (GPU)."""
+import json
+
+import pytest
+import torch
+
+
+def test_cache_round_trip_and_bad_entries(tmp_path):
+    from nixis_gb300 import autotune as A
+    p = str(tmp_path / "t.json")
+    assert A.lookup("gpuX", p) is None
+    A.store("gpuX", A.TbConfig(48, 3, 256), {"48/3/256": 1.5}, path=p)
+    A.store("gpuY", A.TbConfig(32, 5, 1024), path=p)
+    assert A.lookup("gpuX", p) == A.TbConfig(48, 3, 256)
+    assert A.lookup("gpuY", p) == A.TbConfig(32, 5, 1024)
+    with open(p) as f:
+        assert json.load(f)["gpuX"]["timings_ms"] == {"48/3/256": 1.5}
+    with open(p, "w") as f:
+        f.write("{not json")
+    assert A.lookup("gpuX", p) is None
+    with open(p, "w") as f:
+        json.dump({"gpuX": {"tile_side": "a"}}, f)
+    assert A.lookup("gpuX", p) is None
+
+
+@pytest.mark.gpu
+def test_tuning_keeps_results_and_applies_the_choice():
+    from nixis_gb300 import autotune as A, mesh, planets
+    cands = [A.TbConfig(32, 2, 256), A.TbConfig(40, 4, 512), A.TbConfig(48, 3, 1024)]
+    cfg, timings = A.tune(divisions=60, iters=9, reps=1, configs=cands, save=False)
+    assert cfg in cands and len(timings) == 3
+    assert A.current() == cfg
+    # any setting gives the bits of the plain iteration-at-a-time path
+    cache = mesh.MeshCache()
+    req = planets.PlanetRequest(seed=4, divisions=70, octaves=7, erosion_iters=13)
+    plain = planets.generate_plain(req, cache).heights
+    for c in cands:
+        bt = planets.PlanetBatch([req], cache, tb=c)
+        bt.run()
+        torch.cuda.synchronize()
+        assert torch.equal(bt.results()[0].heights, plain), c
+    A.use(A.DEFAULT)

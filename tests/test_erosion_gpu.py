@@ -1,13 +1,15 @@
 """GPU erosion (variant 3) against the oracle and the reference's goldens.
 
-* kernel arithmetic (binary32 water and sediment, height as a binary32
-  pair): bit-exact against the oracle's restatement, 1 and 50 iterations;
+* kernel arithmetic (height, water and sediment as binary32 pairs):
+  bit-exact against the oracle's restatement, 1 and 50 iterations, with
+  and without rain;
 * flow choice (sign of h_n - h_i per slot): bit-exact against the binary64
   reference on the same input heights;
 * trajectories against the binary64 reference: max|err| / max|field| <=
   ERO_TOL at 1, 10 and 50 iterations (stated tolerance);
 * the power-of-two rescale is exact (scaling inputs by 2^100 scales
-  outputs by 2^100 bit for bit) and keeps 200 iterations finite;
+  outputs by 2^100 bit for bit) and keeps 200 iterations finite and on the
+  binary64 trajectory;
 * batched planets give the same bits as each planet alone.
 """
 import numpy as np
@@ -20,7 +22,9 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-ERO_TOL = {1: 1e-6, 10: 1e-5, 30: 3e-5, 50: 3e-5}
+# max|err| / max|field| against binary64: state and edge lengths are
+# binary32 pairs (~48 bits); measured ~4e-14 through 100 iterations
+ERO_TOL = {1: 1e-10, 10: 1e-10, 30: 1e-10, 50: 1e-10, 100: 1e-10}
 
 
 def golden_case(k):
@@ -72,20 +76,20 @@ def test_kernel_arithmetic_bit_exact_and_flow_choice(k, variant):
     w0 = g[f"ero_k{k}_{variant}_w0"]
     s0 = np.zeros_like(h0)
     el = meshref.edge_lengths(pts, adj)
-    hi, lo = O.split_heights(h0)
-    st0 = np.stack([hi, lo, w0.astype(np.float32), s0.astype(np.float32)], axis=1)
+    st0 = O.pair_rows(h0, w0, s0)
     # one step + flow bits: state rows identical to the oracle's restatement
     _, _, _, _, flow, run = run_gpu(pts, adj, h0, w0, s0, 1, flow=True)
-    assert np.array_equal(run.st.cpu().numpy(), O.erosion_iteration3_f32(el, adj, st0))
+    assert np.array_equal(run.st.cpu().numpy(), O.erosion_iteration3_pair(el, adj, st0))
     # flow choice equals the binary64 reference's slope sign on the same heights
     f = flow.cpu().numpy().astype(np.int64) & 0xFFFF
     assert np.array_equal(f, flow_codes(adj, h0))
-    # 50 steps, still bit-exact
-    _, _, _, _, _, run = run_gpu(pts, adj, h0, w0, s0, 50)
-    st = st0
-    for _ in range(50):
-        st = O.erosion_iteration3_f32(el, adj, st)
-    assert np.array_equal(run.st.cpu().numpy(), st)
+    # 50 steps, still bit-exact; and 20 with rain added before each step
+    for iters, rain in ((50, 0.0), (20, 0.3 / 320)):
+        _, _, _, _, _, run = run_gpu(pts, adj, h0, w0, s0, iters, rain=rain)
+        st = st0
+        for _ in range(iters):
+            st = O.erosion_iteration3_pair(el, adj, st, rain)
+        assert np.array_equal(run.st.cpu().numpy(), st), (iters, rain)
 
 
 def rel_err(got, ref):
@@ -132,9 +136,7 @@ def test_rescale_is_exact_and_keeps_long_runs_finite():
     for x, y in zip(a[:3], b[:3]):
         assert np.array_equal(x * 2.0 ** 100, y)
     # 200 iterations pass binary32's range (water ~1e55); the scaled state
-    # stays finite and keeps the binary64 reference's magnitude.  (Over 200
-    # explosive iterations binary32 water/sediment drift from binary64 by
-    # O(10%); the stated tolerance covers 50 iterations, see the next test.)
+    # stays finite and on the binary64 reference's trajectory
     hG, wG, sG, mass, _, run = run_gpu(pts, adj, h0, w0, s0, 200, mass=True)
     assert run.scale_exponent() > 0
     assert np.isfinite(hG).all() and np.isfinite(wG).all() and np.isfinite(sG).all()
@@ -143,7 +145,7 @@ def test_rescale_is_exact_and_keeps_long_runs_finite():
         O.erosion_iteration3(pts, adj, h, w, s)
     assert np.abs(wG).max() > 1e40
     for got, want in ((hG, h), (wG, w), (sG, s)):
-        assert rel_err(got, want) <= 0.5
+        assert rel_err(got, want) <= 1e-9
     # mass sums: sum(h + s) is invariant; the per-iteration sums match the state
     m = mass.cpu().numpy()
     assert np.allclose(m[-1], [hG.sum(), wG.sum(), sG.sum()], rtol=1e-9)
@@ -151,10 +153,11 @@ def test_rescale_is_exact_and_keeps_long_runs_finite():
     assert np.abs(inv - inv[0]).max() <= 1e-6 * np.abs(m[:, :3]).max()
 
 
-def test_fifty_iterations_on_noise_terrain_within_tolerance():
+def test_hundred_iterations_on_noise_terrain_within_tolerance():
     """The single-planet erosion setting at reduced size: 12-octave fBm
-    heights rescaled to +-8000 m, water 1e-3, sediment 0, 50 iterations of
-    erosion_iteration3, every field against the binary64 oracle."""
+    heights rescaled to +-8000 m, water 1e-3, sediment 0, 100 iterations of
+    erosion_iteration3, every field against the binary64 oracle, and no
+    flow choice differing from binary64's at the end."""
     from nixis_gb300 import mesh
     m = mesh.PlanetMesh(100)
     pts, adj = m.xyz.cpu().numpy(), m.nbr.cpu().numpy()
@@ -163,12 +166,13 @@ def test_fifty_iterations_on_noise_terrain_within_tolerance():
     w = np.full(len(pts), 1e-3)
     s = np.zeros(len(pts))
     out = {}
-    hG, wG, sG, _, _, _ = run_gpu(pts, adj, h, w, s, 50)
-    for _ in range(50):
+    hG, wG, sG, _, _, _ = run_gpu(pts, adj, h, w, s, 100)
+    for _ in range(100):
         O.erosion_iteration3(pts, adj, h, w, s)
     for name, got, want in (("h", hG, h), ("w", wG, w), ("s", sG, s)):
         out[name] = rel_err(got, want)
-        assert out[name] <= ERO_TOL[50], out
+        assert out[name] <= ERO_TOL[100], out
+    assert np.array_equal(flow_codes(adj, hG), flow_codes(adj, h))
 
 
 def test_steepest_descent_matches_find_lowest():
@@ -209,7 +213,7 @@ def test_batched_planets_equal_planets_alone():
         off += n + (-n) % 256
     N = off
     hall = np.concatenate(hs).astype(np.float32)
-    st = torch.zeros((N, 4), dtype=torch.float32, device="cuda")
+    st = torch.zeros((N, 8), dtype=torch.float32, device="cuda")
     st_t = torch.zeros_like(st)
     for (b, n, iters) in descs:
         dst = st_t if iters & 1 else st
@@ -303,7 +307,7 @@ def test_temporally_blocked_long_run_rescales_like_iteration_at_a_time():
             assert res.scale_exponent > 0
             b, n = bt.vbeg[i], reqs[i].n_vertices
             x = st[b:b + n]
-            true = torch.stack([x[:, 0] + x[:, 1], x[:, 2], x[:, 3]]) * 2.0 ** res.scale_exponent
+            true = torch.stack([x[:, 0] + x[:, 1], x[:, 2] + x[:, 3], x[:, 4] + x[:, 5]]) * 2.0 ** res.scale_exponent
             assert torch.isfinite(true).all()
             vals.append(true)
         out.append(vals)

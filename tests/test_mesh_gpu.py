@@ -62,7 +62,7 @@ def test_mesh_of_the_largest_config_builds():
     assert int((nb[:12, 5] == -1).sum()) == 12
     assert int((nb[12:] < 0).sum()) == 0
     assert bool(((nb >= -1) & (nb < m.n)).all())
-    e = m.edge[12:]
+    e = m.edge[12:, :, 0]
     assert float(e.min()) > 0 and float(e.max()) < 1e-3
     # the poles exist for even k
     z = m.xyz[:, 2]
