@@ -292,12 +292,12 @@ def bench_ours(args):
     tune_t0 = time.perf_counter()
     if args.tb or args.profile:
         # profiler runs launch nothing but the batch: a given or the default setting
-        tb = autotune.TbConfig(*(int(x) for x in args.tb.split("/"))) if args.tb else autotune.DEFAULT
+        tb = autotune.parse(args.tb) if args.tb else autotune.DEFAULT
         autotune.use(tb)
-        tune_info = {"setting": f"{tb.tile_side}/{tb.rings}/{tb.threads}", "source": "given" if args.tb else "default"}
+        tune_info = {"setting": tb.label, "source": "given" if args.tb else "default"}
     else:
         tb, timings = autotune.tune(save=False)
-        tune_info = {"setting": f"{tb.tile_side}/{tb.rings}/{tb.threads}", "source": "autotuned",
+        tune_info = {"setting": tb.label, "source": "autotuned",
                      "candidates_ms": timings, "seconds": round(time.perf_counter() - tune_t0, 2)}
     if args.tune_only:
         if rank == 0:
@@ -490,13 +490,24 @@ def run_serving(n_requests, hbm_budget=120 * 2**30):
     return out
 
 
+def profile_insolation():
+    """One insolation launch (365 days x 24 hours) over divisions 474
+    (2,246,762 vertices): the case the ncu capture of the kernel uses."""
+    import torch
+    from nixis_gb300 import mesh, climate
+    m = mesh.PlanetMesh(474)
+    climate.annual_insolation(m.xyz, 1.0)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": "insolation", "vertices": m.n, "sun_positions": 365 * 24}))
+
+
 def bench_serve(args):
     from nixis_gb300 import autotune
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     tb, _ = autotune.tune(save=False)
     res = run_serving(args.serve)
-    res["blocked_erosion"] = f"{tb.tile_side}/{tb.rings}/{tb.threads}"
+    res["blocked_erosion"] = tb.label
     print(json.dumps({"serving": res}))
 
 
@@ -607,7 +618,10 @@ def bench_single(name):
     run.load(hm_t, w0)
     mass, _ = run.steps(iters, mass=True)
     ms_ = mass.cpu().numpy()
-    line["mass_sum_h_plus_s_first_last"] = [float(ms_[0, 0] + ms_[0, 2]), float(ms_[-1, 0] + ms_[-1, 2])]
+    # sum(h + s) is invariant under the update; its drift relative to the
+    # size of the sums (which grow ~2x per iteration)
+    inv0, inv1 = ms_[0, 0] + ms_[0, 2], ms_[-1, 0] + ms_[-1, 2]
+    line["mass_h_plus_s_drift_rel"] = float(abs(inv1 - inv0) / max(abs(ms_[-1, 0]), abs(ms_[-1, 2]), abs(inv0)))
     line["scale_exponent_after"] = run.scale_exponent()
     over = [i + 1 for i in range(iters) if abs(ms_[i, 1]) / n > 3.4e38]
     line["first_iteration_mean_water_above_binary32_max"] = over[0] if over else None
@@ -639,8 +653,11 @@ def main():
     ap.add_argument("--eager", action="store_true", help="launch without a CUDA graph (for profilers)")
     ap.add_argument("--profile", action="store_true", help="build the batch, run it once eagerly, exit (ncu)")
     ap.add_argument("--single", choices=["c1", "c2", "c3"], help="a single-planet configuration (supplementary line)")
-    ap.add_argument("--tb", help="blocked-erosion setting side/rings/threads instead of autotuning (e.g. 40/4/512)")
+    ap.add_argument("--tb", help="blocked-erosion setting side/rings/threads[p] instead of autotuning (e.g. 40/4/512, "
+                                 "40/4/384p with prefetch)")
     ap.add_argument("--tune-only", action="store_true", help="run the autotuner, print its table, exit")
+    ap.add_argument("--profile-insolation", action="store_true",
+                    help="one annual insolation launch on a 2,246,762-vertex sphere (ncu), exit")
     ap.add_argument("--serve", type=int, default=0, help="serving comparison on the first N stream requests, exit")
     ap.add_argument("--serve-requests", type=int, default=200, help="stream requests in the default line's serving leg")
     args = ap.parse_args()
@@ -649,6 +666,9 @@ def main():
         return
     if args.serve:
         bench_serve(args)
+        return
+    if args.profile_insolation:
+        profile_insolation()
         return
     if args.warmup < 3:
         args.warmup = 3

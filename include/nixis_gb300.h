@@ -301,12 +301,14 @@ int nx_erosion_npass(int iters);
 int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
 
 /* Temporal blocking settings (process wide, default 4 rings, 512 threads,
- * enabled): the ring count of the tilings that batches use (passes have up
- * to that many iterations), threads per block of the blocked kernel (256,
- * 512 or 1024), and whether batches with tilings use it (1) or run one
- * iteration per launch (0).  The autotuner (nixis_gb300.autotune) picks
- * rings, threads and the tile side per device. */
-int nx_erosion_tb_config(int rings, int threads, int enabled);
+ * no prefetch, enabled): the ring count of the tilings that batches use
+ * (passes have up to that many iterations), threads per block of the
+ * blocked kernel (256, 512 or 1024; with prefetch = 1, the variant that
+ * loads the next vertex's tile entries ahead, 256 or 384), and whether
+ * batches with tilings use it (1) or run one iteration per launch (0).  The
+ * autotuner (nixis_gb300.autotune) picks these and the tile side per
+ * device. */
+int nx_erosion_tb_config(int rings, int threads, int prefetch, int enabled);
 
 /* Write one planet's state back as binary64 true values (hi + lo of each
  * field times 2^K, K from the workspace's first control block).  w64_dev /

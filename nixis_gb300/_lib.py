@@ -53,7 +53,7 @@ SIGNATURES = {
     "nx_erosion_passes": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_npass": (_i32, [_i32]),
     "nx_tiling_shape": (_i32, [_i32, _i32, _i32, _p, _p, _p]),
-    "nx_erosion_tb_config": (_i32, [_i32, _i32, _i32]),
+    "nx_erosion_tb_config": (_i32, [_i32, _i32, _i32, _i32]),
     "nx_tiling_build": (_i32, [_i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p]),
 }
 

@@ -1,10 +1,12 @@
 """Autotuner for the temporally blocked erosion kernel.
 
-Three knobs set how the blocked erosion maps onto the GPU: the tile side
+Four knobs set how the blocked erosion maps onto the GPU: the tile side
 (tiles are side x side squares of a face grid; bigger tiles waste less work
 on halo rings but need more shared memory per block), the rings per pass
 (iterations done in shared memory between trips to HBM; more rings mean
-fewer trips but wider halos) and the threads per block.  ``tune`` times
+fewer trips but wider halos), the threads per block, and whether each
+thread loads its next vertex's tile entries ahead of computing the current
+one (hides their latency, costs registers and so resident threads).  ``tune`` times
 every candidate on a synthetic planet, checks that all of them give the
 same heights bit for bit (they run the same per-vertex arithmetic), keeps
 the fastest and caches it per device in a JSON file
@@ -26,7 +28,7 @@ SMEM_LIMIT = 200 * 1024          # dynamic shared memory the blocked kernel may 
 ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
 SIDES = (32, 40, 48, 56)
 RINGS = (2, 3, 4, 5)
-THREADS = (256, 512, 1024)
+THREADS = ((256, False), (512, False), (1024, False), (256, True), (384, True))
 
 
 @dataclass(frozen=True)
@@ -34,6 +36,11 @@ class TbConfig:
     tile_side: int = 40
     rings: int = 4
     threads: int = 512
+    prefetch: bool = False
+
+    @property
+    def label(self):
+        return f"{self.tile_side}/{self.rings}/{self.threads}" + ("p" if self.prefetch else "")
 
 
 DEFAULT = TbConfig()
@@ -76,7 +83,7 @@ def lookup(key, path=None):
     if not isinstance(e, dict):
         return None
     try:
-        return TbConfig(int(e["tile_side"]), int(e["rings"]), int(e["threads"]))
+        return TbConfig(int(e["tile_side"]), int(e["rings"]), int(e["threads"]), bool(e.get("prefetch", False)))
     except (KeyError, TypeError, ValueError):
         return None
 
@@ -91,6 +98,13 @@ def store(key, cfg, timings=None, path=None):
     _save(path, table)
 
 
+def parse(label):
+    """TbConfig from its label side/rings/threads, 'p' appended for prefetch."""
+    side, rings, thr = label.split("/")
+    pf = thr.endswith("p")
+    return TbConfig(int(side), int(rings), int(thr.rstrip("p")), pf)
+
+
 def current():
     """The configuration in use on the current device (tuned, cached or default)."""
     _dev.require_cuda()
@@ -102,7 +116,7 @@ def current():
 
 def apply(cfg):
     """Make cfg the blocked kernel's setting (process wide)."""
-    call("nx_erosion_tb_config", int(cfg.rings), int(cfg.threads), 1)
+    call("nx_erosion_tb_config", int(cfg.rings), int(cfg.threads), int(bool(cfg.prefetch)), 1)
 
 
 def use(cfg):
@@ -113,7 +127,7 @@ def use(cfg):
 
 
 def candidates(mesh):
-    """Every (side, rings, threads) whose tiles fit the shared-memory limit."""
+    """Every (side, rings, threads, prefetch) whose tiles fit the shared-memory limit."""
     out = []
     for side in SIDES:
         for rings in RINGS:
@@ -124,8 +138,8 @@ def candidates(mesh):
                 continue                         # more local vertices than a tile may hold
             if nm.value * ROW_SMEM > SMEM_LIMIT:
                 continue
-            for threads in THREADS:
-                out.append(TbConfig(side, rings, threads))
+            for threads, pf in THREADS:
+                out.append(TbConfig(side, rings, threads, pf))
     return out
 
 
@@ -141,7 +155,7 @@ def tune(divisions=400, iters=24, reps=3, configs=None, save=True, verbose=False
     req = _planets.PlanetRequest(seed=12345, divisions=divisions, octaves=12, erosion_iters=iters)
     configs = list(configs) if configs is not None else candidates(m)
     timings, ref, best = {}, None, None
-    configs.sort(key=lambda c: (c.tile_side, c.rings, c.threads))
+    configs.sort(key=lambda c: (c.tile_side, c.rings, c.threads, c.prefetch))
     for cfg in configs:
         for key in [k for k in m._tilings if k != (cfg.tile_side, cfg.rings)]:
             del m._tilings[key]                  # one tiling resident at a time
@@ -165,7 +179,7 @@ def tune(divisions=400, iters=24, reps=3, configs=None, save=True, verbose=False
             b.synchronize()
             ms.append(a.elapsed_time(b))
         t = min(ms)
-        timings[f"{cfg.tile_side}/{cfg.rings}/{cfg.threads}"] = round(t, 4)
+        timings[cfg.label] = round(t, 4)
         if verbose:
             print(f"autotune {cfg}: {t:.3f} ms", flush=True)
         if best is None or t < best[1]:
@@ -192,4 +206,4 @@ def ensure_tuned(**kw):
 
 
 __all__ = ["TbConfig", "DEFAULT", "current", "use", "apply", "tune", "ensure_tuned", "candidates", "lookup", "store",
-           "device_key", "cache_path"]
+           "device_key", "cache_path", "parse"]

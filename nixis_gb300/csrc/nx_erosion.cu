@@ -377,8 +377,26 @@ struct TbArgs {
 // once (a vertex's sediment is read and written only by its own thread).
 __host__ __device__ __forceinline__ size_t tb_smem_bytes(int n) { return (2 * sizeof(float4) + sizeof(float2)) * (size_t)n; }
 
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS, 1024 / THREADS) erosion_tb_kernel(TbArgs a)
+// One vertex's tile-table entries: local neighbour indices and edge pairs.
+struct TileRow {
+    uint32_t p01, p23, p45;
+    float4 d01, d23, d45;
+};
+
+__device__ __forceinline__ TileRow tile_row(const uint32_t *lnb, const float4 *led, int l)
+{
+    TileRow r;
+    r.p01 = __ldg(lnb + 3 * l); r.p23 = __ldg(lnb + 3 * l + 1); r.p45 = __ldg(lnb + 3 * l + 2);
+    r.d01 = __ldg(led + 3 * l); r.d23 = __ldg(led + 3 * l + 1); r.d45 = __ldg(led + 3 * l + 2);
+    return r;
+}
+
+// PF: software-pipelined table reads (the next vertex's entries are loaded
+// before the current vertex is computed; ~80 registers, so 768 threads per
+// SM); otherwise each vertex loads its own entries (64 registers, 1024
+// threads per SM).
+template <int THREADS, bool PF>
+__global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_tb_kernel(TbArgs a)
 {
     extern __shared__ float4 tsm4[];
     const int2 bm = a.blk_map[blockIdx.x];
@@ -436,9 +454,18 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) erosion_tb_kernel(TbA
         const float4 *cur = (mi & 1) ? buf1 : buf0;
         float4 *nxt = (mi & 1) ? buf0 : buf1;
         const bool more = mi + 1 < len;          // rain for the next iteration in the pass
-        for (int l = threadIdx.x; l < C; l += blockDim.x) {
-            const uint32_t p01 = __ldg(lnb + 3 * l), p23 = __ldg(lnb + 3 * l + 1), p45 = __ldg(lnb + 3 * l + 2);
-            const float4 d01 = __ldg(led + 3 * l), d23 = __ldg(led + 3 * l + 1), d45 = __ldg(led + 3 * l + 2);
+        TileRow nextrow;
+        if (PF && (int)threadIdx.x < C) nextrow = tile_row(lnb, led, threadIdx.x);
+        for (int l = threadIdx.x; l < C; l += THREADS) {
+            TileRow row;
+            if (PF) {
+                row = nextrow;
+                if (l + THREADS < C) nextrow = tile_row(lnb, led, l + THREADS);
+            } else {
+                row = tile_row(lnb, led, l);
+            }
+            const uint32_t p01 = row.p01, p23 = row.p23, p45 = row.p45;
+            const float4 d01 = row.d01, d23 = row.d23, d45 = row.d45;
             const float4 me = cur[l];
             const float2 ms = sed[l];
             float2 A = make_float2(0.0f, me.z), L = make_float2(0.0f, me.w);
@@ -746,25 +773,33 @@ static int64_t planet_blocks(const nx_erosion_planet &P) { return (P.n + BLOCK -
 // share it) and a switch for comparisons.
 static int g_tb_rings = 4;
 static int g_tb_threads = 512;
+static bool g_tb_prefetch = false;
 static bool g_tb_enabled = true;
 
-NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int enabled)
+NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int prefetch, int enabled)
 {
     if (rings < 1 || rings > 8) return nx::fail(NX_EINVAL, "nx_erosion_tb_config: rings must be in [1, 8]");
-    if (threads != 256 && threads != 512 && threads != 1024)
-        return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads must be 256, 512 or 1024");
+    const bool ok = prefetch ? (threads == 256 || threads == 384) : (threads == 256 || threads == 512 || threads == 1024);
+    if (!ok)
+        return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads must be 256, 512 or 1024 (256 or 384 with prefetch)");
     g_tb_rings = rings;
     g_tb_threads = threads;
+    g_tb_prefetch = prefetch != 0;
     g_tb_enabled = enabled != 0;
     return NX_OK;
 }
 
 static cudaError_t launch_tb(int64_t grid, size_t smem, cudaStream_t s, const TbArgs &ta)
 {
-    switch (g_tb_threads) {
-    case 256: erosion_tb_kernel<256><<<(unsigned)grid, 256, smem, s>>>(ta); break;
-    case 1024: erosion_tb_kernel<1024><<<(unsigned)grid, 1024, smem, s>>>(ta); break;
-    default: erosion_tb_kernel<512><<<(unsigned)grid, 512, smem, s>>>(ta); break;
+    if (g_tb_prefetch) {
+        if (g_tb_threads == 256) erosion_tb_kernel<256, true><<<(unsigned)grid, 256, smem, s>>>(ta);
+        else erosion_tb_kernel<384, true><<<(unsigned)grid, 384, smem, s>>>(ta);
+    } else {
+        switch (g_tb_threads) {
+        case 256: erosion_tb_kernel<256, false><<<(unsigned)grid, 256, smem, s>>>(ta); break;
+        case 1024: erosion_tb_kernel<1024, false><<<(unsigned)grid, 1024, smem, s>>>(ta); break;
+        default: erosion_tb_kernel<512, false><<<(unsigned)grid, 512, smem, s>>>(ta); break;
+        }
     }
     return cudaGetLastError();
 }
@@ -779,9 +814,11 @@ static int tb_prepare()
     if (dev < 0 || dev >= 64) return nx::fail(NX_EINVAL, "erosion: device id %d out of range", dev);
     std::lock_guard<std::mutex> lk(mu);
     if (!done[dev]) {
-        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<384, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         done[dev] = true;
     }
     return NX_OK;

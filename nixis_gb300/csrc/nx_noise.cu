@@ -237,6 +237,83 @@ __device__ __forceinline__ void decide(T xins, T yins, T zins, T in_sum, Cmp<T, 
     }
 }
 
+
+// The same decision for the binary32 path without data-dependent branches
+// (lanes of a warp sit in different regions at high octaves).  Regions 0
+// and 1 are mirror images: region 1's comparisons are region 0's with both
+// sides negated (exact), its lattice-point codes are 7 - region 0's and its
+// offsets are 1 - region 0's; both tetrahedra and the octahedron are
+// evaluated and the region selects.  Every comparison evaluated records its
+// margin (a superset of those the branching form records), so a lane keeps
+// its binary32 decision only when all of them clear the margin.
+__device__ __forceinline__ void decide_sel(float x, float y, float z, float in_sum, Cmp<float, true> &C, Decision &D)
+{
+    const bool r0 = C.le(in_sum, 1.0f);
+    const bool r1 = !r0 && C.ge(in_sum, 2.0f);
+    // tetrahedron (region 0 form; s = -1 mirrors the comparisons for region 1)
+    const float s = r1 ? -1.0f : 1.0f;
+    const bool xy = C.ge(s * x, s * y);
+    const bool zb = C.gt(s * z, s * y);
+    const bool za = C.gt(s * z, s * x);
+    const bool repb = xy && zb, repa = !xy && za;
+    const float as = repa ? z : x, bs = repb ? z : y;
+    const int ap = repa ? 4 : 1, bp = repb ? 4 : 2;
+    const float wins = (r1 ? 3.0f : 1.0f) - in_sum;
+    const bool n1 = C.gt(s * wins, s * as);
+    const bool n2 = C.gt(s * wins, s * bs);
+    const bool near = n1 || n2;
+    const int cn = C.gt(s * bs, s * as) ? bp : ap;
+    const int cf = ap | bp;
+    const bool cn1 = (cn & 1) != 0, cn2 = (cn & 2) != 0, cn4 = (cn & 4) != 0;
+    float t0x = near ? (cn1 ? 1.f : -1.f) : ((cf & 1) ? 1.f : 0.f);
+    float t1x = near ? (cn1 ? 1.f : 0.f) : ((cf & 1) ? 1.f : -1.f);
+    float t0y = near ? (cn2 ? 1.f : (cn1 ? -1.f : 0.f)) : ((cf & 2) ? 1.f : 0.f);
+    float t1y = near ? (cn2 ? 1.f : (cn1 ? 0.f : -1.f)) : ((cf & 2) ? 1.f : -1.f);
+    float t0z = near ? (cn4 ? 1.f : 0.f) : ((cf & 4) ? 1.f : 0.f);
+    float t1z = near ? (cn4 ? 1.f : -1.f) : ((cf & 4) ? 1.f : -1.f);
+    if (r1) {
+        t0x = 1.f - t0x; t1x = 1.f - t1x; t0y = 1.f - t0y;
+        t1y = 1.f - t1y; t0z = 1.f - t0z; t1z = 1.f - t1z;
+    }
+    // octahedron
+    const float p1 = x + y, p2 = x + z, p3 = y + z;
+    const bool g1 = C.gt(p1, 1.0f), g2 = C.gt(p2, 1.0f), t3 = C.gt(p3, 1.0f);
+    const float oas = g1 ? p1 - 1.0f : 1.0f - p1;
+    const float obs = g2 ? p2 - 1.0f : 1.0f - p2;
+    const float score = t3 ? p3 - 1.0f : 1.0f - p3;
+    const bool ale = C.le(oas, obs);
+    const bool a_lt = C.lt(oas, score), b_lt = C.lt(obs, score);
+    const bool swa = ale && a_lt, swb = !ale && b_lt;
+    const int oap = swa ? (t3 ? 6 : 1) : (g1 ? 3 : 4);
+    const int obp = swb ? (t3 ? 6 : 1) : (g2 ? 5 : 2);
+    const bool af = swa ? t3 : g1, bf = swb ? t3 : g2;
+    float o0x, o0y, o0z, o1x, o1y, o1z;
+    if (af == bf) {
+        const int c = af ? (oap & obp) : (oap | obp);
+        const float b = af ? 1.f : 0.f;
+        o0x = b; o0y = b; o0z = b;
+        // af: the single bit of c picks the axis that gets 2; otherwise the
+        // first axis whose bit is clear gets -1 and the others 1
+        const bool c1 = (c & 1) != 0, c2 = (c & 2) != 0;
+        const bool ax = af ? c1 : !c1, ay = af ? (!c1 && c2) : (c1 && !c2);
+        const bool az = !ax && !ay;
+        const float hit = af ? 2.f : -1.f, miss = af ? 0.f : 1.f;
+        o1x = ax ? hit : miss; o1y = ay ? hit : miss; o1z = az ? hit : miss;
+    } else {
+        const int c1 = af ? oap : obp, c2 = af ? obp : oap;
+        const bool bx = (c1 & 1) == 0, by = !bx && (c1 & 2) == 0;
+        const bool bz = !bx && !by;
+        o0x = bx ? -1.f : 1.f; o0y = by ? -1.f : 1.f; o0z = bz ? -1.f : 1.f;
+        const bool qx = (c2 & 1) != 0, qy = !qx && (c2 & 2) != 0;
+        const bool qz = !qx && !qy;
+        o1x = qx ? 2.f : 0.f; o1y = qy ? 2.f : 0.f; o1z = qz ? 2.f : 0.f;
+    }
+    const bool tet = r0 || r1;
+    D.region = r0 ? 0 : (r1 ? 1 : 2);
+    D.e0x = tet ? t0x : o0x; D.e0y = tet ? t0y : o0y; D.e0z = tet ? t0z : o0z;
+    D.e1x = tet ? t1x : o1x; D.e1y = tet ? t1y : o1y; D.e1z = tet ? t1z : o1z;
+}
+
 // opensimplex.py:18-21 in binary64
 __device__ __forceinline__ long long fastfloor64(double x)
 {
@@ -303,7 +380,7 @@ __device__ __forceinline__ bool decide_f32(float xh, float xl, float yh, float y
     Cmp<float, true> C;
     C.m = fminf(fminf(fminf(xins, 1.0f - xins), fminf(yins, 1.0f - yins)), fminf(zins, 1.0f - zins));
     float in_sum = (xins + yins) + zins;
-    decide<float, true>(xins, yins, zins, in_sum, C, c.D);
+    decide_sel(xins, yins, zins, in_sum, C, c.D);
     return C.m >= TAU && big < PMAX;
 }
 

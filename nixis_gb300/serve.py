@@ -18,10 +18,11 @@ frees up:
 
 A newly admitted planet's fBm, rescale and initial state run on a side
 stream while the main stream keeps eroding the others; it joins the next
-tick.  A planet that finishes erosion gets its heights (main stream), then
-insolation and the copy of its results to pinned host memory on the side
-stream.  Results are the same bits as the planet generated alone
-(planets.generate_plain).
+tick.  Its insolation (which needs only the vertices) starts at admission on
+a third stream, beside its erosion.  A planet that finishes erosion gets
+its heights (main stream), then the copy of its results to page-locked host
+memory on the side stream.  Results are the same bits as the planet
+generated alone (planets.generate_plain).
 
 ``serve_plain`` is the comparator: the same stream of requests handled one
 at a time with the plain per-planet path.
@@ -152,6 +153,7 @@ class Ticket:
     host_i: torch.Tensor = None
     done_event: object = None
     ready_event: object = None
+    inso_event: object = None
     stage: str = "queued"
     minmax: torch.Tensor = None
 
@@ -160,8 +162,16 @@ class Ticket:
         return None if self.finished is None else self.finished - self.arrival
 
 
+def _pinned(a):
+    """A copy of numpy array a in page-locked memory from torch's caching
+    host allocator (reused once freed, instead of a fresh cudaHostAlloc)."""
+    t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0]).dtype, pin_memory=True)
+    t.numpy()[...] = a
+    return t
+
+
 def _descs_tensor(arr):
-    return torch.from_numpy(np.frombuffer(bytes(arr), np.uint8).copy()).pin_memory()
+    return _pinned(np.frombuffer(bytes(arr), np.uint8))
 
 
 class ServeEngine:
@@ -192,6 +202,7 @@ class ServeEngine:
         self.meshes = ResidentMeshes(self.budget - R * ROW_BYTES - self.ws.numel(), self.tb)
         self.main = torch.cuda.Stream()
         self.side = torch.cuda.Stream()
+        self.inso_stream = torch.cuda.Stream()
         self.desc_dev = torch.empty(slots * ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device=dev)
         self.chunk = int(lib().nx_fbm_chunk_size())
         self.tick = 0
@@ -260,10 +271,10 @@ class ServeEngine:
         for j, t in enumerate(new):
             tabs[j, 0], tabs[j, 1] = _osx.init(t.request.seed)
         with torch.cuda.stream(self.side):
-            tab_dev = torch.from_numpy(tabs).pin_memory().to("cuda", non_blocking=True)
+            tab_dev = _pinned(tabs).to("cuda", non_blocking=True)
             mm = torch.tensor([[-1, 0]] * n, dtype=torch.int64).to(torch.int32)
             mm[:, 0] = -1
-            mm_dev = mm.pin_memory().to("cuda", non_blocking=True)
+            mm_dev = _pinned(mm.numpy()).to("cuda", non_blocking=True)
             for j, t in enumerate(new):
                 r = t.request
                 f = fb[j]
@@ -299,20 +310,39 @@ class ServeEngine:
                      ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg),
                      ctypes.c_void_p(self.st_tmp.data_ptr() + 32 * t.vbeg), s)
                 t._e_single = (e, e_dev)
-                t.host_h = torch.empty(t.mesh.n, dtype=torch.float32).pin_memory()
+                t.host_h = torch.empty(t.mesh.n, dtype=torch.float32, pin_memory=True)
                 if r.insolation:
-                    t.host_i = torch.empty(t.mesh.n, dtype=torch.float32).pin_memory()
+                    t.host_i = torch.empty(t.mesh.n, dtype=torch.float32, pin_memory=True)
                 ev = torch.cuda.Event()
                 ev.record(self.side)
                 t.ready_event = ev
                 t._keep = (tab_dev, mm_dev, fb_dev, fb)
+                if r.insolation:
+                    self._insolation(t, ev)
                 if r.erosion_iters == 0:
                     t.stage = "output"
                 else:
                     t.stage = "waiting"
 
+    def _insolation(self, t, after):
+        """Insolation depends on the vertices only: it runs on its own stream
+        as soon as the planet is admitted, beside its erosion."""
+        r = t.request
+        n = t.mesh.n
+        self.inso_stream.wait_event(after)
+        with torch.cuda.stream(self.inso_stream):
+            tab, nre, pairs, ntilt, scale = self._schedule_table(r)
+            out = self.inso[t.vbeg:t.vbeg + n]
+            call("nx_insolation", _dev.ptr(t.mesh.xyz), n, float(r.radius), _dev.ptr(tab), nre, pairs, ntilt,
+                 _dev.ptr(out), 0, _dev.stream_handle(self.inso_stream))
+            out.mul_(scale)
+            t.host_i.copy_(out, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(self.inso_stream)
+        t.inso_event = ev
+
     def _output(self, t, after_main):
-        """Heights (+ insolation) and the copy to the host for a finished planet."""
+        """Heights and their copy to the host for a finished planet."""
         r = t.request
         e, e_dev = t._e_single
         ws = _dev.ptr(self.ws)
@@ -327,16 +357,10 @@ class ServeEngine:
         ev = torch.cuda.Event()
         ev.record(stream)
         self.side.wait_event(ev)
-        ss = _dev.stream_handle(self.side)
         with torch.cuda.stream(self.side):
             n = t.mesh.n
-            if r.insolation:
-                tab, nre, pairs, ntilt, scale = self._schedule_table(r)
-                out = self.inso[t.vbeg:t.vbeg + n]
-                call("nx_insolation", _dev.ptr(t.mesh.xyz), n, float(r.radius), _dev.ptr(tab), nre, pairs, ntilt,
-                     _dev.ptr(out), 0, ss)
-                out.mul_(scale)
-                t.host_i.copy_(out, non_blocking=True)
+            if t.inso_event is not None:
+                self.side.wait_event(t.inso_event)
             t.host_h.copy_(self.heights[t.vbeg:t.vbeg + n], non_blocking=True)
             done = torch.cuda.Event()
             done.record(self.side)
@@ -419,8 +443,11 @@ class ServeEngine:
         for t in self.active:
             if t.stage == "copying" and t.done_event.query():
                 t.finished = time.perf_counter()
-                t.heights = t.host_h.numpy()
-                t.insolation = t.host_i.numpy() if t.host_i is not None else None
+                # results move to ordinary host memory; the page-locked
+                # buffers go back to the caching allocator for later planets
+                t.heights = t.host_h.numpy().copy()
+                t.insolation = t.host_i.numpy().copy() if t.host_i is not None else None
+                t.host_h = t.host_i = None
                 self.arena.release(t.vbeg, t.mesh.n)
                 self.free_slots.append(t.slot)
                 self.meshes.release(t.request.divisions)
