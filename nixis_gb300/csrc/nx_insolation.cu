@@ -18,10 +18,7 @@
 // (| |v|^2 - r^2 | > 1e-12 r^2) take the reference's general formula.
 //
 // Sums per tilt are binary32 (<= 360 terms); the running total over tilts
-// is compensated (Kahan) so the result tracks the binary64 sum.  With a
-// fixed count of rotation pairs (HP, 12 for hourly sun positions), two pairs
-// are evaluated at once in paired binary32 lanes (FFMA2/FMUL2/FADD2) and
-// summed as two partial sums per tilt.
+// is compensated (Kahan) so the result tracks the binary64 sum.
 #include "nx_common.cuh"
 
 namespace nx {
@@ -70,16 +67,10 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
     float tot = 0.0f, comp = 0.0f;          // Kahan over tilts
     const int nr = HP > 0 ? HP : a.n_rot;
     if (on_sphere) {
-        static_assert(HP % 2 == 0, "rotation pairs come two at a time");
-        constexpr int H2 = HP > 0 ? HP / 2 : 1;
-        float2 rc[H2], rs[H2];                   // (cos, cos), (sin, sin) of pairs 2h, 2h+1
+        float2 rt[HP > 0 ? HP : 1];
         if (HP > 0) {
 #pragma unroll
-            for (int h = 0; h < H2; ++h) {
-                const float2 p = a.rot[2 * h], q = a.rot[2 * h + 1];
-                rc[h] = make_float2(p.x, q.x);
-                rs[h] = make_float2(p.y, q.y);
-            }
+            for (int h = 0; h < (HP > 0 ? HP : 1); ++h) rt[h] = a.rot[h];
         }
         for (int d = 0; d < a.n_tilt; ++d) {
             const float2 t = a.tilt[d];
@@ -88,14 +79,11 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
             if (a.pairs) {
                 const float aC = fabsf(C);
                 if (HP > 0) {
-                    const float2 A2 = make_float2(A, A), B2 = make_float2(B, B);
-                    float2 s2 = make_float2(0.0f, 0.0f);
 #pragma unroll
-                    for (int h = 0; h < H2; ++h) {
-                        const float2 u = __ffma2_rn(A2, rc[h], __fmul2_rn(B2, rs[h]));
-                        s2 = __fadd2_rn(s2, make_float2(fmaxf(aC, fabsf(u.x)), fmaxf(aC, fabsf(u.y))));
+                    for (int h = 0; h < (HP > 0 ? HP : 1); ++h) {
+                        float u = fmaf(A, rt[h].x, B * rt[h].y);
+                        s += fmaxf(aC, fabsf(u));
                     }
-                    s = s2.x + s2.y;
                 } else {
                     for (int h = 0; h < nr; ++h) {
                         float2 q = a.rot[h];
