@@ -30,8 +30,9 @@ sys.path.insert(0, ROOT)
 N_PLANETS = 64
 METRIC = "batched planets/s (64 planets, divisions 100-800, 4-12 octaves, 0-100 erosion iterations)"
 UNIT = "planets/s"
-SAMPLE_ALG_BYTES = 96      # erosion: algorithmic bytes per vertex-iteration (state in 24 + out 24: h, w, s as
-                           # binary32 pairs; neighbour ids 24, edge lengths 24)
+SAMPLE_ALG_BYTES = 72      # erosion: algorithmic bytes per vertex-iteration, the binary32 model (state 12 in +
+                           # 12 out, neighbour ids 24, edge lengths 24); the pair state and edge lengths used
+                           # here would count 120
 
 
 def workload(name="batch64"):
