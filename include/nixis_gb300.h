@@ -342,6 +342,54 @@ int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_eros
                              int nplanets, const float *st_dev, const void *workspace, float *out_dev,
                              void *stream);
 
+/* Latitude-table insolation (climate.py:503-597).  Tables for n_tilts
+ * tilts (degrees, device float64[n_tilts]) into tables_dev
+ * float[n_tilts * 181]: entry i is latitude i for i <= 90, i - 181 above,
+ * each the binary32 running sum over 360 rotations of one degree from -180
+ * (calc_insolation_slice). */
+int nx_insolation_slices(const double *tilts_dev, int n_tilts, double radius, float *tables_dev, void *stream);
+
+/* Every vertex's insolation interpolated between the entries of floor(lat)
+ * and ceil(lat) (interpolate_insolation), summed in binary32 over n_tables
+ * tables in order (calc_yearly_insolation: 360 tables); accumulate = 1 adds
+ * to out_dev. */
+int nx_interpolate_insolation(const double *xyz_dev, int64_t n, double radius, const float *tables_dev, int n_tables,
+                              float *out_dev, int accumulate, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Height shaping (nixis.py:332-364), binary64                         */
+/* ------------------------------------------------------------------ */
+
+/* Workspace bytes for the shaping calls on n values (16-byte aligned). */
+size_t nx_shape_workspace_size(int64_t n);
+
+/* util.rescale (util.py:110-176): form 0 plain min/max normalisation to
+ * [lower, upper]; 1 with mid (each side of mid mapped separately); 2 mode
+ * 'lower' (only x <= mid); 3 mode 'upper' (only x >= mid).  has_umin /
+ * has_umax: u_min / u_max widen the input range.  Min and max are found on
+ * the device (all reads finish before the first write: out_dev may equal
+ * x_dev). */
+int nx_rescale(const double *x_dev, int64_t n, double lower, double upper, double mid, int form, double u_min,
+               int has_umin, double u_max, int has_umax, double *out_dev, void *ws, size_t ws_bytes, void *stream);
+
+/* util.power_rescale (util.py:179-250): mode 1 rescales the values where
+ * mask_dev is non-zero, 0 where it is zero, -1 none (copy); the masked range
+ * is the reference's running min/max update. */
+int nx_power_rescale(const double *x_dev, int64_t n, const uint8_t *mask_dev, int mode, double power, double *out_dev,
+                     void *ws, size_t ws_bytes, void *stream);
+
+/* terrain.make_bool_elevation_mask (terrain.py:61-72): mask = h <= level. */
+int nx_elevation_mask(const double *h_dev, int64_t n, double level, uint8_t *mask_dev, void *stream);
+
+/* nixis.py:332-364 on the device: rescale to [min_alt, max_alt], ocean level
+ * = util.find_percent_val(min, max, ocean_percent), ocean mask, power_rescale
+ * (ocean, 0.5) then (land, 2.0), minus the level, rescale about 0.
+ * out_dev: the heights; tmp_dev: n doubles of scratch; mask_dev: the ocean
+ * mask; level_dev (optional, device double): the level. */
+int nx_shape_heights(const double *h_dev, int64_t n, double min_alt, double max_alt, double ocean_percent,
+                     double *out_dev, double *tmp_dev, uint8_t *mask_dev, double *level_dev, void *ws,
+                     size_t ws_bytes, void *stream);
+
 /* Erosion for callers that cannot allocate device memory.  No counterpart
  * in the reference (whose erosion is host code).  Some callers run inside
  * a host application's own device-memory pool, where a direct cudaMalloc

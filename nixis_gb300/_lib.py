@@ -52,6 +52,13 @@ SIGNATURES = {
     "nx_erosion_ticks": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_passes": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_npass": (_i32, [_i32]),
+    "nx_shape_workspace_size": (ctypes.c_size_t, [_i64]),
+    "nx_insolation_slices": (_i32, [_p, _i32, _d, _p, _p]),
+    "nx_interpolate_insolation": (_i32, [_p, _i64, _d, _p, _i32, _p, _i32, _p]),
+    "nx_rescale": (_i32, [_p, _i64, _d, _d, _d, _i32, _d, _i32, _d, _i32, _p, _p, ctypes.c_size_t, _p]),
+    "nx_power_rescale": (_i32, [_p, _i64, _p, _i32, _d, _p, _p, ctypes.c_size_t, _p]),
+    "nx_elevation_mask": (_i32, [_p, _i64, _d, _p, _p]),
+    "nx_shape_heights": (_i32, [_p, _i64, _d, _d, _d, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "nx_tiling_shape": (_i32, [_i32, _i32, _i32, _p, _p, _p]),
     "nx_erosion_tb_config": (_i32, [_i32, _i32, _i32, _i32]),
     "nx_tiling_build": (_i32, [_i32, _i32, _i32, _p, _p, _p, _p, _p, _p, _p, _p]),

@@ -1,9 +1,12 @@
 """Drop-in for the insolation part of the reference's climate module
-(climate.py:167-201, 415-500) and the fused annual accumulation.
+(climate.py:167-201, 415-597) and the fused annual accumulation.
 
 ``sample_insolation`` keeps the reference's in-place float32 ``arr +=``;
 ``insolation_sum`` evaluates any (tilt x rotation) schedule in one kernel;
-``annual_insolation`` is the year of days x hourly sun positions.
+``annual_insolation`` is the year of days x hourly sun positions.  The
+latitude-table path (``calc_insolation_slice``, ``interpolate_insolation``,
+``calc_daily_insolation``, ``calc_yearly_insolation``) builds its tables and
+interpolates on the GPU; tables are cached per (radius, tilts).
 """
 import ctypes
 import math
@@ -115,3 +118,76 @@ def annual_insolation(verts, radius, axial_tilt=23.44, year_length=365, days=365
     if mean_wm2:
         s.mul_(SOLAR_CONSTANT / (days * hours))
     return s
+
+
+_tables = {}
+
+
+def _slice_tables(radius, tilts):
+    """Device float32 (len(tilts), 181) latitude tables (cached)."""
+    key = (float(radius), tuple(float(t) for t in tilts))
+    t = _tables.get(key)
+    if t is None:
+        _dev.require_cuda()
+        td = torch.tensor(list(key[1]), dtype=torch.float64, device="cuda")
+        t = torch.empty((len(tilts), 181), dtype=torch.float32, device="cuda")
+        call("nx_insolation_slices", _dev.ptr(td), len(tilts), float(radius), _dev.ptr(t), _dev.stream_handle())
+        if len(_tables) > 64:
+            _tables.clear()
+        _tables[key] = t
+    return t
+
+
+def calc_insolation_slice(radius, tilt):
+    """climate.calc_insolation_slice (climate.py:503-533): float32 (181,),
+    entry i the summed insolation of latitude i (i <= 90) or i - 181, over
+    360 rotations of one degree."""
+    return _slice_tables(radius, [tilt])[0].cpu().numpy()
+
+
+def interpolate_insolation(verts, lookup_table, insolation, radius):
+    """climate.interpolate_insolation (climate.py:551-577): insolation[v] =
+    the table interpolated at the vertex's latitude, in place (numpy float32
+    or a float32 CUDA tensor)."""
+    xyz = _dev.to_device(verts, np.float64, name="verts")
+    _dev.check_vertices(xyz)
+    n = xyz.shape[0]
+    tab = _dev.to_device(lookup_table, np.float32, (181,), "lookup_table")
+    host = _dev.is_host(insolation)
+    out = torch.empty(n, dtype=torch.float32, device="cuda") if host else insolation
+    if not host and (out.dtype != torch.float32 or out.shape != (n,)):
+        raise ValueError("insolation must be a float32 array of shape (N,)")
+    call("nx_interpolate_insolation", _dev.ptr(xyz), n, float(radius), _dev.ptr(tab), 1, _dev.ptr(out), 0,
+         _dev.stream_handle())
+    if host:
+        insolation[...] = out.cpu().numpy()
+
+
+def calc_daily_insolation(verts, altitudes, radius, tilt):
+    """climate.calc_daily_insolation (climate.py:536-548): a new float32
+    array (altitudes do not enter the result, as in the reference)."""
+    host = _dev.is_host(verts)
+    xyz = _dev.to_device(verts, np.float64, name="verts")
+    _dev.check_vertices(xyz)
+    out = torch.empty(xyz.shape[0], dtype=torch.float32, device="cuda")
+    tab = _slice_tables(radius, [tilt])
+    call("nx_interpolate_insolation", _dev.ptr(xyz), xyz.shape[0], float(radius), _dev.ptr(tab), 1, _dev.ptr(out), 0,
+         _dev.stream_handle())
+    return out.cpu().numpy() if host else out
+
+
+def calc_yearly_insolation(points, height, radius, axial_tilt, snapshot=False):
+    """climate.calc_yearly_insolation (climate.py:579-597): the daily tables
+    of 360 orbital degrees (tilt calculate_seasonal_tilt(axial_tilt, x)),
+    interpolated at every vertex and summed in binary32; a new float32 array."""
+    if snapshot:
+        raise NotImplementedError("insolation snapshots (PNG export) are not provided by nixis_gb300")
+    host = _dev.is_host(points)
+    xyz = _dev.to_device(points, np.float64, name="points")
+    _dev.check_vertices(xyz)
+    n = xyz.shape[0]
+    tab = _slice_tables(radius, [calculate_seasonal_tilt(axial_tilt, x) for x in range(360)])
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    call("nx_interpolate_insolation", _dev.ptr(xyz), n, float(radius), _dev.ptr(tab), 360, _dev.ptr(out), 0,
+         _dev.stream_handle())
+    return out.cpu().numpy() if host else out

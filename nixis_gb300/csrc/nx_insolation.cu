@@ -152,6 +152,81 @@ __global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const
     }
 }
 
+// ---------------------------------------------------------------------------
+// Latitude-table path (climate.py:503-597): per tilt, a table of 181
+// latitudes (entry i = latitude i for i <= 90, i - 181 above), each the
+// binary32 running sum over 360 rotations of 1 degree from -180 of the
+// reference's term at (lat, lon 0) (calc_insolation_slice, with
+// sample_insolation's formula in binary64); then per vertex a linear
+// interpolation between floor(lat) and ceil(lat), summed in binary32 over
+// the tables (calc_yearly_insolation adds 360 daily tables).
+
+constexpr double DEG = 3.141592653589793 / 180;
+
+__device__ __forceinline__ double ref_term(double x, double y, double z, double radius, double cr, double sr,
+                                           double ct, double st)
+{
+    // climate.py:423-442 with util.xyz2latlon (util.py:60-75)
+    const double rx = x * cr - y * sr;
+    const double ry = x * sr + y * cr;
+    const double rz = z;
+    const double tx = rx * ct + rz * st;
+    const double ty = ry;
+    const double tz = rz * ct - rx * st;
+    const double q = fmin(fmax(tz / radius, -1.0), 1.0);
+    const double lat = asin(q) * (180.0 / 3.141592653589793);
+    const double lon = atan2(ty, tx) * (180.0 / 3.141592653589793);
+    const double a = fmax(cos(fabs(lat) * 3.141592653589793 / 180), 0.0);
+    const double b = fmax(cos(lon * 3.141592653589793 / 180), 0.0);
+    return a * b;
+}
+
+// one block per table, one thread per latitude entry
+__global__ void __launch_bounds__(192) slice_kernel(const double *__restrict__ tilts, int n_tilts, double radius,
+                                                    float *__restrict__ tables)
+{
+    const int d = blockIdx.x, i = threadIdx.x;
+    if (d >= n_tilts || i >= 181) return;
+    const double lat = (double)(i <= 90 ? i : i - 181);
+    // util.latlon2xyz (util.py:79-88) at lon 0
+    const double x = radius * cos(lat * DEG) * cos(0.0 * DEG);
+    const double y = radius * cos(lat * DEG) * sin(0.0 * DEG);
+    const double z = radius * sin(lat * DEG);
+    const double tilt = tilts[d];
+    const double ct = cos(tilt * 3.141592653589793 / 180), st = sin(tilt * 3.141592653589793 / 180);
+    float acc = 0.0f;
+    double rotation = -180.0;
+    for (int j = 0; j < 360; ++j) {
+        const double cr = cos(rotation * 3.141592653589793 / 180), sr = sin(rotation * 3.141592653589793 / 180);
+        acc = (float)((double)acc + ref_term(x, y, z, radius, cr, sr, ct, st));
+        rotation += 1.0;
+    }
+    tables[181 * d + i] = acc;
+}
+
+// climate.py:551-577 per vertex and table, summed in binary32 over tables
+__global__ void __launch_bounds__(256) interp_kernel(const double *__restrict__ xyz, int64_t n, double radius,
+                                                     const float *__restrict__ tables, int n_tables,
+                                                     float *__restrict__ out, int accumulate)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const double q = fmin(fmax(xyz[3 * v + 2] / radius, -1.0), 1.0);
+        const double lat = asin(q) * (180.0 / 3.141592653589793);
+        const double fl = floor(lat), cl = ceil(lat);
+        const int lower = (int)fl, upper = (int)cl;
+        const int il = (lower + 181) % 181, iu = (upper + 181) % 181;
+        const double frac = lat - fl, span = (double)(upper - lower);
+        float acc = accumulate ? out[v] : 0.0f;
+        for (int d = 0; d < n_tables; ++d) {
+            const float tl = __ldg(tables + 181 * d + il), tu = __ldg(tables + 181 * d + iu);
+            float val = tl;
+            if (lower != upper) val = (float)((double)tl + frac * ((double)__fsub_rn(tu, tl) / span));
+            acc = (n_tables == 1 && !accumulate) ? val : __fadd_rn(acc, val);
+        }
+        out[v] = acc;
+    }
+}
+
 int grid_for(int64_t n)
 {
     int64_t g = (n + 255) / 256;
@@ -262,6 +337,35 @@ NX_EXPORT int nx_insolation_batch(const nx_inso_planet *planets_dev, const nx_in
     else
         insolation_batch_kernel<0><<<grid, 256, 0, s>>>(a, planets_dev, nplanets, total);
     NX_CHECK_LAUNCH("insolation_batch_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+// Daily latitude tables for n_tilts tilts (degrees, device array):
+// tables_dev float[n_tilts * 181].
+NX_EXPORT int nx_insolation_slices(const double *tilts_dev, int n_tilts, double radius, float *tables_dev,
+                                   void *stream)
+{
+    if (n_tilts <= 0 || !tilts_dev || !tables_dev || !(radius > 0.0))
+        return nx::fail(NX_EINVAL, "nx_insolation_slices: bad arguments");
+    slice_kernel<<<n_tilts, 192, 0, (cudaStream_t)stream>>>(tilts_dev, n_tilts, radius, tables_dev);
+    NX_CHECK_LAUNCH("slice_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+// Interpolated insolation of every vertex from n_tables tables, summed in
+// binary32 in table order (accumulate = 1 adds to out_dev; with one table
+// and accumulate = 0 the value is written as interpolate_insolation does).
+NX_EXPORT int nx_interpolate_insolation(const double *xyz_dev, int64_t n, double radius, const float *tables_dev,
+                                        int n_tables, float *out_dev, int accumulate, void *stream)
+{
+    if (n < 0 || n_tables <= 0 || (n > 0 && (!xyz_dev || !tables_dev || !out_dev)) || !(radius > 0.0))
+        return nx::fail(NX_EINVAL, "nx_interpolate_insolation: bad arguments");
+    if (n == 0) return NX_OK;
+    interp_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(xyz_dev, n, radius, tables_dev, n_tables, out_dev,
+                                                                 accumulate);
+    NX_CHECK_LAUNCH("interp_kernel");
     nx::note_launch(1);
     return NX_OK;
 }

@@ -85,3 +85,10 @@ def sample_octaves(verts, elevations, perm, pgi, n_octaves=1, n_init_roughness=1
         return elevations
     fbm(verts, perm, pgi, scale, strength, world_radius, out=elevations, accumulate=True)
     return elevations
+
+
+def make_bool_elevation_mask(height, mask_elevation):
+    """terrain.make_bool_elevation_mask (terrain.py:61-72): height <=
+    mask_elevation, on the GPU (see util.make_bool_elevation_mask)."""
+    from .util import make_bool_elevation_mask as _mask
+    return _mask(height, mask_elevation)

@@ -682,6 +682,70 @@ NXO_API void nxo_annual_insolation(const double *xyz, int64_t n, double radius, 
     }
 }
 
+/* util.py:79-88 */
+static void latlon2xyz(double lat, double lon, double r, double *o)
+{
+    o[0] = r * cos(lat * (PI / 180)) * cos(lon * (PI / 180));
+    o[1] = r * cos(lat * (PI / 180)) * sin(lon * (PI / 180));
+    o[2] = r * sin(lat * (PI / 180));
+}
+
+/* climate.py:503-533: 181 entries, entry i holding latitude i for i <= 90
+ * and i - 181 above (the reference's negative indexing), each the binary32
+ * sum of sample_insolation over 360 rotations of 1 degree from -180. */
+NXO_API void nxo_calc_insolation_slice(double radius, double tilt, float *out)
+{
+    double v[181 * 3];
+    for (int i = -90; i <= 90; ++i) latlon2xyz((double)i, 0.0, radius, v + 3 * ((i + 181) % 181));
+    for (int i = 0; i < 181; ++i) out[i] = 0.0f;
+    double rotation = -180.0;
+    for (int x = 0; x < 360; ++x) {
+        double cr = cos(rotation * PI / 180), sr = sin(rotation * PI / 180);
+        double ct = cos(tilt * PI / 180), st = sin(tilt * PI / 180);
+        for (int i = 0; i < 181; ++i)
+            out[i] = (float)((double)out[i] + insolation_term(v[3 * i], v[3 * i + 1], v[3 * i + 2], radius, cr, sr, ct, st));
+        rotation += 1.0;
+    }
+}
+
+/* climate.py:551-577: linear interpolation between the table entries of
+ * floor(lat) and ceil(lat) (the latitude depends on z only); the difference of the two binary32 entries is
+ * taken in binary32, the rest in binary64, the result rounded to binary32. */
+static float interp_one(const float *table, double z, double radius)
+{
+    double q = z / radius;
+    if (q < -1) q = -1;
+    if (q > 1) q = 1;
+    const double lat = asin(q) * (180.0 / PI);
+    const long lower = (long)floor(lat), upper = (long)ceil(lat);
+    const float tl = table[(lower + 181) % 181], tu = table[(upper + 181) % 181];
+    if (lower == upper) return tl;
+    const float dt = tu - tl;
+    return (float)((double)tl + (lat - (double)lower) * ((double)dt / (double)(upper - lower)));
+}
+
+NXO_API void nxo_interpolate_insolation(const double *xyz, int64_t n, const float *table, float *out, double radius)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = interp_one(table, xyz[3 * i + 2], radius);
+}
+
+/* climate.py:579-597 (no snapshots): 360 daily tables at the seasonal tilt
+ * of each orbital degree, interpolated and summed in binary32. */
+NXO_API void nxo_calc_yearly_insolation(const double *xyz, int64_t n, double radius, double axial_tilt, float *out)
+{
+    float *tab = (float *)malloc(sizeof(float) * 181 * 360);
+    if (!tab) return;
+    for (int d = 0; d < 360; ++d) nxo_calc_insolation_slice(radius, nxo_calculate_seasonal_tilt(axial_tilt, (double)d),
+                                                             tab + 181 * d);
+    for (int64_t i = 0; i < n; ++i) {
+        float acc = 0.0f;
+        for (int d = 0; d < 360; ++d)
+            acc = acc + interp_one(tab + 181 * d, xyz[3 * i + 2], radius);
+        out[i] = acc;
+    }
+    free(tab);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Mesh adjacency and scalar helpers                                          */
 /* ------------------------------------------------------------------------ */
@@ -835,6 +899,95 @@ NXO_API void nxo_rescale(const double *x, int64_t n, double lower, double upper,
     }
     double xr = mx - mn, nr = upper - lower;
     for (int64_t i = 0; i < n; ++i) out[i] = ((x[i] - mn) / xr) * nr + lower;
+}
+
+/* util.py:110-176, every form.  form: 0 plain, 1 with mid (each side of mid
+ * mapped separately), 2 mode 'lower' (only x <= mid), 3 mode 'upper' (only
+ * x >= mid).  u_min / u_max widen the input range (util.py:128-131). */
+NXO_API void nxo_rescale_full(const double *x, int64_t n, double lower, double upper, double mid, int form,
+                              double u_min, int has_umin, double u_max, int has_umax, double *out)
+{
+    if (n <= 0) return;
+    double x_min = x[0], x_max = x[0];
+    for (int64_t i = 1; i < n; ++i) {
+        if (x[i] < x_min) x_min = x[i];
+        if (x[i] > x_max) x_max = x[i];
+    }
+    if (has_umin && u_min < x_min) x_min = u_min;
+    if (has_umax && u_max > x_max) x_max = u_max;
+    for (int64_t i = 0; i < n; ++i) {
+        const double v = x[i];
+        double r = v;
+        if (form == 0) {
+            r = ((v - x_min) / (x_max - x_min)) * (upper - lower) + lower;
+        } else if (form == 1) {
+            if (v <= mid) r = ((v - x_min) / (mid - x_min)) * (mid - lower) + lower;
+            else r = ((v - mid) / (x_max - mid)) * (upper - mid) + mid;
+        } else if (form == 2) {
+            if (v <= mid) r = ((v - x_min) / (mid - x_min)) * (mid - lower) + lower;
+        } else {
+            if (v >= mid) r = ((v - mid) / (x_max - mid)) * (upper - mid) + mid;
+        }
+        out[i] = r;
+    }
+}
+
+/* util.py:556-566 */
+NXO_API double nxo_find_percent_val(double minval, double maxval, double percent)
+{
+    if (!(0.0 < percent && percent < 100.0)) percent = 50.0;
+    return minval + ((maxval - minval) * percent / 100.0);
+}
+
+/* util.py:179-250.  mode: -1 (None), 0 (rescale where mask is false), 1
+ * (where mask is true).  The masked range comes from the reference's
+ * running update (a new running minimum is not compared with the maximum). */
+NXO_API void nxo_power_rescale(const double *x, int64_t n, const uint8_t *mask, int mode, double power, double *out)
+{
+    if (n <= 0) return;
+    const double temp_upper = 1.0, temp_lower = 0.0, temp_range = temp_upper - temp_lower;
+    double x_min = x[0], x_max = x[0];
+    for (int64_t i = 1; i < n; ++i) {
+        if (x[i] < x_min) x_min = x[i];
+        if (x[i] > x_max) x_max = x[i];
+    }
+    double lo = x_max, hi = x_min;
+    for (int64_t i = 0; i < n; ++i) {
+        const int sel = mode == 1 ? mask[i] != 0 : (mode == 0 ? mask[i] == 0 : 0);
+        if (sel && x[i] < lo) lo = x[i];
+        else if (sel && x[i] > hi) hi = x[i];
+    }
+    const double range = hi - lo;
+    for (int64_t i = 0; i < n; ++i) {
+        const int sel = mode == 1 ? mask[i] != 0 : (mode == 0 ? mask[i] == 0 : 0);
+        double v = x[i];
+        if (sel) {
+            v = ((v - lo) / range) * temp_range + temp_lower;
+            v = pow(v, power);
+            v = ((v - temp_lower) / temp_range) * range + lo;
+        }
+        out[i] = v;
+    }
+}
+
+/* nixis.py:332-364: rescale to [min_alt, max_alt], ocean level, mask, the
+ * two masked power rescales, shift, rescale about 0.  tmp: n doubles. */
+NXO_API double nxo_shape_heights(const double *h, int64_t n, double min_alt, double max_alt, double ocean_percent,
+                                 double *out, double *tmp, uint8_t *mask)
+{
+    nxo_rescale_full(h, n, min_alt, max_alt, 0.0, 0, 0.0, 0, 0.0, 0, out);
+    double mn = out[0], mx = out[0];
+    for (int64_t i = 1; i < n; ++i) {
+        if (out[i] < mn) mn = out[i];
+        if (out[i] > mx) mx = out[i];
+    }
+    const double level = nxo_find_percent_val(mn, mx, ocean_percent);
+    nxo_make_bool_elevation_mask(out, n, level, mask);
+    nxo_power_rescale(out, n, mask, 1, 0.5, tmp);
+    nxo_power_rescale(tmp, n, mask, 0, 2.0, out);
+    for (int64_t i = 0; i < n; ++i) tmp[i] = out[i] - level;
+    nxo_rescale_full(tmp, n, min_alt, max_alt, 0.0, 1, 0.0, 0, 0.0, 0, out);
+    return level;
 }
 
 NXO_API int nxo_num_threads(void)

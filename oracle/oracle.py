@@ -56,6 +56,13 @@ def lib():
             "nxo_build_adjacency": (_i32, [_p, _i64, _p]),
             "nxo_sort_adjacency": (_i32, [_p, _i64]),
             "nxo_rescale": (None, [_p, _i64, _d, _d, _p]),
+            "nxo_rescale_full": (None, [_p, _i64, _d, _d, _d, ctypes.c_int, _d, ctypes.c_int, _d, ctypes.c_int, _p]),
+            "nxo_find_percent_val": (_d, [_d, _d, _d]),
+            "nxo_power_rescale": (None, [_p, _i64, _p, ctypes.c_int, _d, _p]),
+            "nxo_shape_heights": (_d, [_p, _i64, _d, _d, _d, _p, _p, _p]),
+            "nxo_calc_insolation_slice": (None, [_d, _d, _p]),
+            "nxo_interpolate_insolation": (None, [_p, _i64, _p, _p, _d]),
+            "nxo_calc_yearly_insolation": (None, [_p, _i64, _d, _d, _p]),
             "nxo_num_threads": (_i32, []),
             "nxo_icosphere": (_i32, [_i32, _p, _p, _p, _p, _p, _p]),
         }
@@ -242,6 +249,66 @@ def rescale(x, lower, upper):
     x = _c(x, np.float64)
     out = np.empty_like(x)
     lib().nxo_rescale(_ptr(x), len(x), float(lower), float(upper), _ptr(out))
+    return out
+
+
+_FORMS = {None: 0, "lower": 2, "upper": 3}
+
+
+def rescale_full(x, lower, upper, mid=None, mode=None, u_min=None, u_max=None):
+    """util.rescale (util.py:110-176) in every form; returns a new array, or
+    x itself when a mode is given without mid (as the reference does)."""
+    x = _c(x, np.float64)
+    if mode is not None and mid is None:
+        return x
+    form = 1 if (mode is None and mid is not None) else _FORMS[mode]
+    out = np.empty_like(x)
+    lib().nxo_rescale_full(_ptr(x), len(x), float(lower), float(upper), float(mid or 0.0), form,
+                           float(u_min or 0.0), int(u_min is not None), float(u_max or 0.0), int(u_max is not None),
+                           _ptr(out))
+    return out
+
+
+def find_percent_val(minval, maxval, percent):
+    return lib().nxo_find_percent_val(float(minval), float(maxval), float(percent))
+
+
+def power_rescale(x, mask=None, mode=None, power=1.0):
+    x = _c(x, np.float64)
+    m = _c(np.zeros(len(x), np.uint8) if mask is None else np.asarray(mask).astype(np.uint8), np.uint8)
+    out = np.empty_like(x)
+    lib().nxo_power_rescale(_ptr(x), len(x), _ptr(m), -1 if mode is None else int(mode), float(power), _ptr(out))
+    return out
+
+
+def shape_heights(h, min_alt=-4000.0, max_alt=8850.0, ocean_percent=55.0):
+    """nixis.py:332-364 -> (heights, ocean mask, ocean level)."""
+    h = _c(h, np.float64)
+    out, tmp = np.empty_like(h), np.empty_like(h)
+    mask = np.empty(len(h), np.uint8)
+    level = lib().nxo_shape_heights(_ptr(h), len(h), float(min_alt), float(max_alt), float(ocean_percent), _ptr(out),
+                                    _ptr(tmp), _ptr(mask))
+    return out, mask, level
+
+
+def calc_insolation_slice(radius, tilt):
+    out = np.empty(181, np.float32)
+    lib().nxo_calc_insolation_slice(float(radius), float(tilt), _ptr(out))
+    return out
+
+
+def interpolate_insolation(verts, table, radius):
+    v = _c(verts, np.float64)
+    t = _c(table, np.float32)
+    out = np.empty(len(v), np.float32)
+    lib().nxo_interpolate_insolation(_ptr(v), len(v), _ptr(t), _ptr(out), float(radius))
+    return out
+
+
+def calc_yearly_insolation(verts, radius, axial_tilt):
+    v = _c(verts, np.float64)
+    out = np.empty(len(v), np.float32)
+    lib().nxo_calc_yearly_insolation(_ptr(v), len(v), float(radius), float(axial_tilt), _ptr(out))
     return out
 
 

@@ -9,8 +9,10 @@ Every expected value in the output comes from the reference's own Python
 functions (opensimplex.init / noise3d, terrain.sample_noise / sample_octaves,
 erosion.erosion_iteration3 / erode_terrain3 / find_lowest,
 climate.sample_insolation / brute_daily_insolation / calculate_seasonal_tilt /
-day2deg, util.build_adjacency / sort_adjacency / rescale) imported through
-ref_shim.  Inputs are seeded; meshes come from tests/meshref.py (the same
+day2deg, util.build_adjacency / sort_adjacency / rescale / power_rescale /
+find_percent_val, terrain.make_bool_elevation_mask, climate.calc_insolation_slice /
+interpolate_insolation / calc_daily_insolation / calc_yearly_insolation) imported through
+ref_shim.  `python tests/golden/make_golden.py shaping` regenerates one set.  Inputs are seeded; meshes come from tests/meshref.py (the same
 construction as the GPU generator).
 """
 import os
@@ -228,13 +230,87 @@ def gen_insolation(R):
     np.savez_compressed(os.path.join(HERE, "insolation.npz"), **out)
 
 
+def gen_shaping(R):
+    """The post-noise shaping of nixis.py:330-364 (rescale to [min_alt,
+    max_alt], ocean level at a percent of the range, elevation mask, masked
+    power rescales, shift, two-sided rescale about 0) on 12-octave terrain,
+    plus rescale's mid/mode/u_min/u_max forms and power_rescale on arrays
+    that exercise its running min/max update (a masked value that is the
+    running minimum is not considered for the maximum)."""
+    util, ter, osi = R.util, R.terrain, R.opensimplex
+    out = {}
+    pts, _ = meshref.icosphere(24)
+    perm, pgi = osi.init(5)
+    h = np.asarray(quiet(ter.sample_octaves, pts, None, perm, pgi, 12, 1.0, 1.0, 2.0, 0.5, 1.0), np.float64)
+    out["noise"] = h.copy()
+    min_alt, max_alt, ocean_percent = -4000.0, 8850.0, 55.0       # nixis.py:312-315
+    h1 = np.asarray(util.rescale(h, min_alt, max_alt), np.float64)
+    ocean_level = util.find_percent_val(np.amin(h1), np.amax(h1), ocean_percent)
+    ocean = np.asarray(ter.make_bool_elevation_mask(h1, ocean_level))
+    h2 = np.asarray(quiet(util.power_rescale, h1, mask=ocean, mode=1, power=0.5), np.float64)
+    h3 = np.asarray(quiet(util.power_rescale, h2, mask=ocean, mode=0, power=2.0), np.float64)
+    h4 = h3 - ocean_level
+    h5 = np.asarray(util.rescale(h4, min_alt, max_alt, mid=0), np.float64)
+    out.update(h1=h1, ocean_level=np.array([ocean_level]), ocean=ocean.astype(np.uint8), h2=h2, h3=h3, h5=h5)
+    rng = np.random.default_rng(17)
+    x = rng.normal(0.0, 3.0, 2000)
+    out["x"] = x
+    out["rescale_mid"] = np.asarray(util.rescale(x, -10.0, 20.0, mid=0.5), np.float64)
+    out["rescale_lower"] = np.asarray(util.rescale(x, -10.0, 20.0, mid=0.5, mode="lower"), np.float64)
+    out["rescale_upper"] = np.asarray(util.rescale(x, -10.0, 20.0, mid=0.5, mode="upper"), np.float64)
+    out["rescale_umin_umax"] = np.asarray(util.rescale(x, 0.0, 1.0, u_min=-100.0, u_max=100.0), np.float64)
+    out["rescale_umin_inside"] = np.asarray(util.rescale(x, 0.0, 1.0, u_min=0.0, u_max=1.0), np.float64)
+    m = rng.random(2000) < 0.4
+    out["pmask"] = m.astype(np.uint8)
+    for mode, power in ((1, 0.5), (0, 2.0), (1, 3.0), (0, 0.25)):
+        out[f"power_m{mode}_p{power}"] = np.asarray(quiet(util.power_rescale, x, mask=m, mode=mode, power=power),
+                                                    np.float64)
+    # the first masked value is the largest masked value: the running
+    # update never records it as the maximum
+    y = x.copy()
+    first = int(np.argmax(m))
+    y[first] = np.max(y[m]) + 1.0
+    out["y"] = y
+    out["power_first_is_max"] = np.asarray(quiet(util.power_rescale, y, mask=m, mode=1, power=0.5), np.float64)
+    out["percent_vals"] = np.array([util.find_percent_val(-4000.0, 8850.0, p) for p in (55.0, 0.0, 100.0, 12.5)])
+    np.savez_compressed(os.path.join(HERE, "shaping.npz"), **out)
+
+
+def gen_lut_insolation(R):
+    """The latitude-table insolation path (climate.py:503-597):
+    calc_insolation_slice for a few tilts and radii, calc_daily_insolation
+    and interpolate_insolation on icosphere vertices, and a full
+    calc_yearly_insolation (360 daily tables) on a small sphere."""
+    cl = R.climate
+    out = {}
+    cases = [(1.0, 23.44), (1.0, 0.0), (1.0, -17.3), (6378100.0, 10.0)]
+    out["slice_cases"] = np.array(cases)
+    for i, (r, t) in enumerate(cases):
+        out[f"slice_{i}"] = np.asarray(cl.calc_insolation_slice(r, t), np.float32)
+    p8, _ = meshref.icosphere(8)
+    h8 = np.linspace(-1.0, 1.0, len(p8))
+    out["daily_k8_t23"] = np.asarray(quiet(cl.calc_daily_insolation, p8, h8, 1.0, 23.44), np.float32)
+    tab = out["slice_2"]
+    ins = np.zeros(len(p8), np.float32)
+    pe = p8 * 6378100.0
+    cl.interpolate_insolation(pe, tab, ins, 6378100.0)
+    out["interp_k8_earth"] = ins
+    p4, _ = meshref.icosphere(4)
+    out["yearly_k4_t23"] = np.asarray(quiet(cl.calc_yearly_insolation, p4, np.zeros(len(p4)), 1.0, 23.44),
+                                      np.float32)
+    np.savez_compressed(os.path.join(HERE, "lut_insolation.npz"), **out)
+
+
+GENERATORS = {"perm": gen_perm, "noise": gen_noise, "octaves": gen_octaves, "mesh_erosion": gen_mesh_erosion,
+              "insolation": gen_insolation, "shaping": gen_shaping,
+              "lut_insolation": gen_lut_insolation}
+
+
 def main():
     R = ref_shim.load()
-    gen_perm(R)
-    gen_noise(R)
-    gen_octaves(R)
-    gen_mesh_erosion(R)
-    gen_insolation(R)
+    names = sys.argv[1:] or list(GENERATORS)
+    for name in names:
+        GENERATORS[name](R)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -88,3 +88,40 @@ def test_vertices_off_the_sphere_use_the_general_formula():
     got = climate.annual_insolation(v, 1.0, days=20, hours=24).cpu().numpy()
     ref = annual_ref(v, 1.0, 20, 24)
     assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
+
+
+# ---------------------------------------------------------------------------
+# latitude-table path (climate.py:503-597).  The tables sum 360 binary64
+# terms in binary32 as the reference does; CUDA's and libm's asin/atan2/cos
+# differ in the last bits of a term, which can move a binary32 rounding by
+# one ulp: tables and interpolations are held to 2 ulp of their maximum,
+# the 360-table year to 1e-6 of its maximum.
+
+def test_lut_tables_and_interpolation_match_reference():
+    import golden_io
+    from nixis_gb300 import climate
+    g = golden_io.load("lut_insolation")
+    for i, (r, t) in enumerate(g["slice_cases"]):
+        got, want = climate.calc_insolation_slice(r, t), g[f"slice_{i}"]
+        assert np.abs(got - want).max() <= 2 * np.spacing(np.float32(want.max())), i
+    p8, _ = meshref.icosphere(8)
+    d = climate.calc_daily_insolation(p8, np.zeros(len(p8)), 1.0, 23.44)
+    assert np.abs(d - g["daily_k8_t23"]).max() <= 2 * np.spacing(np.float32(g["daily_k8_t23"].max()))
+    ins = np.zeros(len(p8), np.float32)
+    climate.interpolate_insolation(p8 * 6378100.0, g["slice_2"], ins, 6378100.0)
+    # the table is given: only the latitude (one asin) can differ
+    assert np.abs(ins - g["interp_k8_earth"]).max() <= 2 * np.spacing(np.float32(g["interp_k8_earth"].max()))
+    p4, _ = meshref.icosphere(4)
+    y = climate.calc_yearly_insolation(p4, np.zeros(len(p4)), 1.0, 23.44)
+    assert np.abs(y - g["yearly_k4_t23"]).max() <= 1e-6 * g["yearly_k4_t23"].max()
+
+
+def test_lut_yearly_on_a_large_sphere_matches_oracle():
+    from nixis_gb300 import climate, mesh
+    m = mesh.PlanetMesh(300)
+    y = climate.calc_yearly_insolation(m.xyz, None, 1.0, 23.44).cpu().numpy()
+    rng = np.random.default_rng(5)
+    idx = rng.choice(m.n, 20000, replace=False)
+    want = O.calc_yearly_insolation(m.xyz.cpu().numpy()[idx], 1.0, 23.44)
+    assert np.abs(y[idx] - want).max() <= 1e-6 * want.max()
+    assert np.isfinite(y).all() and y.min() > 0       # with a tilt even the poles see the sun

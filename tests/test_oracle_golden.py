@@ -114,6 +114,37 @@ def test_erode_terrain3_bit_exact(k):
         assert np.array_equal(h, g[f"erode3_k{k}_n{n_iter}"])
 
 
+def test_shaping_bit_exact():
+    """util.rescale in every form, find_percent_val, power_rescale (including
+    the running-maximum quirk) and the whole nixis.py:332-364 sequence."""
+    g = golden_io.load("shaping")
+    x, m = g["x"], g["pmask"]
+    assert np.array_equal(O.rescale_full(x, -10, 20, mid=0.5), g["rescale_mid"])
+    assert np.array_equal(O.rescale_full(x, -10, 20, mid=0.5, mode="lower"), g["rescale_lower"])
+    assert np.array_equal(O.rescale_full(x, -10, 20, mid=0.5, mode="upper"), g["rescale_upper"])
+    assert np.array_equal(O.rescale_full(x, 0, 1, u_min=-100, u_max=100), g["rescale_umin_umax"])
+    assert np.array_equal(O.rescale_full(x, 0, 1, u_min=0, u_max=1), g["rescale_umin_inside"])
+    for mode, p in ((1, 0.5), (0, 2.0), (1, 3.0), (0, 0.25)):
+        assert np.array_equal(O.power_rescale(x, m, mode, p), g[f"power_m{mode}_p{p}"]), (mode, p)
+    assert np.array_equal(O.power_rescale(g["y"], m, 1, 0.5), g["power_first_is_max"])
+    h, mask, level = O.shape_heights(g["noise"])
+    assert np.array_equal(h, g["h5"]) and np.array_equal(mask, g["ocean"]) and level == g["ocean_level"][0]
+    assert [O.find_percent_val(-4000, 8850, p) for p in (55.0, 0.0, 100.0, 12.5)] == list(g["percent_vals"])
+
+
+def test_lut_insolation_bit_exact():
+    """calc_insolation_slice, interpolate_insolation, calc_daily_insolation
+    (climate.py:503-577) and a full calc_yearly_insolation (579-597)."""
+    g = golden_io.load("lut_insolation")
+    for i, (r, t) in enumerate(g["slice_cases"]):
+        assert np.array_equal(O.calc_insolation_slice(r, t), g[f"slice_{i}"]), i
+    p8, _ = meshref.icosphere(8)
+    assert np.array_equal(O.interpolate_insolation(p8, O.calc_insolation_slice(1.0, 23.44), 1.0), g["daily_k8_t23"])
+    assert np.array_equal(O.interpolate_insolation(p8 * 6378100.0, g["slice_2"], 6378100.0), g["interp_k8_earth"])
+    p4, _ = meshref.icosphere(4)
+    assert np.array_equal(O.calc_yearly_insolation(p4, 1.0, 23.44), g["yearly_k4_t23"])
+
+
 def test_find_lowest_matches_reference():
     g = golden_io.load("mesh_erosion")
     adj = g["adj_k6"]
