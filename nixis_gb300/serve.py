@@ -165,7 +165,7 @@ class Ticket:
 def _pinned(a):
     """A copy of numpy array a in page-locked memory from torch's caching
     host allocator (reused once freed, instead of a fresh cudaHostAlloc)."""
-    t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0]).dtype, pin_memory=True)
+    t = torch.empty(a.shape, dtype=torch.from_numpy(np.empty(0, a.dtype)).dtype, pin_memory=True)
     t.numpy()[...] = a
     return t
 
