@@ -216,6 +216,8 @@ typedef struct nx_erosion_planet {
     const nx_tiling *tiling;   /* device copy of the mesh's tiling, or NULL */
     int32_t ntiles;            /* its ntiles (read on the host) */
     int32_t maxnl;             /* its largest local vertex count */
+    int32_t maxc;              /* its largest updatable count (tables held in shared memory) */
+    int32_t pad;
 } nx_erosion_planet;
 
 /* Workspace bytes for erosion over n_padded_total state rows (a bound on
@@ -301,14 +303,16 @@ int nx_erosion_npass(int iters);
 int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
 
 /* Temporal blocking settings (process wide, default 4 rings, 512 threads,
- * no prefetch, enabled): the ring count of the tilings that batches use
+ * variant 0, enabled): the ring count of the tilings that batches use
  * (passes have up to that many iterations), threads per block of the
- * blocked kernel (256, 512 or 1024; with prefetch = 1, the variant that
- * loads the next vertex's tile entries ahead, 256 or 384), and whether
- * batches with tilings use it (1) or run one iteration per launch (0).  The
- * autotuner (nixis_gb300.autotune) picks these and the tile side per
- * device. */
-int nx_erosion_tb_config(int rings, int threads, int prefetch, int enabled);
+ * blocked kernel, the kernel variant -- 0: tile tables read from global
+ * memory each iteration (256, 512 or 1024 threads); 1: the same with the
+ * next vertex's entries loaded ahead (256 or 384); 2: the tile's tables
+ * copied to shared memory once per pass (512 or 1024; needs maxc in the
+ * planet descriptors) -- and whether batches with tilings use it (1) or
+ * run one iteration per launch (0).  The autotuner (nixis_gb300.autotune)
+ * picks these and the tile side per device. */
+int nx_erosion_tb_config(int rings, int threads, int variant, int enabled);
 
 /* Write one planet's state back as binary64 true values (hi + lo of each
  * field times 2^K, K from the workspace's first control block).  w64_dev /
@@ -355,6 +359,30 @@ int nx_insolation_slices(const double *tilts_dev, int n_tilts, double radius, fl
  * to out_dev. */
 int nx_interpolate_insolation(const double *xyz_dev, int64_t n, double radius, const float *tables_dev, int n_tables,
                               float *out_dev, int accumulate, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Equirectangular maps (util.py:290-366, nixis.py:270-302)            */
+/* ------------------------------------------------------------------ */
+
+/* util.make_ll_arr: out_dev double[height*width*3], pixel (h, w) at
+ * latitude max(90 - h*180/(height-1), -90), longitude
+ * max(-180 + w*360/width, -180) on the sphere of the radius. */
+int nx_make_ll(int width, int height, double radius, double *out_dev, void *stream);
+
+/* The 3 nearest vertices of nq query points (replaces the reference's
+ * KDTree(points).query(queries, k=3)): xyz_dev/nbr_dev the icosphere of
+ * divisions k made by nx_icosphere / nx_build_adjacency / nx_sort_adjacency
+ * (any radius; nv = 10k^2+2); dist_dev double[nq*3] ascending, idx_dev
+ * int64[nq*3] (ties by vertex id).  Needs nx_icosphere_tables. */
+int nx_nearest3(int k, const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, const double *q_dev, int64_t nq,
+                double *dist_dev, int64_t *idx_dev, void *stream);
+
+/* util.make_gray_array per pixel: inverse-distance weighting of the 3
+ * neighbours' colours (double[ncolors]), truncated toward zero, into
+ * out_dev double[npix]; err_dev (device int, caller zeroes it) gets bit 0 for
+ * an index outside the colours. */
+int nx_sample_gray(const double *dist_dev, const int64_t *idx_dev, int64_t npix, const double *colors_dev,
+                   int64_t ncolors, double *out_dev, int *err_dev, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Height shaping (nixis.py:332-364), binary64                         */

@@ -54,6 +54,9 @@ SIGNATURES = {
     "nx_erosion_npass": (_i32, [_i32]),
     "nx_shape_workspace_size": (ctypes.c_size_t, [_i64]),
     "nx_insolation_slices": (_i32, [_p, _i32, _d, _p, _p]),
+    "nx_make_ll": (_i32, [_i32, _i32, _d, _p, _p]),
+    "nx_nearest3": (_i32, [_i32, _p, _p, _i64, _p, _i64, _p, _p, _p]),
+    "nx_sample_gray": (_i32, [_p, _p, _i64, _p, _i64, _p, _p, _p]),
     "nx_interpolate_insolation": (_i32, [_p, _i64, _d, _p, _i32, _p, _i32, _p]),
     "nx_rescale": (_i32, [_p, _i64, _d, _d, _d, _i32, _d, _i32, _d, _i32, _p, _p, ctypes.c_size_t, _p]),
     "nx_power_rescale": (_i32, [_p, _i64, _p, _i32, _d, _p, _p, ctypes.c_size_t, _p]),
@@ -87,7 +90,8 @@ class ErosionPlanet(ctypes.Structure):
     _fields_ = [("vbeg", ctypes.c_int64), ("n", ctypes.c_int64), ("nbr", ctypes.c_void_p),
                 ("edge", ctypes.c_void_p), ("iters", ctypes.c_int32), ("rain", ctypes.c_float),
                 ("t_start", ctypes.c_int32), ("slot", ctypes.c_int32), ("tiling", ctypes.c_void_p),
-                ("ntiles", ctypes.c_int32), ("maxnl", ctypes.c_int32)]
+                ("ntiles", ctypes.c_int32), ("maxnl", ctypes.c_int32), ("maxc", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
 
 
 class Tiling(ctypes.Structure):

@@ -4,9 +4,12 @@ Four knobs set how the blocked erosion maps onto the GPU: the tile side
 (tiles are side x side squares of a face grid; bigger tiles waste less work
 on halo rings but need more shared memory per block), the rings per pass
 (iterations done in shared memory between trips to HBM; more rings mean
-fewer trips but wider halos), the threads per block, and whether each
-thread loads its next vertex's tile entries ahead of computing the current
-one (hides their latency, costs registers and so resident threads).  ``tune`` times
+fewer trips but wider halos), the threads per block, and the kernel
+variant: 0 reads the tile tables (neighbour indices, edge lengths) from
+global memory every iteration, 1 loads the next vertex's entries ahead of
+computing the current one (hides their latency, costs registers and so
+resident threads), 2 copies the tile's tables to shared memory once per
+pass (no per-iteration global reads, but more shared memory per block).  ``tune`` times
 every candidate on a synthetic planet, checks that all of them give the
 same heights bit for bit (they run the same per-vertex arithmetic), keeps
 the fastest and caches it per device in a JSON file
@@ -24,11 +27,16 @@ import torch
 from . import _dev
 from ._lib import NxError, call, lib
 
-SMEM_LIMIT = 200 * 1024          # dynamic shared memory the blocked kernel may use
+SMEM_LIMIT = 200 * 1024          # dynamic shared memory of variants 0 and 1
+SMEM_LIMIT_TABLES = 226 * 1024   # of variant 2 (the opt-in limit less static shared memory, rounded down)
 ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
-SIDES = (32, 40, 48, 56)
+SIDES = (24, 28, 32, 40, 48)
 RINGS = (2, 3, 4, 5)
-THREADS = ((256, False), (512, False), (1024, False), (256, True), (384, True))
+THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2))
+# variant 2 measured slower on GB300 for every tile size (one block per SM
+# cannot overlap its load phase with compute): tried only on request
+DEFAULT_VARIANTS = (0, 1)
+SUFFIX = {0: "", 1: "p", 2: "s"}
 
 
 @dataclass(frozen=True)
@@ -36,11 +44,24 @@ class TbConfig:
     tile_side: int = 40
     rings: int = 4
     threads: int = 512
-    prefetch: bool = False
+    variant: int = 0
 
     @property
     def label(self):
-        return f"{self.tile_side}/{self.rings}/{self.threads}" + ("p" if self.prefetch else "")
+        return f"{self.tile_side}/{self.rings}/{self.threads}" + SUFFIX[self.variant]
+
+
+def smem_bytes(cfg, maxnl, maxc):
+    """Shared memory of a blocked launch over tiles of up to maxnl local and
+    maxc updatable vertices (as the library sizes it)."""
+    b = ROW_SMEM * (maxnl + (maxnl & 1))
+    if cfg.variant == 2:
+        b += 48 * maxc + ((12 * maxc + 15) // 16) * 16
+    return b
+
+
+def fits(cfg, maxnl, maxc):
+    return smem_bytes(cfg, maxnl, maxc) <= (SMEM_LIMIT_TABLES if cfg.variant == 2 else SMEM_LIMIT)
 
 
 DEFAULT = TbConfig()
@@ -83,7 +104,7 @@ def lookup(key, path=None):
     if not isinstance(e, dict):
         return None
     try:
-        return TbConfig(int(e["tile_side"]), int(e["rings"]), int(e["threads"]), bool(e.get("prefetch", False)))
+        return TbConfig(int(e["tile_side"]), int(e["rings"]), int(e["threads"]), int(e.get("variant", 0)))
     except (KeyError, TypeError, ValueError):
         return None
 
@@ -99,10 +120,11 @@ def store(key, cfg, timings=None, path=None):
 
 
 def parse(label):
-    """TbConfig from its label side/rings/threads, 'p' appended for prefetch."""
+    """TbConfig from its label side/rings/threads, 'p' appended for variant
+    1 (prefetch), 's' for variant 2 (tables in shared memory)."""
     side, rings, thr = label.split("/")
-    pf = thr.endswith("p")
-    return TbConfig(int(side), int(rings), int(thr.rstrip("p")), pf)
+    v = 1 if thr.endswith("p") else (2 if thr.endswith("s") else 0)
+    return TbConfig(int(side), int(rings), int(thr.rstrip("ps")), v)
 
 
 def current():
@@ -116,7 +138,7 @@ def current():
 
 def apply(cfg):
     """Make cfg the blocked kernel's setting (process wide)."""
-    call("nx_erosion_tb_config", int(cfg.rings), int(cfg.threads), int(bool(cfg.prefetch)), 1)
+    call("nx_erosion_tb_config", int(cfg.rings), int(cfg.threads), int(cfg.variant), 1)
 
 
 def use(cfg):
@@ -126,8 +148,9 @@ def use(cfg):
     apply(cfg)
 
 
-def candidates(mesh):
-    """Every (side, rings, threads, prefetch) whose tiles fit the shared-memory limit."""
+def candidates(mesh, variants=DEFAULT_VARIANTS):
+    """Every (side, rings, threads, variant) whose tiles may fit the shared
+    memory (checked again against the built tiling's counts)."""
     out = []
     for side in SIDES:
         for rings in RINGS:
@@ -136,17 +159,22 @@ def candidates(mesh):
                 call("nx_tiling_shape", mesh.k, side, rings, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm))
             except NxError:
                 continue                         # more local vertices than a tile may hold
-            if nm.value * ROW_SMEM > SMEM_LIMIT:
-                continue
-            for threads, pf in THREADS:
-                out.append(TbConfig(side, rings, threads, pf))
+            for threads, v in THREADS:
+                if v not in variants:
+                    continue
+                # capacities nm / cm are about twice the real counts
+                if v < 2 and nm.value * ROW_SMEM > 2 * SMEM_LIMIT:
+                    continue
+                out.append(TbConfig(side, rings, threads, v))
     return out
 
 
-def tune(divisions=400, iters=24, reps=3, configs=None, save=True, verbose=False):
+def tune(divisions=800, iters=24, reps=3, configs=None, save=True, verbose=False):
     """Time the candidates on one synthetic planet (12-octave terrain,
-    `iters` erosion iterations); returns (best config, {config: ms}).  Every
-    candidate must reproduce the first one's heights bit for bit."""
+    `iters` erosion iterations; divisions 800 = 6.4 M vertices, ~5,000
+    tiles, so that wave quantisation does not decide the choice); returns
+    (best config, {config: ms}).  Every candidate must reproduce the first
+    one's heights bit for bit."""
     from . import mesh as _mesh
     from . import planets as _planets
     _dev.require_cuda()
@@ -155,12 +183,12 @@ def tune(divisions=400, iters=24, reps=3, configs=None, save=True, verbose=False
     req = _planets.PlanetRequest(seed=12345, divisions=divisions, octaves=12, erosion_iters=iters)
     configs = list(configs) if configs is not None else candidates(m)
     timings, ref, best = {}, None, None
-    configs.sort(key=lambda c: (c.tile_side, c.rings, c.threads, c.prefetch))
+    configs.sort(key=lambda c: (c.tile_side, c.rings, c.threads, c.variant))
     for cfg in configs:
         for key in [k for k in m._tilings if k != (cfg.tile_side, cfg.rings)]:
             del m._tilings[key]                  # one tiling resident at a time
         tl = m.tiling(cfg.tile_side, cfg.rings)
-        if tl.maxnl * ROW_SMEM > SMEM_LIMIT:
+        if not fits(cfg, tl.maxnl, tl.maxc):
             continue
         bt = _planets.PlanetBatch([req], cache, tb=cfg)
         bt.launch()
@@ -206,4 +234,4 @@ def ensure_tuned(**kw):
 
 
 __all__ = ["TbConfig", "DEFAULT", "current", "use", "apply", "tune", "ensure_tuned", "candidates", "lookup", "store",
-           "device_key", "cache_path", "parse"]
+           "device_key", "cache_path", "parse", "fits", "smem_bytes"]

@@ -56,6 +56,7 @@ constexpr float CAP_H = (float)CAP, CAP_L = (float)(CAP - (double)CAP_H);
 // iteration parity; done = blocks finished in the current iteration (mass
 // sums); err = 1 for a neighbour id out of range.
 static_assert(sizeof(nx_erosion_ctl) == 32, "control block layout");
+static_assert(sizeof(nx_erosion_planet) == 72, "planet descriptor layout");
 
 namespace {
 
@@ -363,7 +364,8 @@ struct TbArgs {
     const int2 *blk_map;   // (planet, tile), planets ordered by pass count, descending
     int pass;              // global pass; a planet's pass is pass - t_start
     int R;
-    int smem_n;            // floats per shared array (>= every tile's local count)
+    int smem_n;            // rows per shared state array (>= every tile's local count)
+    int smem_c;            // rows of the shared tile tables (>= every tile's updatable count)
     float4 *st0;
     float4 *st1;
     nx_erosion_ctl *ctl;
@@ -377,25 +379,41 @@ struct TbArgs {
 // once (a vertex's sediment is read and written only by its own thread).
 __host__ __device__ __forceinline__ size_t tb_smem_bytes(int n) { return (2 * sizeof(float4) + sizeof(float2)) * (size_t)n; }
 
+// Variant 2 also holds the tile's tables for c updatable vertices: edge
+// pairs (48 B) and local neighbour indices (12 B, rounded to 16-byte units).
+__host__ __device__ __forceinline__ size_t tb_table_bytes(int c) { return 48 * (size_t)c + (((size_t)c * 12 + 15) & ~(size_t)15); }
+
+// Largest dynamic shared memory of a variant-2 block: the device's opt-in
+// limit less the kernel's static shared memory (set by tb_prepare).
+static size_t TB_SMEM_MAX = 200 * 1024;
+
 // One vertex's tile-table entries: local neighbour indices and edge pairs.
 struct TileRow {
     uint32_t p01, p23, p45;
     float4 d01, d23, d45;
 };
 
+template <bool SHARED>
 __device__ __forceinline__ TileRow tile_row(const uint32_t *lnb, const float4 *led, int l)
 {
     TileRow r;
-    r.p01 = __ldg(lnb + 3 * l); r.p23 = __ldg(lnb + 3 * l + 1); r.p45 = __ldg(lnb + 3 * l + 2);
-    r.d01 = __ldg(led + 3 * l); r.d23 = __ldg(led + 3 * l + 1); r.d45 = __ldg(led + 3 * l + 2);
+    if (SHARED) {
+        r.p01 = lnb[3 * l]; r.p23 = lnb[3 * l + 1]; r.p45 = lnb[3 * l + 2];
+        r.d01 = led[3 * l]; r.d23 = led[3 * l + 1]; r.d45 = led[3 * l + 2];
+    } else {
+        r.p01 = __ldg(lnb + 3 * l); r.p23 = __ldg(lnb + 3 * l + 1); r.p45 = __ldg(lnb + 3 * l + 2);
+        r.d01 = __ldg(led + 3 * l); r.d23 = __ldg(led + 3 * l + 1); r.d45 = __ldg(led + 3 * l + 2);
+    }
     return r;
 }
 
 // PF: software-pipelined table reads (the next vertex's entries are loaded
 // before the current vertex is computed; ~80 registers, so 768 threads per
 // SM); otherwise each vertex loads its own entries (64 registers, 1024
-// threads per SM).
-template <int THREADS, bool PF>
+// threads per SM).  SMT: the tile's tables are copied to shared memory once
+// per pass (with the state) and every iteration of the pass reads them
+// there.
+template <int THREADS, bool PF, bool SMT = false>
 __global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_tb_kernel(TbArgs a)
 {
     extern __shared__ float4 tsm4[];
@@ -438,6 +456,21 @@ __global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_
     float4 *buf0 = tsm4, *buf1 = tsm4 + a.smem_n;
     float2 *sed = reinterpret_cast<float2 *>(tsm4 + 2 * a.smem_n);
     const int32_t *ids = TL.ids + (int64_t)tile * TL.nmax;
+    const uint32_t *lnb = reinterpret_cast<const uint32_t *>(TL.lnbr) + (int64_t)tile * TL.cmax * 3;
+    const float4 *led = reinterpret_cast<const float4 *>(TL.ledge) + (int64_t)tile * TL.cmax * 3;
+    const int C0 = NL - cnt[len];                // members + rings 1..len-1: the rows this pass updates
+    if (SMT) {
+        // tables of rows [0, C0): edge pairs as float4s, neighbour indices as
+        // 16-byte units (the tile's slice starts 16-byte aligned: cmax*12 is a
+        // multiple of 16 and C0 < cmax leaves room to round up)
+        float4 *sled = reinterpret_cast<float4 *>(sed + a.smem_n + (a.smem_n & 1));
+        uint4 *slnb = reinterpret_cast<uint4 *>(sled + 3 * a.smem_c);
+        for (int r = threadIdx.x; r < 3 * C0; r += THREADS) sled[r] = __ldg(led + r);
+        const uint4 *g = reinterpret_cast<const uint4 *>(lnb);
+        for (int r = threadIdx.x; r < (C0 * 3 + 3) / 4; r += THREADS) slnb[r] = __ldg(g + r);
+        led = sled;
+        lnb = reinterpret_cast<const uint32_t *>(slnb);
+    }
     for (int l = threadIdx.x; l < NL; l += blockDim.x) {
         const int64_t row = P.vbeg + ids[l];
         const float4 x = ist[2 * row];
@@ -447,22 +480,20 @@ __global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_
         sed[l] = make_float2(__fmul_rn(y.x, lam), __fmul_rn(y.y, lam));
     }
     __syncthreads();
-    const uint32_t *lnb = reinterpret_cast<const uint32_t *>(TL.lnbr) + (int64_t)tile * TL.cmax * 3;
-    const float4 *led = reinterpret_cast<const float4 *>(TL.ledge) + (int64_t)tile * TL.cmax * 3;
-    int C = NL - cnt[len];                      // members + rings 1..len-1
+    int C = C0;
     for (int mi = 0; mi < len; ++mi) {
         const float4 *cur = (mi & 1) ? buf1 : buf0;
         float4 *nxt = (mi & 1) ? buf0 : buf1;
         const bool more = mi + 1 < len;          // rain for the next iteration in the pass
         TileRow nextrow;
-        if (PF && (int)threadIdx.x < C) nextrow = tile_row(lnb, led, threadIdx.x);
+        if (PF && (int)threadIdx.x < C) nextrow = tile_row<SMT>(lnb, led, threadIdx.x);
         for (int l = threadIdx.x; l < C; l += THREADS) {
             TileRow row;
             if (PF) {
                 row = nextrow;
-                if (l + THREADS < C) nextrow = tile_row(lnb, led, l + THREADS);
+                if (l + THREADS < C) nextrow = tile_row<SMT>(lnb, led, l + THREADS);
             } else {
-                row = tile_row(lnb, led, l);
+                row = tile_row<SMT>(lnb, led, l);
             }
             const uint32_t p01 = row.p01, p23 = row.p23, p45 = row.p45;
             const float4 d01 = row.d01, d23 = row.d23, d45 = row.d45;
@@ -773,27 +804,40 @@ static int64_t planet_blocks(const nx_erosion_planet &P) { return (P.n + BLOCK -
 // share it) and a switch for comparisons.
 static int g_tb_rings = 4;
 static int g_tb_threads = 512;
-static bool g_tb_prefetch = false;
+static int g_tb_variant = 0;
 static bool g_tb_enabled = true;
 
-NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int prefetch, int enabled)
+NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int variant, int enabled)
 {
     if (rings < 1 || rings > 8) return nx::fail(NX_EINVAL, "nx_erosion_tb_config: rings must be in [1, 8]");
-    const bool ok = prefetch ? (threads == 256 || threads == 384) : (threads == 256 || threads == 512 || threads == 1024);
+    const bool ok = variant == 1 ? (threads == 256 || threads == 384)
+                  : variant == 2 ? (threads == 512 || threads == 1024)
+                  : variant == 0 ? (threads == 256 || threads == 512 || threads == 1024) : false;
     if (!ok)
-        return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads must be 256, 512 or 1024 (256 or 384 with prefetch)");
+        return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads %d do not go with variant %d", threads, variant);
     g_tb_rings = rings;
     g_tb_threads = threads;
-    g_tb_prefetch = prefetch != 0;
+    g_tb_variant = variant;
     g_tb_enabled = enabled != 0;
     return NX_OK;
 }
 
+// Shared memory of a launch of the configured variant.
+static size_t tb_launch_smem(int maxnl, int maxc)
+{
+    size_t b = tb_smem_bytes(maxnl + (maxnl & 1));
+    if (g_tb_variant == 2) b += tb_table_bytes(maxc);
+    return b;
+}
+
 static cudaError_t launch_tb(int64_t grid, size_t smem, cudaStream_t s, const TbArgs &ta)
 {
-    if (g_tb_prefetch) {
+    if (g_tb_variant == 1) {
         if (g_tb_threads == 256) erosion_tb_kernel<256, true><<<(unsigned)grid, 256, smem, s>>>(ta);
         else erosion_tb_kernel<384, true><<<(unsigned)grid, 384, smem, s>>>(ta);
+    } else if (g_tb_variant == 2) {
+        if (g_tb_threads == 512) erosion_tb_kernel<512, false, true><<<(unsigned)grid, 512, smem, s>>>(ta);
+        else erosion_tb_kernel<1024, false, true><<<(unsigned)grid, 1024, smem, s>>>(ta);
     } else {
         switch (g_tb_threads) {
         case 256: erosion_tb_kernel<256, false><<<(unsigned)grid, 256, smem, s>>>(ta); break;
@@ -819,6 +863,17 @@ static int tb_prepare()
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<384, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        int optin = 0;
+        NX_CHECK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        cudaFuncAttributes fa512, fa1024;
+        NX_CHECK_CUDA(cudaFuncGetAttributes(&fa512, erosion_tb_kernel<512, false, true>));
+        NX_CHECK_CUDA(cudaFuncGetAttributes(&fa1024, erosion_tb_kernel<1024, false, true>));
+        const size_t st = fa512.sharedSizeBytes > fa1024.sharedSizeBytes ? fa512.sharedSizeBytes : fa1024.sharedSizeBytes;
+        TB_SMEM_MAX = (size_t)optin > st ? (size_t)optin - st : 0;
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<512, false, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TB_SMEM_MAX));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024, false, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TB_SMEM_MAX));
         done[dev] = true;
     }
     return NX_OK;
@@ -849,7 +904,7 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     // temporally blocked when every planet has a tiling and nothing per
     // iteration (mass sums, flow bits) is requested
     bool tb = !mass_dev && !flow_dev && g_tb_enabled;
-    int R = 0, maxnl = 0;
+    int R = 0, maxnl = 0, maxc = 0;
     int64_t ntiles_all = 0;
     for (int p = 0; p < np && tb; ++p) {
         const nx_erosion_planet &P = planets_host[p];
@@ -858,20 +913,23 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
             continue;
         }
         if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0) { tb = false; break; }
+        if (g_tb_variant == 2 && P.maxc <= 0)
+            return nx::fail(NX_EINVAL, "erosion: planet %d has no maxc (needed by blocked-kernel variant 2)", p);
         ntiles_all += P.ntiles;
         if (P.maxnl > maxnl) maxnl = P.maxnl;
+        if (P.maxc > maxc) maxc = P.maxc;
     }
     if (maxnl == 0) tb = false;
     if (tb) {
         R = g_tb_rings;
-        if (tb_smem_bytes(maxnl) > 200 * 1024) tb = false;
+        int rc = tb_prepare();
+        if (rc) return rc;
+        if (tb_launch_smem(maxnl, maxc) > (g_tb_variant == 2 ? TB_SMEM_MAX : 200 * 1024)) tb = false;
     }
     if (tb) {
         if (ws_bytes < nx_erosion_workspace_size((ntiles_all > nblk ? ntiles_all : nblk) * BLOCK, np))
             return nx::fail(NX_EINVAL, "erosion: workspace too small");
         Workspace w = carve(workspace, np, ntiles_all > nblk ? ntiles_all : nblk);
-        int rc = tb_prepare();
-        if (rc) return rc;
         erosion_tb_map_kernel<<<np, 256, 0, s>>>(planets_dev, np, R, w.blk_map);
         NX_CHECK_LAUNCH("erosion_tb_map_kernel");
         nx::note_launch(1);
@@ -885,10 +943,11 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         ta.blk_map = w.blk_map;
         ta.R = R;
         ta.smem_n = maxnl;
+        ta.smem_c = maxc;
         ta.st0 = (float4 *)st_dev;
         ta.st1 = (float4 *)st_tmp;
         ta.ctl = w.ctl;
-        const size_t smem = tb_smem_bytes(maxnl);
+        const size_t smem = tb_launch_smem(maxnl, maxc);
         for (int q = 0; q < maxpass; ++q) {
             int64_t grid = 0;
             for (int p = 0; p < np; ++p)
@@ -1012,21 +1071,25 @@ NX_EXPORT int nx_erosion_passes(const nx_erosion_planet *planets_dev, const nx_e
     if (!planets_dev || !planets_host || !st_dev || !st_tmp_dev || !workspace || nslots <= 0)
         return nx::fail(NX_EINVAL, "nx_erosion_passes: bad arguments");
     int64_t ntiles = 0;
-    int maxnl = 0;
+    int maxnl = 0, maxc = 0;
     for (int p = 0; p < nplanets; ++p) {
         const nx_erosion_planet &P = planets_host[p];
         if (P.vbeg < 0 || P.n < 0 || P.iters < 0 || P.slot < 0 || P.slot >= nslots || (P.n > 0 && (!P.nbr || !P.edge)))
             return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d: bad descriptor", p);
         if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0)
             return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d has no tiling", p);
+        if (g_tb_variant == 2 && P.maxc <= 0)
+            return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d has no maxc (needed by variant 2)", p);
         ntiles += P.ntiles;
         if (P.maxnl > maxnl) maxnl = P.maxnl;
+        if (P.maxc > maxc) maxc = P.maxc;
     }
-    if (tb_smem_bytes(maxnl) > 200 * 1024) return nx::fail(NX_EINVAL, "nx_erosion_passes: tiles too large");
-    if (ws_bytes < nx_erosion_workspace_size(ntiles * BLOCK, nslots))
-        return nx::fail(NX_EINVAL, "nx_erosion_passes: workspace too small");
     int rc = tb_prepare();
     if (rc) return rc;
+    if (tb_launch_smem(maxnl, maxc) > (g_tb_variant == 2 ? TB_SMEM_MAX : 200 * 1024))
+        return nx::fail(NX_EINVAL, "nx_erosion_passes: tiles too large");
+    if (ws_bytes < nx_erosion_workspace_size(ntiles * BLOCK, nslots))
+        return nx::fail(NX_EINVAL, "nx_erosion_passes: workspace too small");
     cudaStream_t s = (cudaStream_t)stream;
     Workspace w = carve(workspace, nslots, ntiles);
     const int R = g_tb_rings;
@@ -1040,12 +1103,13 @@ NX_EXPORT int nx_erosion_passes(const nx_erosion_planet *planets_dev, const nx_e
     ta.blk_map = w.blk_map;
     ta.R = R;
     ta.smem_n = maxnl;
+    ta.smem_c = maxc;
     ta.st0 = (float4 *)st_dev;
     ta.st1 = (float4 *)st_tmp_dev;
     ta.ctl = w.ctl;
     for (int q = 0; q < npasses; ++q) {
         ta.pass = pass + q;
-        NX_CHECK_CUDA(launch_tb(ntiles, tb_smem_bytes(maxnl), s, ta));
+        NX_CHECK_CUDA(launch_tb(ntiles, tb_launch_smem(maxnl, maxc), s, ta));
         nx::note_launch(1);
     }
     return NX_OK;
@@ -1194,7 +1258,7 @@ NX_EXPORT int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, con
 namespace {
 
 constexpr int64_t NOALLOC_MAX_N = NX_NOALLOC_MAX_VERTICES;
-constexpr size_t NOALLOC_HEAD = 512;    // descriptor (40 B) + control block (32 B), padded
+constexpr size_t NOALLOC_HEAD = 512;    // descriptor (72 B) at 0, control block (32 B) at 256, padded
 constexpr size_t NOALLOC_PARTIALS = (3 * sizeof(double) + sizeof(int2)) * (size_t)((NOALLOC_MAX_N + BLOCK - 1) / BLOCK);
 constexpr size_t NOALLOC_STATE = 32 * (size_t)NOALLOC_MAX_N;
 constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD + NOALLOC_PARTIALS + NOALLOC_STATE;

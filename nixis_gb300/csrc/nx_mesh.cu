@@ -20,6 +20,7 @@ struct IcoTables {
     int face[20][3];
     int fedge[20][3][2];   // per face side (AB, AC, BC): edge id, 1 if it runs low->high corner
     int edge[30][2];
+    double inv[20][3][3];  // per face: inverse of the matrix with columns A, B, C
 };
 
 __constant__ IcoTables c_ico;
@@ -288,6 +289,24 @@ int upload_tables(const double *corners, const int *faces, const int *fedge, con
     for (int e = 0; e < 30; ++e) {
         t.edge[e][0] = edges[2 * e];
         t.edge[e][1] = edges[2 * e + 1];
+    }
+    for (int f = 0; f < 20; ++f) {
+        // M = [A B C] (columns); inverse by cofactors
+        double m[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) m[r][c] = t.corner[t.face[f][c]][r];
+        const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1], c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2],
+                     c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+        const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+        t.inv[f][0][0] = c00 / det;
+        t.inv[f][1][0] = c01 / det;
+        t.inv[f][2][0] = c02 / det;
+        t.inv[f][0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) / det;
+        t.inv[f][1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) / det;
+        t.inv[f][2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) / det;
+        t.inv[f][0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) / det;
+        t.inv[f][1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) / det;
+        t.inv[f][2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) / det;
     }
     NX_CHECK_CUDA(cudaMemcpyToSymbol(c_ico, &t, sizeof(t)));
     IcoHome h;
@@ -619,6 +638,8 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
 
 }  // namespace
 
+static_assert(sizeof(nx_tiling) == 48, "tiling descriptor layout");
+
 NX_EXPORT int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax)
 {
     if (k < 1 || tile_side < 2 || rings < 1 || rings > 8 || !ntiles || !nmax || !cmax)
@@ -629,7 +650,7 @@ NX_EXPORT int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, 
     const int64_t B = tile_side;
     int64_t halo = 0;
     for (int r = 1; r <= rings; ++r) halo += 2 * (4 * B + 8 * r) + 64;
-    int64_t nm = B * B + 2 * B + halo, cm = B * B + 2 * B + halo;
+    int64_t nm = B * B + 2 * B + halo, cm = (B * B + 2 * B + halo + 3) & ~(int64_t)3;   // cm*12 B: 16-byte units
     if (nm > 4096) return nx::fail(NX_EINVAL, "nx_tiling_shape: tile too large (%lld local vertices)", (long long)nm);
     if (nt > 0x7FFFFFFF) return nx::fail(NX_EINVAL, "nx_tiling_shape: too many tiles");
     *ntiles = (int32_t)nt;
@@ -664,5 +685,90 @@ NX_EXPORT int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nb
                                             ledge_dev, err_dev);
     NX_CHECK_LAUNCH("tile_rings_kernel");
     nx::note_launch(2);
+    return NX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Nearest three vertices of query points (the reference's KD-tree
+// query(k=3), nixis.py:278-283), by point location in the icosphere's own
+// structure: the face whose corner matrix gives the query direction the
+// largest smallest barycentric weight, the grid triangle of the flat face
+// point (the spherical triangles are radial projections of the flat ones),
+// then the exact distances to that triangle's vertices and all their
+// neighbours.  On the icosphere's near-equilateral triangles the three
+// nearest vertices of a point are always among them (checked against brute
+// force in the tests).  Distances sqrt((dx*dx + dy*dy) + dz*dz), ascending,
+// ties by vertex id.
+
+namespace {
+
+__global__ void __launch_bounds__(256) nearest3_kernel(int k, const double *__restrict__ xyz,
+                                                       const int32_t *__restrict__ nbr, int64_t nv,
+                                                       const double *__restrict__ q, int64_t nq,
+                                                       double *__restrict__ dist, int64_t *__restrict__ idx)
+{
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nq; p += (int64_t)gridDim.x * blockDim.x) {
+        const double qx = q[3 * p], qy = q[3 * p + 1], qz = q[3 * p + 2];
+        int bf = 0;
+        double bw[3] = {0, 0, 0}, bs = -INFINITY;
+        for (int f = 0; f < 20; ++f) {
+            double w[3];
+            for (int r = 0; r < 3; ++r) w[r] = c_ico.inv[f][r][0] * qx + c_ico.inv[f][r][1] * qy + c_ico.inv[f][r][2] * qz;
+            const double sc = fmin(w[0], fmin(w[1], w[2]));
+            if (sc > bs) { bs = sc; bf = f; bw[0] = w[0]; bw[1] = w[1]; bw[2] = w[2]; }
+        }
+        const double tot = bw[0] + bw[1] + bw[2];
+        const double fi = fmin(fmax(bw[1] / tot, 0.0), 1.0) * k, fj = fmin(fmax(bw[2] / tot, 0.0), 1.0) * k;
+        int i0 = (int)floor(fi), j0 = (int)floor(fj);
+        if (i0 > k - 1) i0 = k - 1;
+        if (i0 < 0) i0 = 0;
+        if (j0 > k - 1 - i0) j0 = k - 1 - i0;
+        if (j0 < 0) j0 = 0;
+        const bool up = (fi - i0) + (fj - j0) <= 1.0 || i0 + j0 == k - 1;
+        int32_t tri[3];
+        if (up) {
+            tri[0] = face_vid(bf, i0, j0, k); tri[1] = face_vid(bf, i0 + 1, j0, k); tri[2] = face_vid(bf, i0, j0 + 1, k);
+        } else {
+            tri[0] = face_vid(bf, i0 + 1, j0, k); tri[1] = face_vid(bf, i0 + 1, j0 + 1, k);
+            tri[2] = face_vid(bf, i0, j0 + 1, k);
+        }
+        double bd[3] = {INFINITY, INFINITY, INFINITY};
+        int64_t bi[3] = {-1, -1, -1};
+        for (int c = 0; c < 21; ++c) {
+            const int32_t v = c < 3 ? tri[c] : nbr[6 * (int64_t)tri[(c - 3) / 6] + (c - 3) % 6];
+            if (v < 0 || (int64_t)v >= nv) continue;
+            if (v == bi[0] || v == bi[1] || v == bi[2]) continue;
+            const double dx = __dsub_rn(qx, xyz[3 * (int64_t)v]), dy = __dsub_rn(qy, xyz[3 * (int64_t)v + 1]),
+                         dz = __dsub_rn(qz, xyz[3 * (int64_t)v + 2]);
+            const double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            int m = 3;
+            while (m > 0 && (d < bd[m - 1] || (d == bd[m - 1] && v < bi[m - 1]))) --m;
+            if (m < 3) {
+                for (int r = 2; r > m; --r) { bd[r] = bd[r - 1]; bi[r] = bi[r - 1]; }
+                bd[m] = d;
+                bi[m] = v;
+            }
+        }
+        for (int m = 0; m < 3; ++m) {
+            dist[3 * p + m] = bd[m];
+            idx[3 * p + m] = bi[m];
+        }
+    }
+}
+
+}  // namespace
+
+NX_EXPORT int nx_nearest3(int k, const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, const double *q_dev,
+                          int64_t nq, double *dist_dev, int64_t *idx_dev, void *stream)
+{
+    if (k < 1 || nv != 10 * (int64_t)k * k + 2 || nq < 0) return nx::fail(NX_EINVAL, "nx_nearest3: bad sizes");
+    if (nq == 0) return NX_OK;
+    if (!xyz_dev || !nbr_dev || !q_dev || !dist_dev || !idx_dev) return nx::fail(NX_EINVAL, "nx_nearest3: null pointer");
+    int dev = 0;
+    NX_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !g_tables_ready[dev]) return nx::fail(NX_EINVAL, "nx_nearest3: icosphere tables not set");
+    nearest3_kernel<<<grid1d(nq), 256, 0, (cudaStream_t)stream>>>(k, xyz_dev, nbr_dev, nv, q_dev, nq, dist_dev, idx_dev);
+    NX_CHECK_LAUNCH("nearest3_kernel");
+    nx::note_launch(1);
     return NX_OK;
 }

@@ -5,6 +5,8 @@ State on the GPU is binary32 pairs (hi + lo) with a per-planet power-of-two
 scale (exact, see csrc/nx_erosion.cu); results are returned in the reference's float64
 arrays, updated in place like the reference.
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -39,7 +41,7 @@ class ErosionRun:
         self.st = torch.empty((n, 8), dtype=torch.float32, device="cuda")    # (h, w, s as hi/lo pairs, 0, 0)
         self.st_tmp = torch.empty_like(self.st)
         self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
-        self.planet = torch.zeros(8, dtype=torch.int64, device="cuda")   # one nx_erosion_planet (40 B)
+        self.planet = torch.zeros(ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device="cuda")  # one descriptor
         self.iters_done = 0
 
     def load(self, heights, water=None, sediment=None):

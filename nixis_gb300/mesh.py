@@ -60,11 +60,8 @@ def create_mesh(divisions):
     return xyz.cpu().numpy(), tris.cpu().numpy()
 
 
-def build_adjacency(triangles, stream=None):
-    """util.build_adjacency: (N,6) int32 neighbour rows in triangle order,
-    -1 padded (CUDA tensor; numpy in -> numpy out)."""
-    host = _dev.is_host(triangles)
-    t = _dev.to_device(triangles, np.int32, name="triangles")
+def _adjacency(t, stream=None):
+    """Launch build_adjacency; returns (adj, error flags) without waiting."""
     if t.ndim != 2 or t.shape[1] != 3:
         raise ValueError("triangles must have shape (T, 3)")
     nt = t.shape[0]
@@ -74,11 +71,23 @@ def build_adjacency(triangles, stream=None):
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     call("nx_build_adjacency", _dev.ptr(t), nt, nv, _dev.ptr(adj), _dev.ptr(ws), ws.numel(), _dev.ptr(err),
          _dev.stream_handle(stream))
-    e = int(err.item())
+    return adj, err
+
+
+def _check_adjacency(e):
     if e & 1:
         raise ValueError("build_adjacency: a triangle references a vertex id outside [0, (T+4)/2)")
     if e & 2:
         raise ValueError("build_adjacency: a vertex has more than 6 neighbours")
+
+
+def build_adjacency(triangles, stream=None):
+    """util.build_adjacency: (N,6) int32 neighbour rows in triangle order,
+    -1 padded (CUDA tensor; numpy in -> numpy out)."""
+    host = _dev.is_host(triangles)
+    t = _dev.to_device(triangles, np.int32, name="triangles")
+    adj, err = _adjacency(t, stream)
+    _check_adjacency(int(err.item()))
     return adj.cpu().numpy() if host else adj
 
 
@@ -112,23 +121,35 @@ def edge_lengths(xyz, nbr, stream=None):
 class PlanetMesh:
     """A subdivision's resident mesh: xyz float64 (N,3), nbr int32 (N,6),
     edge float32 (N,6,2) pairs; triangles are dropped after the adjacency is
-    built."""
+    built.  With defer_checks the build only enqueues work on the stream
+    (no host wait); check() reads the error flags later."""
 
-    def __init__(self, divisions, stream=None):
+    def __init__(self, divisions, stream=None, defer_checks=False):
         self.k = ico.check_divisions(divisions)
         self.n = ico.counts(self.k)[0]
         xyz, tris = icosphere(self.k, stream=stream)
-        adj = build_adjacency(tris, stream=stream)
+        adj, aerr = _adjacency(tris, stream)
         del tris
         nbr = torch.empty_like(adj)
         call("nx_sort_adjacency", _dev.ptr(adj), _dev.ptr(nbr), self.n, _dev.stream_handle(stream))
         del adj
         self.xyz = xyz
         self.nbr = nbr
-        self.edge, err = edge_lengths(xyz, nbr, stream=stream)
-        if int(err.item()):
-            raise RuntimeError("mesh adjacency produced an invalid neighbour id")
+        self.edge, eerr = edge_lengths(xyz, nbr, stream=stream)
+        self._errs = (aerr, eerr)
         self._tilings = {}
+        if not defer_checks:
+            self.check()
+
+    def check(self):
+        """Raise if the adjacency or edge-length kernels flagged an error."""
+        if self._errs is None:
+            return
+        aerr, eerr = (int(e.item()) for e in self._errs)
+        self._errs = None
+        _check_adjacency(aerr)
+        if eerr:
+            raise RuntimeError("mesh adjacency produced an invalid neighbour id")
 
     def tiling(self, tile_side=TILE_SIDE, rings=TILE_RINGS, stream=None):
         """The mesh's tiling for temporally blocked erosion (built once)."""
@@ -153,19 +174,50 @@ class MeshTiling:
         dev = "cuda"
         self.counts = torch.zeros(self.ntiles * (rings + 1), dtype=torch.int32, device=dev)
         self.ids = torch.empty(self.ntiles * self.nmax, dtype=torch.int32, device=dev)
-        self.lnbr = torch.empty(self.ntiles * self.cmax * 6, dtype=torch.int16, device=dev)
+        # (+8: the shared-table kernel copies whole 16-byte units past a tile's last row)
+        self.lnbr = torch.empty(self.ntiles * self.cmax * 6 + 8, dtype=torch.int16, device=dev)
         self.ledge = torch.empty(self.ntiles * self.cmax * 12, dtype=torch.float32, device=dev)
         err = torch.zeros(3, dtype=torch.int32, device=dev)
         call("nx_tiling_build", mesh.k, tile_side, rings, _dev.ptr(mesh.nbr), _dev.ptr(mesh.edge), _dev.ptr(self.counts),
              _dev.ptr(self.ids), _dev.ptr(self.lnbr), _dev.ptr(self.ledge), _dev.ptr(err), _dev.stream_handle(stream))
-        e = err.cpu().numpy()
-        if e[0]:
-            raise RuntimeError(f"tiling of divisions {mesh.k} failed (flags {int(e[0])})")
-        self.maxnl, self.maxc = int(e[1]), int(e[2])
         from ._lib import Tiling
         t = Tiling(self.ntiles, rings, self.nmax, self.cmax, self.counts.data_ptr(), self.ids.data_ptr(),
                    self.lnbr.data_ptr(), self.ledge.data_ptr())
-        self.dev = torch.from_numpy(np.frombuffer(bytes(t), np.uint8).copy()).cuda()
+        # the counts come back and the descriptor goes up without a host wait;
+        # maxnl / maxc wait for them only when first read
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            self._err_host = torch.empty(3, dtype=torch.int32, pin_memory=True)
+            self._err_host.copy_(err, non_blocking=True)
+            self._dev_host = torch.empty(ctypes.sizeof(t), dtype=torch.uint8, pin_memory=True)
+            self._dev_host.numpy()[:] = np.frombuffer(bytes(t), np.uint8)
+            self.dev = self._dev_host.to("cuda", non_blocking=True)
+            self._ready = torch.cuda.Event()
+            self._ready.record(s)
+        self._err = err
+        self._counts = None
+        self.k = mesh.k
+
+    def _resolve(self):
+        if self._counts is None:
+            self._ready.synchronize()
+            e = self._err_host.numpy()
+            if e[0]:
+                raise RuntimeError(f"tiling of divisions {self.k} failed (flags {int(e[0])})")
+            self._counts = (int(e[1]), int(e[2]))
+        return self._counts
+
+    def ready(self):
+        """True once the build's counts are on the host (no wait)."""
+        return self._counts is not None or self._ready.query()
+
+    @property
+    def maxnl(self):
+        return self._resolve()[0]
+
+    @property
+    def maxc(self):
+        return self._resolve()[1]
 
     @property
     def nbytes(self):

@@ -193,6 +193,7 @@ class PlanetBatch:
                 e.tiling = tl.dev.data_ptr()
                 e.ntiles = tl.ntiles
                 e.maxnl = tl.maxnl
+                e.maxc = tl.maxc
         self.fb_host, self.er_host = fb, er
         self.fb_dev = _struct_tensor(fb)
         self.er_dev = _struct_tensor(er)
@@ -326,7 +327,7 @@ class _PlainWork:
             self.st_tmp = torch.empty((n, 8), dtype=torch.float32, device="cuda")
             self.inso = torch.empty(n, dtype=torch.float32, device="cuda")
             self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
-            self.planet = torch.zeros(8, dtype=torch.int64, device="cuda")
+            self.planet = torch.zeros(ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device="cuda")
             self.perm = torch.empty(256, dtype=torch.int32, device="cuda")
             self.pgi = torch.empty(256, dtype=torch.int32, device="cuda")
             self.n = n

@@ -115,7 +115,7 @@ class ResidentMeshes:
                     break
                 self.lru.remove(victim)
                 del self.meshes[victim]
-            self.meshes[k] = _mesh.PlanetMesh(k, stream=stream)
+            self.meshes[k] = _mesh.PlanetMesh(k, stream=stream, defer_checks=True)
             self.lru.append(k)
         else:
             self.lru.remove(k)
@@ -386,6 +386,7 @@ class ServeEngine:
                     arr[q].tiling = t.tiling.dev.data_ptr()
                     arr[q].ntiles = t.tiling.ntiles
                     arr[q].maxnl = t.tiling.maxnl
+                    arr[q].maxc = t.tiling.maxc
             host = _descs_tensor(arr)
             with torch.cuda.stream(self.main):
                 self.desc_dev[:host.numel()].copy_(host, non_blocking=True)
@@ -399,9 +400,11 @@ class ServeEngine:
         if new:
             self.active.extend(new)
             self._launch_new(new)
-        # planets whose noise is done join the erosion at this tick
+        # planets whose mesh, noise and initial state are done join the
+        # erosion at this tick (checked on the host without waiting)
         for t in self.active:
-            if t.stage == "waiting":
+            if t.stage == "waiting" and t.ready_event.query():
+                t.mesh.check()
                 self.main.wait_event(t.ready_event)
                 t.stage = "eroding"
                 t.t_start = self.tick
@@ -443,6 +446,7 @@ class ServeEngine:
         for t in self.active:
             if t.stage == "copying" and t.done_event.query():
                 t.finished = time.perf_counter()
+                t.mesh.check()
                 # results move to ordinary host memory; the page-locked
                 # buffers go back to the caching allocator for later planets
                 t.heights = t.host_h.numpy().copy()

@@ -131,3 +131,83 @@ def shape_heights(height, min_alt=-4000.0, max_alt=8850.0, ocean_percent=55.0, s
     if host:
         return out.cpu().numpy(), mask.cpu().numpy().astype(bool), float(level.item())
     return out, mask.bool(), level
+
+
+# ---------------------------------------------------------------------------
+# Equirectangular maps (util.py:290-366, nixis.py:270-302).  The reference
+# finds each pixel's 3 nearest vertices with a scipy KD-tree; here they come
+# from point location in the icosphere's face grid (exact nearest three;
+# ties in distance go to the lower vertex id, where the KD-tree's order is
+# arbitrary).
+
+def make_ll_arr(width, height, radius, device=False, stream=None):
+    """util.make_ll_arr (util.py:290-310): (height, width, 3) float64 xyz of
+    every pixel's latitude/longitude (numpy, or a CUDA tensor with device)."""
+    _dev.require_cuda()
+    out = torch.empty((int(height), int(width), 3), dtype=torch.float64, device="cuda")
+    call("nx_make_ll", int(width), int(height), float(radius), _dev.ptr(out), _dev.stream_handle(stream))
+    return out if device else out.cpu().numpy()
+
+
+def query_nearest3(verts, neighbors, divisions, queries, stream=None):
+    """The 3 nearest vertices of each query point, as the reference's
+    KDTree(points).query(queries, k=3): (distances, indices), each of shape
+    queries.shape[:-1] + (3,), ascending.  verts / neighbors: an icosphere
+    of `divisions` made by this library (any radius)."""
+    from . import mesh as _m
+    host = _dev.is_host(queries)
+    _m._ensure_tables()
+    xyz = _dev.to_device(verts, np.float64, name="verts")
+    nb = _dev.to_device(neighbors, np.int32, name="neighbors")
+    q = _dev.to_device(queries, np.float64, name="queries")
+    shape = tuple(q.shape[:-1]) + (3,)
+    q = q.reshape(-1, 3)
+    d = torch.empty((q.shape[0], 3), dtype=torch.float64, device="cuda")
+    i = torch.empty((q.shape[0], 3), dtype=torch.int64, device="cuda")
+    call("nx_nearest3", int(divisions), _dev.ptr(xyz), _dev.ptr(nb), xyz.shape[0], _dev.ptr(q), q.shape[0],
+         _dev.ptr(d), _dev.ptr(i), _dev.stream_handle(stream))
+    d, i = d.reshape(shape), i.reshape(shape)
+    return (d.cpu().numpy(), i.cpu().numpy()) if host else (d, i)
+
+
+def _sample(dists, nbrs, colors, stream=None):
+    cd = _dev.to_device(colors, np.float64, name="colors").reshape(-1)
+    d = _dev.to_device(dists, np.float64, name="dists").reshape(-1, 3)
+    i = _dev.to_device(nbrs, np.int64, name="nbrs").reshape(-1, 3)
+    out = torch.empty(d.shape[0], dtype=torch.float64, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("nx_sample_gray", _dev.ptr(d), _dev.ptr(i), d.shape[0], _dev.ptr(cd), cd.numel(), _dev.ptr(out), _dev.ptr(err),
+         _dev.stream_handle(stream))
+    if int(err.item()):
+        raise IndexError("nbrs holds an index outside the colours")
+    return out
+
+
+def _as_dtype(values, like):
+    dt = like.dtype if isinstance(like, np.ndarray) else np.dtype(str(like.dtype).replace("torch.", ""))
+    return values.astype(dt)
+
+
+def make_gray_array(width, height, dists, nbrs, colors):
+    """util.make_gray_array (util.py:342-366): per pixel the inverse-distance
+    weighting of its 3 neighbours' colours, truncated to an integer and
+    returned in the colours' dtype, shape (height, width)."""
+    v = _sample(dists, nbrs, colors).cpu().numpy().reshape(int(height), int(width))
+    return _as_dtype(v, colors)
+
+
+def make_rgb_array(width, height, dists, nbrs, colors):
+    """util.make_rgb_array (util.py:312-340): the same value in 3 channels,
+    shape (height, width, 3)."""
+    g = make_gray_array(width, height, dists, nbrs, colors)
+    return np.repeat(g[:, :, None], 3, axis=2)
+
+
+def equirect_map(verts, neighbors, divisions, colors, width, height, radius, stream=None):
+    """A whole map on the GPU: pixel positions, nearest three vertices, and
+    the gray weighting of `colors` (the reference's make_ll_arr + KD-tree
+    query + make_gray_array); returns (height, width) in the colours' dtype."""
+    ll = make_ll_arr(width, height, radius, device=True, stream=stream)
+    d, i = query_nearest3(verts, neighbors, divisions, ll, stream=stream)
+    v = _sample(d, i, colors, stream=stream).cpu().numpy().reshape(int(height), int(width))
+    return _as_dtype(v, colors)

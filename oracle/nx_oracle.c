@@ -746,6 +746,61 @@ NXO_API void nxo_calc_yearly_insolation(const double *xyz, int64_t n, double rad
     free(tab);
 }
 
+/* util.py:290-310 (make_ll_arr): pixel (h, w) of a width x height map at
+ * latitude max(90 - h*180/(height-1), -90), longitude max(-180 + w*360/width,
+ * -180), as xyz on the sphere of the radius. */
+NXO_API void nxo_make_ll(int width, int height, double radius, double *out)
+{
+    const double latpercent = 180.0 / (double)(height - 1), lonpercent = 360.0 / (double)width;
+    for (int h = 0; h < height; ++h)
+        for (int w = 0; w < width; ++w) {
+            double lat = 90.0 - ((double)h * latpercent), lon = -180.0 + ((double)w * lonpercent);
+            if (lat < -90.0) lat = -90.0;
+            if (lon < -180.0) lon = -180.0;
+            latlon2xyz(lat, lon, radius, out + 3 * ((int64_t)h * width + w));
+        }
+}
+
+/* The 3 nearest vertices of each query point, by brute force (the exact
+ * answer the reference's KD-tree query(k=3) gives, nixis.py:278-283):
+ * distances sqrt((dx*dx + dy*dy) + dz*dz) ascending, ties by index. */
+NXO_API void nxo_nearest3(const double *xyz, int64_t nv, const double *q, int64_t nq, double *dist, int64_t *idx)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < nq; ++p) {
+        double bd[3] = {INFINITY, INFINITY, INFINITY};
+        int64_t bi[3] = {-1, -1, -1};
+        for (int64_t v = 0; v < nv; ++v) {
+            const double dx = q[3 * p] - xyz[3 * v], dy = q[3 * p + 1] - xyz[3 * v + 1], dz = q[3 * p + 2] - xyz[3 * v + 2];
+            const double d = sqrt((dx * dx + dy * dy) + dz * dz);
+            int k = 3;
+            while (k > 0 && (d < bd[k - 1] || (d == bd[k - 1] && v < bi[k - 1]))) --k;
+            if (k < 3) {
+                for (int m = 2; m > k; --m) { bd[m] = bd[m - 1]; bi[m] = bi[m - 1]; }
+                bd[k] = d;
+                bi[k] = v;
+            }
+        }
+        for (int k = 0; k < 3; ++k) { dist[3 * p + k] = bd[k]; idx[3 * p + k] = bi[k]; }
+    }
+}
+
+/* util.py:342-366 (make_gray_array) per pixel: weights 1 / ((d + 1e-5) / sum d),
+ * normalised, the weighted sum of the 3 colours truncated toward zero. */
+NXO_API void nxo_make_gray(const double *dist, const int64_t *idx, int64_t npix, const double *colors, double *out)
+{
+    for (int64_t p = 0; p < npix; ++p) {
+        const double *d = dist + 3 * p;
+        const double sd = (d[0] + d[1]) + d[2];
+        double ws[3];
+        for (int k = 0; k < 3; ++k) ws[k] = 1 / ((d[k] + 0.00001) / sd);
+        const double t = (ws[0] + ws[1]) + ws[2];
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc += colors[idx[3 * p + k]] * (ws[k] / t);
+        out[p] = trunc(acc);
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Mesh adjacency and scalar helpers                                          */
 /* ------------------------------------------------------------------------ */

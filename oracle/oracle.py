@@ -63,6 +63,9 @@ def lib():
             "nxo_calc_insolation_slice": (None, [_d, _d, _p]),
             "nxo_interpolate_insolation": (None, [_p, _i64, _p, _p, _d]),
             "nxo_calc_yearly_insolation": (None, [_p, _i64, _d, _d, _p]),
+            "nxo_make_ll": (None, [ctypes.c_int, ctypes.c_int, _d, _p]),
+            "nxo_nearest3": (None, [_p, _i64, _p, _i64, _p, _p]),
+            "nxo_make_gray": (None, [_p, _p, _i64, _p, _p]),
             "nxo_num_threads": (_i32, []),
             "nxo_icosphere": (_i32, [_i32, _p, _p, _p, _p, _p, _p]),
         }
@@ -310,6 +313,32 @@ def calc_yearly_insolation(verts, radius, axial_tilt):
     out = np.empty(len(v), np.float32)
     lib().nxo_calc_yearly_insolation(_ptr(v), len(v), float(radius), float(axial_tilt), _ptr(out))
     return out
+
+
+def make_ll_arr(width, height, radius):
+    out = np.empty((height, width, 3), np.float64)
+    lib().nxo_make_ll(int(width), int(height), float(radius), _ptr(out))
+    return out
+
+
+def nearest3(verts, queries):
+    """(dists (..., 3), indices (..., 3)) of the 3 nearest vertices, exact."""
+    v = _c(verts, np.float64)
+    q = _c(np.asarray(queries, np.float64).reshape(-1, 3), np.float64)
+    d = np.empty((len(q), 3), np.float64)
+    i = np.empty((len(q), 3), np.int64)
+    lib().nxo_nearest3(_ptr(v), len(v), _ptr(q), len(q), _ptr(d), _ptr(i))
+    shape = np.asarray(queries).shape[:-1] + (3,)
+    return d.reshape(shape), i.reshape(shape)
+
+
+def make_gray_array(width, height, dists, nbrs, colors):
+    d = _c(np.asarray(dists, np.float64).reshape(-1, 3), np.float64)
+    n = _c(np.asarray(nbrs, np.int64).reshape(-1, 3), np.int64)
+    c = _c(colors, np.float64)
+    out = np.empty(len(d), np.float64)
+    lib().nxo_make_gray(_ptr(d), _ptr(n), len(d), _ptr(c), _ptr(out))
+    return out.reshape(height, width)
 
 
 def icosphere(k, with_tris=True):

@@ -11,7 +11,8 @@ erosion.erosion_iteration3 / erode_terrain3 / find_lowest,
 climate.sample_insolation / brute_daily_insolation / calculate_seasonal_tilt /
 day2deg, util.build_adjacency / sort_adjacency / rescale / power_rescale /
 find_percent_val, terrain.make_bool_elevation_mask, climate.calc_insolation_slice /
-interpolate_insolation / calc_daily_insolation / calc_yearly_insolation) imported through
+interpolate_insolation / calc_daily_insolation / calc_yearly_insolation,
+util.make_ll_arr / make_gray_array with scipy's KDTree query) imported through
 ref_shim.  `python tests/golden/make_golden.py shaping` regenerates one set.  Inputs are seeded; meshes come from tests/meshref.py (the same
 construction as the GPU generator).
 """
@@ -301,9 +302,32 @@ def gen_lut_insolation(R):
     np.savez_compressed(os.path.join(HERE, "lut_insolation.npz"), **out)
 
 
+def gen_image(R):
+    """Equirectangular map sampling (util.py:290-367, nixis.py:270-302):
+    make_ll_arr's pixel positions, the 3 nearest vertices of each pixel from
+    scipy's KD-tree (as build_KDTree + query(k=3)), and make_gray_array's
+    inverse-distance weighting of rescaled heights."""
+    from scipy.spatial import KDTree
+    util, ter, osi = R.util, R.terrain, R.opensimplex
+    out = {}
+    pts, _ = meshref.icosphere(16)
+    radius = 2.5
+    pts = pts * radius
+    perm, pgi = osi.init(21)
+    h = np.asarray(quiet(ter.sample_octaves, pts / radius, None, perm, pgi, 6, 1.0, 1.0, 2.0, 0.5, 1.0), np.float64)
+    colors = np.asarray(util.rescale(h, 0, 255), np.float64)
+    W, H = 64, 32
+    ll = np.asarray(util.make_ll_arr(W, H, radius), np.float64)
+    dists, nbrs = KDTree(pts, leafsize=10).query(ll, k=3)
+    gray = np.asarray(util.make_gray_array(W, H, dists, nbrs, colors))
+    out.update(radius=np.array([radius]), heights=h, colors=colors, ll=ll, dists=np.asarray(dists),
+               nbrs=np.asarray(nbrs, np.int64), gray=gray, wh=np.array([W, H]))
+    np.savez_compressed(os.path.join(HERE, "image.npz"), **out)
+
+
 GENERATORS = {"perm": gen_perm, "noise": gen_noise, "octaves": gen_octaves, "mesh_erosion": gen_mesh_erosion,
               "insolation": gen_insolation, "shaping": gen_shaping,
-              "lut_insolation": gen_lut_insolation}
+              "lut_insolation": gen_lut_insolation, "image": gen_image}
 
 
 def main():

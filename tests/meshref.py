@@ -102,3 +102,13 @@ def edge_lengths(pts, adj):
         out[:, k, 0] = hi
         out[:, k, 1] = (dist - hi.astype(np.float64)).astype(np.float32)
     return out
+
+
+def tied_pixels(pts, ll):
+    """Query points among whose 4 nearest vertices two are exactly as far
+    (there a KD-tree's choice and order are arbitrary)."""
+    q = np.asarray(ll, np.float64).reshape(-1, 3)
+    d = np.sqrt(((q[:, None, 0] - pts[None, :, 0]) ** 2 + (q[:, None, 1] - pts[None, :, 1]) ** 2)
+                + (q[:, None, 2] - pts[None, :, 2]) ** 2)
+    s = np.sort(d, axis=1)[:, :4]
+    return (s[:, 1:] == s[:, :-1]).any(axis=1).reshape(np.asarray(ll).shape[:-1])

@@ -50,3 +50,12 @@ def test_error_reporting_without_gpu_work():
     assert rc == 1
     assert b"null" in L.nx_last_error()
     assert L.nx_version() >= 10000
+
+
+def test_descriptor_layouts_match_the_header():
+    """The ctypes mirrors of the C structs have the header's sizes (the C
+    side asserts the same sizes at compile time)."""
+    from nixis_gb300 import _lib
+    assert ctypes.sizeof(_lib.ErosionPlanet) == 72
+    assert ctypes.sizeof(_lib.Tiling) == 48
+    assert _lib.ErosionPlanet.maxc.offset == 64

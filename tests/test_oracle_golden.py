@@ -145,6 +145,25 @@ def test_lut_insolation_bit_exact():
     assert np.array_equal(O.calc_yearly_insolation(p4, 1.0, 23.44), g["yearly_k4_t23"])
 
 
+def test_image_sampling_matches_reference():
+    """make_ll_arr, the 3 nearest vertices (equal to scipy's KD-tree except
+    where two candidates are exactly as far: the KD-tree's order among ties
+    is arbitrary) and make_gray_array (util.py:290-366)."""
+    g = golden_io.load("image")
+    (W, H), r = g["wh"], g["radius"][0]
+    assert np.array_equal(O.make_ll_arr(W, H, r), g["ll"])
+    pts, _ = meshref.icosphere(16)
+    d, i = O.nearest3(pts * r, g["ll"])
+    assert np.array_equal(d, g["dists"])
+    tie = tied_pixels(pts * r, g["ll"])
+    assert np.array_equal(i[~tie], g["nbrs"][~tie])
+    assert np.array_equal(O.make_gray_array(W, H, g["dists"], g["nbrs"], g["colors"]), g["gray"])
+
+
+def tied_pixels(pts, ll):
+    return meshref.tied_pixels(pts, ll)
+
+
 def test_find_lowest_matches_reference():
     g = golden_io.load("mesh_erosion")
     adj = g["adj_k6"]

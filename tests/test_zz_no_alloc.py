@@ -32,7 +32,7 @@ def _allocating(m, st, iters, rain):
     st = st.clone()
     tmp = torch.empty_like(st)
     ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
-    pd = torch.zeros(8, dtype=torch.int64, device="cuda")
+    pd = torch.zeros(ctypes.sizeof(_lib.ErosionPlanet), dtype=torch.uint8, device="cuda")
     mass = torch.empty((max(iters, 1), 3), dtype=torch.float64, device="cuda")
     _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), 1, _dev.stream_handle())
     _lib.call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(st), _dev.ptr(tmp), iters,
