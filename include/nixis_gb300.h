@@ -309,7 +309,9 @@ int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *
  * memory each iteration (256, 512 or 1024 threads); 1: the same with the
  * next vertex's entries loaded ahead (256 or 384); 2: the tile's tables
  * copied to shared memory once per pass (512 or 1024; needs maxc in the
- * planet descriptors) -- and whether batches with tilings use it (1) or
+ * planet descriptors); 3: one vertex per thread, its table row held in
+ * registers for the pass (512 or 1024; every tile's updatable count maxc
+ * must fit the block) -- and whether batches with tilings use it (1) or
  * run one iteration per launch (0).  The autotuner (nixis_gb300.autotune)
  * picks these and the tile side per device. */
 int nx_erosion_tb_config(int rings, int threads, int variant, int enabled);

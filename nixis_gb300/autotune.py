@@ -9,7 +9,9 @@ variant: 0 reads the tile tables (neighbour indices, edge lengths) from
 global memory every iteration, 1 loads the next vertex's entries ahead of
 computing the current one (hides their latency, costs registers and so
 resident threads), 2 copies the tile's tables to shared memory once per
-pass (no per-iteration global reads, but more shared memory per block).  ``tune`` times
+pass (no per-iteration global reads, but more shared memory per block), 3
+runs one vertex per thread with its table row held in registers for the
+pass (small tiles only: every tile's updatable vertices must fit the block).  ``tune`` times
 every candidate on a synthetic planet, checks that all of them give the
 same heights bit for bit (they run the same per-vertex arithmetic), keeps
 the fastest and caches it per device in a JSON file
@@ -30,13 +32,13 @@ from ._lib import NxError, call, lib
 SMEM_LIMIT = 200 * 1024          # dynamic shared memory of variants 0 and 1
 SMEM_LIMIT_TABLES = 226 * 1024   # of variant 2 (the opt-in limit less static shared memory, rounded down)
 ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
-SIDES = (24, 28, 32, 40, 48)
+SIDES = (16, 20, 24, 28, 32, 40, 48)
 RINGS = (2, 3, 4, 5)
-THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2))
+THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2), (512, 3), (1024, 3))
 # variant 2 measured slower on GB300 for every tile size (one block per SM
 # cannot overlap its load phase with compute): tried only on request
-DEFAULT_VARIANTS = (0, 1)
-SUFFIX = {0: "", 1: "p", 2: "s"}
+DEFAULT_VARIANTS = (0, 1, 3)
+SUFFIX = {0: "", 1: "p", 2: "s", 3: "o"}
 
 
 @dataclass(frozen=True)
@@ -61,6 +63,8 @@ def smem_bytes(cfg, maxnl, maxc):
 
 
 def fits(cfg, maxnl, maxc):
+    if cfg.variant == 3 and maxc > cfg.threads:
+        return False
     return smem_bytes(cfg, maxnl, maxc) <= (SMEM_LIMIT_TABLES if cfg.variant == 2 else SMEM_LIMIT)
 
 
@@ -121,10 +125,11 @@ def store(key, cfg, timings=None, path=None):
 
 def parse(label):
     """TbConfig from its label side/rings/threads, 'p' appended for variant
-    1 (prefetch), 's' for variant 2 (tables in shared memory)."""
+    1 (prefetch), 's' for variant 2 (tables in shared memory), 'o' for
+    variant 3 (one vertex per thread)."""
     side, rings, thr = label.split("/")
-    v = 1 if thr.endswith("p") else (2 if thr.endswith("s") else 0)
-    return TbConfig(int(side), int(rings), int(thr.rstrip("ps")), v)
+    v = {"p": 1, "s": 2, "o": 3}.get(thr[-1], 0)
+    return TbConfig(int(side), int(rings), int(thr.rstrip("pso")), v)
 
 
 def current():

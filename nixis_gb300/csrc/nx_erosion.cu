@@ -147,7 +147,9 @@ __device__ __forceinline__ unsigned erode_accum(float hh, float hl, float4 o, fl
 
 // erosion.py:261-267 from the accumulated S and W: sed = s + sol*S,
 // h -= sed, s += sed, w = w_i + W*(1 - evap), then the capacity test.
-// wi is the vertex's water including this iteration's rain.
+// wi is the vertex's water including this iteration's rain.  (Evaluating
+// these in paired lanes measured slower: assembling the lane pairs costs
+// more instructions than it saves.)
 __device__ __forceinline__ void erode_finish(Pair hi, Pair wi, Pair si, float2 A, float2 L, Pair &hn, Pair &wn,
                                              Pair &sn)
 {
@@ -407,13 +409,40 @@ __device__ __forceinline__ TileRow tile_row(const uint32_t *lnb, const float4 *l
     return r;
 }
 
+// One vertex of a pass iteration: its row of the tile tables, the state
+// rows `cur` (read) and `nxt` (written), its sediment pair in place.
+__device__ __forceinline__ void tb_update(int l, const TileRow &row, const float4 *cur, float4 *nxt, float2 *sed,
+                                          float rain, bool more)
+{
+    const float4 me = cur[l];
+    const float2 ms = sed[l];
+    float2 A = make_float2(0.0f, me.z), L = make_float2(0.0f, me.w);
+    const uint32_t nb[6] = {row.p01 & 0xFFFFu, row.p01 >> 16, row.p23 & 0xFFFFu, row.p23 >> 16,
+                            row.p45 & 0xFFFFu, row.p45 >> 16};
+    const float dh[6] = {row.d01.x, row.d01.z, row.d23.x, row.d23.z, row.d45.x, row.d45.z};
+    const float dl[6] = {row.d01.y, row.d01.w, row.d23.y, row.d23.w, row.d45.y, row.d45.w};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        // a missing neighbour (pentagon slot) is stored as the vertex itself:
+        // equal heights contribute nothing, as the reference's skip of -1
+        erode_accum(me.x, me.y, cur[nb[k]], dh[k], dl[k], A, L);
+    }
+    Pair hn, wn, sn;
+    erode_finish(Pair{me.x, me.y}, Pair{me.z, me.w}, Pair{ms.x, ms.y}, A, L, hn, wn, sn);
+    const Pair wr = more ? prain(wn.h, wn.l, rain) : wn;
+    nxt[l] = make_float4(hn.h, hn.l, wr.h, wr.l);
+    sed[l] = make_float2(sn.h, sn.l);
+}
+
 // PF: software-pipelined table reads (the next vertex's entries are loaded
 // before the current vertex is computed; ~80 registers, so 768 threads per
 // SM); otherwise each vertex loads its own entries (64 registers, 1024
 // threads per SM).  SMT: the tile's tables are copied to shared memory once
 // per pass (with the state) and every iteration of the pass reads them
-// there.
-template <int THREADS, bool PF, bool SMT = false>
+// there.  ONE: one vertex per thread (tiles whose updatable count fits the
+// block); each thread loads its table row once per pass into registers, so
+// the iterations of the pass make no global reads.
+template <int THREADS, bool PF, bool SMT = false, bool ONE = false>
 __global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_tb_kernel(TbArgs a)
 {
     extern __shared__ float4 tsm4[];
@@ -471,6 +500,14 @@ __global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_
         led = sled;
         lnb = reinterpret_cast<const uint32_t *>(slnb);
     }
+    TileRow myrow;
+    if (ONE) {
+        if (C0 > THREADS) {                      // tile too large for one vertex per thread
+            if (threadIdx.x == 0) c->err = 3;
+            return;
+        }
+        if ((int)threadIdx.x < C0) myrow = tile_row<false>(lnb, led, threadIdx.x);
+    }
     for (int l = threadIdx.x; l < NL; l += blockDim.x) {
         const int64_t row = P.vbeg + ids[l];
         const float4 x = ist[2 * row];
@@ -485,36 +522,21 @@ __global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_
         const float4 *cur = (mi & 1) ? buf1 : buf0;
         float4 *nxt = (mi & 1) ? buf0 : buf1;
         const bool more = mi + 1 < len;          // rain for the next iteration in the pass
-        TileRow nextrow;
-        if (PF && (int)threadIdx.x < C) nextrow = tile_row<SMT>(lnb, led, threadIdx.x);
-        for (int l = threadIdx.x; l < C; l += THREADS) {
-            TileRow row;
-            if (PF) {
-                row = nextrow;
-                if (l + THREADS < C) nextrow = tile_row<SMT>(lnb, led, l + THREADS);
-            } else {
-                row = tile_row<SMT>(lnb, led, l);
+        if (ONE) {
+            if ((int)threadIdx.x < C) tb_update(threadIdx.x, myrow, cur, nxt, sed, rain, more);
+        } else {
+            TileRow nextrow;
+            if (PF && (int)threadIdx.x < C) nextrow = tile_row<SMT>(lnb, led, threadIdx.x);
+            for (int l = threadIdx.x; l < C; l += THREADS) {
+                TileRow row;
+                if (PF) {
+                    row = nextrow;
+                    if (l + THREADS < C) nextrow = tile_row<SMT>(lnb, led, l + THREADS);
+                } else {
+                    row = tile_row<SMT>(lnb, led, l);
+                }
+                tb_update(l, row, cur, nxt, sed, rain, more);
             }
-            const uint32_t p01 = row.p01, p23 = row.p23, p45 = row.p45;
-            const float4 d01 = row.d01, d23 = row.d23, d45 = row.d45;
-            const float4 me = cur[l];
-            const float2 ms = sed[l];
-            float2 A = make_float2(0.0f, me.z), L = make_float2(0.0f, me.w);
-            const uint32_t nb[6] = {p01 & 0xFFFFu, p01 >> 16, p23 & 0xFFFFu, p23 >> 16, p45 & 0xFFFFu, p45 >> 16};
-            const float dh[6] = {d01.x, d01.z, d23.x, d23.z, d45.x, d45.z};
-            const float dl[6] = {d01.y, d01.w, d23.y, d23.w, d45.y, d45.w};
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                // a missing neighbour (pentagon slot) is stored as the vertex
-                // itself: equal heights contribute nothing, as the reference's
-                // skip of -1
-                erode_accum(me.x, me.y, cur[nb[k]], dh[k], dl[k], A, L);
-            }
-            Pair hn, wn, sn;
-            erode_finish(Pair{me.x, me.y}, Pair{me.z, me.w}, Pair{ms.x, ms.y}, A, L, hn, wn, sn);
-            const Pair wr = more ? prain(wn.h, wn.l, rain) : wn;
-            nxt[l] = make_float4(hn.h, hn.l, wr.h, wr.l);
-            sed[l] = make_float2(sn.h, sn.l);
         }
         __syncthreads();
         if (more) C -= cnt[len - 1 - mi];
@@ -811,7 +833,7 @@ NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int variant, int enab
 {
     if (rings < 1 || rings > 8) return nx::fail(NX_EINVAL, "nx_erosion_tb_config: rings must be in [1, 8]");
     const bool ok = variant == 1 ? (threads == 256 || threads == 384)
-                  : variant == 2 ? (threads == 512 || threads == 1024)
+                  : (variant == 2 || variant == 3) ? (threads == 512 || threads == 1024)
                   : variant == 0 ? (threads == 256 || threads == 512 || threads == 1024) : false;
     if (!ok)
         return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads %d do not go with variant %d", threads, variant);
@@ -838,6 +860,9 @@ static cudaError_t launch_tb(int64_t grid, size_t smem, cudaStream_t s, const Tb
     } else if (g_tb_variant == 2) {
         if (g_tb_threads == 512) erosion_tb_kernel<512, false, true><<<(unsigned)grid, 512, smem, s>>>(ta);
         else erosion_tb_kernel<1024, false, true><<<(unsigned)grid, 1024, smem, s>>>(ta);
+    } else if (g_tb_variant == 3) {
+        if (g_tb_threads == 512) erosion_tb_kernel<512, false, false, true><<<(unsigned)grid, 512, smem, s>>>(ta);
+        else erosion_tb_kernel<1024, false, false, true><<<(unsigned)grid, 1024, smem, s>>>(ta);
     } else {
         switch (g_tb_threads) {
         case 256: erosion_tb_kernel<256, false><<<(unsigned)grid, 256, smem, s>>>(ta); break;
@@ -862,6 +887,10 @@ static int tb_prepare()
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<512, false, false, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024, false, false, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<384, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         int optin = 0;
         NX_CHECK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -913,8 +942,12 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
             continue;
         }
         if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0) { tb = false; break; }
-        if (g_tb_variant == 2 && P.maxc <= 0)
-            return nx::fail(NX_EINVAL, "erosion: planet %d has no maxc (needed by blocked-kernel variant 2)", p);
+        if (g_tb_variant >= 2 && P.maxc <= 0)
+            return nx::fail(NX_EINVAL, "erosion: planet %d has no maxc (needed by blocked-kernel variant %d)", p,
+                            g_tb_variant);
+        if (g_tb_variant == 3 && P.maxc > g_tb_threads)
+            return nx::fail(NX_EINVAL, "erosion: planet %d: tiles of %d updatable vertices exceed %d threads (variant 3)",
+                            p, P.maxc, g_tb_threads);
         ntiles_all += P.ntiles;
         if (P.maxnl > maxnl) maxnl = P.maxnl;
         if (P.maxc > maxc) maxc = P.maxc;
@@ -1078,8 +1111,11 @@ NX_EXPORT int nx_erosion_passes(const nx_erosion_planet *planets_dev, const nx_e
             return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d: bad descriptor", p);
         if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0)
             return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d has no tiling", p);
-        if (g_tb_variant == 2 && P.maxc <= 0)
-            return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d has no maxc (needed by variant 2)", p);
+        if (g_tb_variant >= 2 && P.maxc <= 0)
+            return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d has no maxc (needed by variant %d)", p, g_tb_variant);
+        if (g_tb_variant == 3 && P.maxc > g_tb_threads)
+            return nx::fail(NX_EINVAL, "nx_erosion_passes: planet %d: tiles exceed %d threads (variant 3)", p,
+                            g_tb_threads);
         ntiles += P.ntiles;
         if (P.maxnl > maxnl) maxnl = P.maxnl;
         if (P.maxc > maxc) maxc = P.maxc;

@@ -240,8 +240,26 @@ __global__ void adj_sort_kernel(int64_t nv, const int32_t *__restrict__ in, int3
     }
 }
 
+__device__ __forceinline__ double edge_len(const double *xyz, int64_t v, int64_t j)
+{
+    const double dx = __dsub_rn(xyz[3 * v], xyz[3 * j]);
+    const double dy = __dsub_rn(xyz[3 * v + 1], xyz[3 * j + 1]);
+    const double dz = __dsub_rn(xyz[3 * v + 2], xyz[3 * j + 2]);
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+__device__ __forceinline__ float2 edge_pair(double d)
+{
+    const float hi = (float)d;
+    return make_float2(hi, (float)(d - (double)hi));
+}
+
 // erosion.py:38-40 in binary64 (squares by multiplication), split into a
-// pair hi + lo of binary32s: el[2q] = hi, el[2q+1] = lo.
+// pair hi + lo of binary32s: el[2q] = hi, el[2q+1] = lo.  |v_i - v_j| and
+// |v_j - v_i| are the same number (the differences only change sign), so
+// the binary64 square root -- slow at GB300's binary64 rate -- is taken once
+// per edge: this pass fills the slots whose neighbour has the larger id,
+// edge_mirror_kernel copies them into the reverse slots.
 __global__ void edge_len_kernel(const double *__restrict__ xyz, const int32_t *__restrict__ nbr, int64_t nv,
                                 float2 *__restrict__ el, int *__restrict__ err)
 {
@@ -249,16 +267,29 @@ __global__ void edge_len_kernel(const double *__restrict__ xyz, const int32_t *_
         int64_t v = q / 6;
         int32_t j = nbr[q];
         double d = 0.0;
+        if (j >= 0 && (int64_t)j < nv && (int64_t)j < v) continue;     // the mirror pass fills it
         if (j >= 0 && (int64_t)j < nv) {
-            double dx = __dsub_rn(xyz[3 * v], xyz[3 * (int64_t)j]);
-            double dy = __dsub_rn(xyz[3 * v + 1], xyz[3 * (int64_t)j + 1]);
-            double dz = __dsub_rn(xyz[3 * v + 2], xyz[3 * (int64_t)j + 2]);
-            d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            d = edge_len(xyz, v, j);
         } else if (j != -1 && err) {
             atomicOr(err, 1);
         }
-        const float hi = (float)d;
-        el[q] = make_float2(hi, (float)(d - (double)hi));
+        el[q] = edge_pair(d);
+    }
+}
+
+// Slots whose neighbour j has the smaller id take the pair of j's slot that
+// points back; a table that is not symmetric gets the distance computed.
+__global__ void edge_mirror_kernel(const double *__restrict__ xyz, const int32_t *__restrict__ nbr, int64_t nv,
+                                   float2 *__restrict__ el)
+{
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 6 * nv; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = q / 6;
+        const int32_t j = nbr[q];
+        if (j < 0 || (int64_t)j >= nv || (int64_t)j >= v) continue;
+        int m = -1;
+        for (int s = 0; s < 6; ++s)
+            if (nbr[6 * (int64_t)j + s] == (int32_t)v) { m = s; break; }
+        el[q] = m >= 0 ? el[6 * (int64_t)j + m] : edge_pair(edge_len(xyz, v, j));
     }
 }
 
@@ -405,6 +436,9 @@ NX_EXPORT int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int
     if (!xyz_dev || !nbr_dev || !edge_dev) return nx::fail(NX_EINVAL, "nx_edge_lengths: null pointer");
     edge_len_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, (float2 *)edge_dev, err_dev);
     NX_CHECK_LAUNCH("edge_len_kernel");
+    edge_mirror_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, (float2 *)edge_dev);
+    NX_CHECK_LAUNCH("edge_mirror_kernel");
+    nx::note_launch(1);
     nx::note_launch(1);
     return NX_OK;
 }

@@ -15,7 +15,7 @@ def test_cache_round_trip_and_bad_entries(tmp_path):
     assert A.lookup("gpuX", p) == A.TbConfig(48, 3, 256)
     assert A.lookup("gpuY", p) == A.TbConfig(32, 5, 384, 1)
     assert A.parse("32/5/384p") == A.TbConfig(32, 5, 384, 1) and A.parse("40/4/512") == A.DEFAULT
-    assert A.parse("24/4/512s") == A.TbConfig(24, 4, 512, 2)
+    assert A.parse("24/4/512s") == A.TbConfig(24, 4, 512, 2) and A.parse("16/3/1024o") == A.TbConfig(16, 3, 1024, 3)
     assert A.parse(A.TbConfig(48, 2, 1024).label) == A.TbConfig(48, 2, 1024)
     with open(p) as f:
         assert json.load(f)["gpuX"]["timings_ms"] == {"48/3/256": 1.5}
@@ -31,7 +31,8 @@ def test_cache_round_trip_and_bad_entries(tmp_path):
 def test_tuning_keeps_results_and_applies_the_choice():
     from nixis_gb300 import autotune as A, mesh, planets
     cands = [A.TbConfig(32, 2, 256), A.TbConfig(40, 4, 512), A.TbConfig(48, 3, 1024), A.TbConfig(40, 4, 384, 1),
-             A.TbConfig(24, 4, 512, 2), A.TbConfig(32, 3, 1024, 2)]
+             A.TbConfig(24, 4, 512, 2), A.TbConfig(32, 3, 1024, 2), A.TbConfig(16, 4, 1024, 3),
+             A.TbConfig(12, 3, 512, 3)]
     cfg, timings = A.tune(divisions=60, iters=9, reps=1, configs=cands, save=False)
     assert cfg in cands and len(timings) == len(cands)
     assert A.current() == cfg
