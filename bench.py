@@ -308,7 +308,7 @@ def bench_ours(args):
     for r in reqs:
         cache.get(r.divisions)
     torch.cuda.synchronize()
-    batch = planets.PlanetBatch(reqs, cache)
+    batch = planets.PlanetBatch(reqs, cache, blocked=not args.no_blocked)
     if args.profile:
         # one eager run of the batch (what the ncu captures record), then exit
         batch.launch()
@@ -491,6 +491,26 @@ def run_serving(n_requests, hbm_budget=120 * 2**30):
     return out
 
 
+def profile_extras():
+    """One run of each kernel outside the batch on a mid-size sphere
+    (divisions 500, 2,500,002 vertices): mesh and tiling build, the height
+    shaping sequence, the latitude-table year, an equirectangular map of
+    1024 x 512 pixels.  The case the ncu summaries of those kernels use."""
+    import torch
+    from oracle import oracle as O
+    from nixis_gb300 import mesh, terrain, util, climate
+    m = mesh.PlanetMesh(500)
+    m.tiling(40, 4).maxnl
+    perm, pgi = O.init(3)
+    h = terrain.sample_octaves(m.xyz, None, perm, pgi, 8, 1.0, 1.0, 2.0, 0.5, 1.0)
+    shaped, _, _ = util.shape_heights(h)
+    climate.calc_yearly_insolation(m.xyz, None, 1.0, 23.44)
+    colors = util.rescale(shaped, 0, 255)
+    util.equirect_map(m.xyz, m.nbr, 500, colors, 1024, 512, 1.0)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": "extras", "vertices": m.n}))
+
+
 def profile_insolation():
     """One insolation launch (365 days x 24 hours) over divisions 474
     (2,246,762 vertices): the case the ncu capture of the kernel uses."""
@@ -659,6 +679,10 @@ def main():
     ap.add_argument("--tune-only", action="store_true", help="run the autotuner, print its table, exit")
     ap.add_argument("--profile-insolation", action="store_true",
                     help="one annual insolation launch on a 2,246,762-vertex sphere (ncu), exit")
+    ap.add_argument("--profile-extras", action="store_true",
+                    help="one run of the mesh, shaping, latitude-table and map kernels (ncu), exit")
+    ap.add_argument("--no-blocked", action="store_true",
+                    help="with --profile: one launch per erosion iteration instead of blocked passes")
     ap.add_argument("--serve", type=int, default=0, help="serving comparison on the first N stream requests, exit")
     ap.add_argument("--serve-requests", type=int, default=200, help="stream requests in the default line's serving leg")
     args = ap.parse_args()
@@ -670,6 +694,9 @@ def main():
         return
     if args.profile_insolation:
         profile_insolation()
+        return
+    if args.profile_extras:
+        profile_extras()
         return
     if args.warmup < 3:
         args.warmup = 3

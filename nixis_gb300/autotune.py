@@ -35,9 +35,11 @@ ROW_SMEM = 40                    # bytes of shared memory per local vertex (two 
 SIDES = (16, 20, 24, 28, 32, 40, 48)
 RINGS = (2, 3, 4, 5)
 THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2), (512, 3), (1024, 3))
-# variant 2 measured slower on GB300 for every tile size (one block per SM
-# cannot overlap its load phase with compute): tried only on request
-DEFAULT_VARIANTS = (0, 1, 3)
+# variants 2 and 3 measured slower on GB300 for every tile size (variant 2:
+# one block per SM cannot overlap its load phase with compute; variant 3:
+# tiles small enough for one vertex per thread recompute ~2x the halo):
+# tried only on request
+DEFAULT_VARIANTS = (0, 1)
 SUFFIX = {0: "", 1: "p", 2: "s", 3: "o"}
 
 
