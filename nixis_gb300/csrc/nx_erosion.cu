@@ -128,7 +128,9 @@ __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y
 // 2 lower, 0 equal.
 __device__ __forceinline__ unsigned erode_accum(float hh, float hl, float4 o, float dh, float dl, float2 &A, float2 &L)
 {
-    const float diff = __fadd_rn(__fsub_rn(o.x, hh), __fsub_rn(o.y, hl));
+    // (o.x - hh, o.y - hl) in one paired subtraction, then their sum
+    const float2 d2 = __fadd2_rn(make_float2(o.x, o.y), make_float2(-hh, -hl));
+    const float diff = __fadd_rn(d2.x, d2.y);
     const bool up = diff > 0.0f, dn = diff < 0.0f;
     const float g = up ? 1.0f : (dn ? -1.0f : 0.0f);
     const float xh = __fmul_rn(g, o.z), xl = __fmul_rn(g, o.w);

@@ -156,55 +156,86 @@ __global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const
 // Latitude-table path (climate.py:503-597): per tilt, a table of 181
 // latitudes (entry i = latitude i for i <= 90, i - 181 above), each the
 // binary32 running sum over 360 rotations of 1 degree from -180 of the
-// reference's term at (lat, lon 0) (calc_insolation_slice, with
-// sample_insolation's formula in binary64); then per vertex a linear
+// reference's binary64 term at (lat, lon 0) (calc_insolation_slice with
+// sample_insolation's formula); then per vertex a linear
 // interpolation between floor(lat) and ceil(lat), summed in binary32 over
 // the tables (calc_yearly_insolation adds 360 daily tables).
 
 constexpr double DEG = 3.141592653589793 / 180;
 
-__device__ __forceinline__ double ref_term(double x, double y, double z, double radius, double cr, double sr,
-                                           double ct, double st)
-{
-    // climate.py:423-442 with util.xyz2latlon (util.py:60-75)
-    const double rx = x * cr - y * sr;
-    const double ry = x * sr + y * cr;
-    const double rz = z;
-    const double tx = rx * ct + rz * st;
-    const double ty = ry;
-    const double tz = rz * ct - rx * st;
-    const double q = fmin(fmax(tz / radius, -1.0), 1.0);
-    const double lat = asin(q) * (180.0 / 3.141592653589793);
-    const double lon = atan2(ty, tx) * (180.0 / 3.141592653589793);
-    const double a = fmax(cos(fabs(lat) * 3.141592653589793 / 180), 0.0);
-    const double b = fmax(cos(lon * 3.141592653589793 / 180), 0.0);
-    return a * b;
-}
-
-// one block per table, one thread per latitude entry
+// One block per table, one thread per latitude entry.  The table's points
+// lie on the sphere of the given radius at longitude 0 (y = 0), so the
+// reference's term equals max(tx, 0) / radius with tx = x cos(theta)
+// cos(tau) + z sin(tau) (the identity at the top of this file); it is
+// evaluated in binary64 and summed in binary32 over the 360 rotations
+// (-180, -179, ..., 179 degrees: the running sum of 1.0 steps is exact) as
+// the reference sums its binary64 terms.  The rotations' cosines are
+// computed once per block into shared memory.
 __global__ void __launch_bounds__(192) slice_kernel(const double *__restrict__ tilts, int n_tilts, double radius,
                                                     float *__restrict__ tables)
 {
+    __shared__ double rc[360];
     const int d = blockIdx.x, i = threadIdx.x;
+    for (int j = i; j < 360; j += blockDim.x) rc[j] = cos((-180.0 + (double)j) * 3.141592653589793 / 180);
+    __syncthreads();
     if (d >= n_tilts || i >= 181) return;
     const double lat = (double)(i <= 90 ? i : i - 181);
     // util.latlon2xyz (util.py:79-88) at lon 0
     const double x = radius * cos(lat * DEG) * cos(0.0 * DEG);
-    const double y = radius * cos(lat * DEG) * sin(0.0 * DEG);
     const double z = radius * sin(lat * DEG);
     const double tilt = tilts[d];
     const double ct = cos(tilt * 3.141592653589793 / 180), st = sin(tilt * 3.141592653589793 / 180);
+    const double xc = x * ct, zs = z * st, inv_r = 1.0 / radius;
     float acc = 0.0f;
-    double rotation = -180.0;
     for (int j = 0; j < 360; ++j) {
-        const double cr = cos(rotation * 3.141592653589793 / 180), sr = sin(rotation * 3.141592653589793 / 180);
-        acc = (float)((double)acc + ref_term(x, y, z, radius, cr, sr, ct, st));
-        rotation += 1.0;
+        const double tx = __fma_rn(xc, rc[j], zs);
+        acc = __double2float_rn(__dadd_rn((double)acc, __dmul_rn(fmax(tx, 0.0), inv_r)));
     }
     tables[181 * d + i] = acc;
 }
 
-// climate.py:551-577 per vertex and table, summed in binary32 over tables
+// One interpolation of climate.py:575, round32(tl + frac * (tu - tl)) with
+// tu - tl rounded to binary32 and the product and sum rounded to binary64,
+// computed in binary32 pairs.  frac = fh + fl (+ a remainder below 2^-48
+// frac); with M = max(|tl|, |tu|) the pair value v' = sh + t is within
+// 2^-45 M of the exact tl + frac (tu - tl), and the reference's binary64
+// value within 2^-52 M of it.  When v' lies more than 2^-43 M from every
+// binary32 rounding boundary both round to the same binary32 value r;
+// otherwise (about one evaluation in 2^19) the binary64 formula is used.
+__device__ __forceinline__ float interp_one(float tl, float tu, float fh, float fl, double frac)
+{
+    const float dd = __fsub_rn(tu, tl);
+    const float ph = __fmul_rn(fh, dd);
+    const float pl = __fmaf_rn(fl, dd, __fmaf_rn(fh, dd, -ph));   // fh*dd = ph + (fh*dd - ph) exactly
+    // two-sum tl + ph = sh + se
+    const float sh = __fadd_rn(tl, ph);
+    const float bb = __fsub_rn(sh, tl);
+    const float se = __fadd_rn(__fsub_rn(tl, __fsub_rn(sh, bb)), __fsub_rn(ph, bb));
+    const float t = __fadd_rn(se, pl);
+    // two-sum sh + t = r + e: v' - r = e exactly
+    const float r = __fadd_rn(sh, t);
+    const float b2 = __fsub_rn(r, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(r, b2)), __fsub_rn(t, b2));
+    const float M = fmaxf(fabsf(tl), fabsf(tu));
+    const uint32_t rb = __float_as_uint(r) & 0x7FFFFFFFu;
+    const uint32_t ex = rb >> 23;
+    if (ex > 24 && ex < 255) {
+        // half an ulp of |r| away from zero, and toward zero (a quarter ulp
+        // below a power of two)
+        const float hu = __uint_as_float((ex - 24) << 23);
+        const float hd = (rb & 0x7FFFFFu) ? hu : 0.5f * hu;
+        const float ea = __float_as_uint(r) >> 31 ? -e : e;     // e measured away from zero
+        const float dist = ea >= 0.0f ? __fsub_rn(hu, ea) : __fadd_rn(hd, ea);
+        if (dist > 0x1p-43f * M) return r;
+    } else if (M == 0.0f) {
+        return r;                                                // tl = tu = 0
+    }
+    return __double2float_rn(__dadd_rn((double)tl, __dmul_rn(frac, (double)dd)));
+}
+
+// climate.py:551-577 per vertex and table, summed in binary32 over tables.
+// The reference divides the table difference by upper - lower, which is
+// exactly 1.0 whenever lower != upper, so no division is issued.
 __global__ void __launch_bounds__(256) interp_kernel(const double *__restrict__ xyz, int64_t n, double radius,
                                                      const float *__restrict__ tables, int n_tables,
                                                      float *__restrict__ out, int accumulate)
@@ -215,12 +246,13 @@ __global__ void __launch_bounds__(256) interp_kernel(const double *__restrict__ 
         const double fl = floor(lat), cl = ceil(lat);
         const int lower = (int)fl, upper = (int)cl;
         const int il = (lower + 181) % 181, iu = (upper + 181) % 181;
-        const double frac = lat - fl, span = (double)(upper - lower);
+        const double frac = lat - fl;
+        const float fh = __double2float_rn(frac);
+        const float fr = __double2float_rn(__dsub_rn(frac, (double)fh));
         float acc = accumulate ? out[v] : 0.0f;
         for (int d = 0; d < n_tables; ++d) {
             const float tl = __ldg(tables + 181 * d + il), tu = __ldg(tables + 181 * d + iu);
-            float val = tl;
-            if (lower != upper) val = (float)((double)tl + frac * ((double)__fsub_rn(tu, tl) / span));
+            const float val = lower != upper ? interp_one(tl, tu, fh, fr, frac) : tl;
             acc = (n_tables == 1 && !accumulate) ? val : __fadd_rn(acc, val);
         }
         out[v] = acc;

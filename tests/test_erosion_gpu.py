@@ -313,3 +313,25 @@ def test_temporally_blocked_long_run_rescales_like_iteration_at_a_time():
         out.append(vals)
     for x, y in zip(*out):
         assert torch.equal(x, y)
+
+
+def test_tiling_with_fewer_rings_than_a_pass_is_reported_not_run():
+    """A batch configured for 5-iteration passes over tilings built with 4
+    rings: the kernel flags err = 2 in the planet's control block and leaves
+    the state alone (no out-of-range reads), and the library is usable
+    afterwards."""
+    from nixis_gb300 import autotune, mesh, planets
+    from nixis_gb300.planets import PlanetRequest
+    cache = mesh.MeshCache()
+    req = PlanetRequest(seed=2, divisions=40, octaves=5, erosion_iters=10)
+    bt = planets.PlanetBatch([req], cache, tb=autotune.TbConfig(40, 4, 512))
+    bt.tb = autotune.TbConfig(40, 5, 512)          # passes of 5 over 4-ring tiles
+    bt.launch()
+    torch.cuda.synchronize()
+    ctl = bt.ws[:32].view(torch.int32)
+    assert int(ctl[6].item()) == 2
+    autotune.use(autotune.DEFAULT)
+    ok = planets.PlanetBatch([req], cache)
+    ok.run()
+    torch.cuda.synchronize()
+    assert torch.equal(ok.results()[0].heights, planets.generate_plain(req, cache).heights)

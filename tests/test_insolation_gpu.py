@@ -116,6 +116,28 @@ def test_lut_tables_and_interpolation_match_reference():
     assert np.abs(y - g["yearly_k4_t23"]).max() <= 1e-6 * g["yearly_k4_t23"].max()
 
 
+def test_lut_interpolation_is_bit_exact_on_random_tables():
+    # tables of random binary32 values (full mantissas, mixed magnitudes):
+    # the interpolation (binary32 pairs, binary64 near rounding boundaries)
+    # must give the reference's binary32 result.  Only a latitude whose asin
+    # rounds differently on the GPU and in libm can move a result, by 1 ulp.
+    from nixis_gb300 import climate
+    rng = np.random.default_rng(21)
+    n = 1 << 20
+    p = rng.normal(size=(n, 3))
+    p /= np.linalg.norm(p, axis=1, keepdims=True)
+    p *= 6378100.0
+    for scale in (1.0, 1e-3, 3e4):
+        tab = (rng.random(181) * scale).astype(np.float32)
+        tab[rng.random(181) < 0.05] = 0.0
+        got = np.zeros(n, np.float32)
+        climate.interpolate_insolation(p, tab, got, 6378100.0)
+        want = O.interpolate_insolation(p, tab, 6378100.0)
+        diff = got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64)
+        assert np.abs(diff).max() <= 1, scale
+        assert np.count_nonzero(diff) <= 8, (scale, np.count_nonzero(diff))
+
+
 def test_lut_yearly_on_a_large_sphere_matches_oracle():
     from nixis_gb300 import climate, mesh
     m = mesh.PlanetMesh(300)
