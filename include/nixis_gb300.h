@@ -362,6 +362,13 @@ int nx_insolation_slices(const double *tilts_dev, int n_tilts, double radius, fl
 int nx_interpolate_insolation(const double *xyz_dev, int64_t n, double radius, const float *tables_dev, int n_tables,
                               float *out_dev, int accumulate, void *stream);
 
+/* Starting surface temperatures (climate.assign_surface_temp,
+ * climate.py:345-411): out_dev float[n], vertex v's value
+ * max(cos(|lat - tilt| * pi / 180), 0) with lat from util.xyz2latlon.  The
+ * reference's altitude term rescales the altitudes to [0, 0], which is 0
+ * (NaN for a constant field) everywhere, so it never enters the result. */
+int nx_surface_temp(const double *xyz_dev, int64_t n, double radius, double tilt, float *out_dev, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Equirectangular maps (util.py:290-366, nixis.py:270-302)            */
 /* ------------------------------------------------------------------ */

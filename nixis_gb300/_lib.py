@@ -58,6 +58,7 @@ SIGNATURES = {
     "nx_nearest3": (_i32, [_i32, _p, _p, _i64, _p, _i64, _p, _p, _p]),
     "nx_sample_gray": (_i32, [_p, _p, _i64, _p, _i64, _p, _p, _p]),
     "nx_interpolate_insolation": (_i32, [_p, _i64, _d, _p, _i32, _p, _i32, _p]),
+    "nx_surface_temp": (_i32, [_p, _i64, _d, _d, _p, _p]),
     "nx_rescale": (_i32, [_p, _i64, _d, _d, _d, _i32, _d, _i32, _d, _i32, _p, _p, ctypes.c_size_t, _p]),
     "nx_power_rescale": (_i32, [_p, _i64, _p, _i32, _d, _p, _p, ctypes.c_size_t, _p]),
     "nx_elevation_mask": (_i32, [_p, _i64, _d, _p, _p]),

@@ -191,3 +191,24 @@ def calc_yearly_insolation(points, height, radius, axial_tilt, snapshot=False):
     call("nx_interpolate_insolation", _dev.ptr(xyz), n, float(radius), _dev.ptr(tab), 360, _dev.ptr(out), 0,
          _dev.stream_handle())
     return out.cpu().numpy() if host else out
+
+
+def assign_surface_temp(verts, altitudes, radius, tilt):
+    """climate.assign_surface_temp (climate.py:345-411): a new float32 array,
+    vertex v's max(cos(|lat - tilt| * pi / 180), 0) with lat from
+    util.xyz2latlon.  The reference rescales the altitudes to [0, 0]
+    (alt_intensity = 0), which gives 0 at every vertex (NaN for a constant
+    field), so its altitude branch (h2 > 0) is never taken; altitudes must
+    still give one value per vertex, and an empty mesh raises as the
+    reference's np.min does."""
+    host = _dev.is_host(verts)
+    xyz = _dev.to_device(verts, np.float64, name="verts")
+    _dev.check_vertices(xyz)
+    n = xyz.shape[0]
+    if altitudes is None or len(altitudes) != n:
+        raise ValueError("altitudes must hold one value per vertex")
+    if n == 0:
+        raise ValueError("zero-size array to reduction operation minimum which has no identity")
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    call("nx_surface_temp", _dev.ptr(xyz), n, float(radius), float(tilt), _dev.ptr(out), _dev.stream_handle())
+    return out.cpu().numpy() if host else out

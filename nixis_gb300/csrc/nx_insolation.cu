@@ -259,6 +259,23 @@ __global__ void __launch_bounds__(256) interp_kernel(const double *__restrict__ 
     }
 }
 
+// climate.assign_surface_temp (climate.py:345-411) per vertex: latitude as
+// util.xyz2latlon (util.py:59-75), then max(cos(|lat - tilt| * pi / 180), 0)
+// in binary64 with the reference's operation order, stored as binary32.
+// The reference's altitude term h2 = rescale(altitudes, 0, 0) is 0 (NaN for
+// a constant field) at every vertex, so its h2 > 0 branch is never taken.
+__global__ void __launch_bounds__(256) surface_temp_kernel(const double *__restrict__ xyz, int64_t n, double radius,
+                                                           double tilt, float *__restrict__ out)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const double q = fmin(fmax(__ddiv_rn(xyz[3 * v + 2], radius), -1.0), 1.0);
+        const double lat = __dmul_rn(asin(q), 180.0 / 3.141592653589793);
+        const double a = __ddiv_rn(__dmul_rn(fabs(__dsub_rn(lat, tilt)), 3.141592653589793), 180.0);
+        const double c = cos(a);
+        out[v] = __double2float_rn(0.0 > c ? 0.0 : c);     // Python max(c, 0): c unless 0 > c
+    }
+}
+
 int grid_for(int64_t n)
 {
     int64_t g = (n + 255) / 256;
@@ -398,6 +415,19 @@ NX_EXPORT int nx_interpolate_insolation(const double *xyz_dev, int64_t n, double
     interp_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(xyz_dev, n, radius, tables_dev, n_tables, out_dev,
                                                                  accumulate);
     NX_CHECK_LAUNCH("interp_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
+// climate.assign_surface_temp: out_dev float[n] for the vertices xyz_dev.
+NX_EXPORT int nx_surface_temp(const double *xyz_dev, int64_t n, double radius, double tilt, float *out_dev,
+                              void *stream)
+{
+    if (n < 0 || (n > 0 && (!xyz_dev || !out_dev)) || !(radius > 0.0))
+        return nx::fail(NX_EINVAL, "nx_surface_temp: bad arguments");
+    if (n == 0) return NX_OK;
+    surface_temp_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(xyz_dev, n, radius, tilt, out_dev);
+    NX_CHECK_LAUNCH("surface_temp_kernel");
     nx::note_launch(1);
     return NX_OK;
 }

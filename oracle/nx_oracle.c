@@ -729,6 +729,22 @@ NXO_API void nxo_interpolate_insolation(const double *xyz, int64_t n, const floa
     for (int64_t i = 0; i < n; ++i) out[i] = interp_one(table, xyz[3 * i + 2], radius);
 }
 
+/* climate.py:345-411 (assign_surface_temp) per vertex: max(cos(|lat - tilt|
+ * * pi / 180), 0) as binary32, lat as util.xyz2latlon (util.py:59-75).  The
+ * altitude term rescale(altitudes, 0, 0) is 0 or NaN everywhere, never > 0,
+ * so the reference's altitude branch does not contribute. */
+NXO_API void nxo_assign_surface_temp(const double *xyz, int64_t n, double radius, double tilt, float *out)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double q = xyz[3 * i + 2] / radius;
+        if (q < -1) q = -1;
+        if (q > 1) q = 1;
+        const double lat = asin(q) * (180.0 / PI);
+        const double c = cos(fabs(lat - tilt) * PI / 180);
+        out[i] = (float)(0.0 > c ? 0.0 : c);     /* Python max(c, 0): c unless 0 > c */
+    }
+}
+
 /* climate.py:579-597 (no snapshots): 360 daily tables at the seasonal tilt
  * of each orbital degree, interpolated and summed in binary32. */
 NXO_API void nxo_calc_yearly_insolation(const double *xyz, int64_t n, double radius, double axial_tilt, float *out)

@@ -63,6 +63,7 @@ def lib():
             "nxo_calc_insolation_slice": (None, [_d, _d, _p]),
             "nxo_interpolate_insolation": (None, [_p, _i64, _p, _p, _d]),
             "nxo_calc_yearly_insolation": (None, [_p, _i64, _d, _d, _p]),
+            "nxo_assign_surface_temp": (None, [_p, _i64, _d, _d, _p]),
             "nxo_make_ll": (None, [ctypes.c_int, ctypes.c_int, _d, _p]),
             "nxo_nearest3": (None, [_p, _i64, _p, _i64, _p, _p]),
             "nxo_make_gray": (None, [_p, _p, _i64, _p, _p]),
@@ -305,6 +306,13 @@ def interpolate_insolation(verts, table, radius):
     t = _c(table, np.float32)
     out = np.empty(len(v), np.float32)
     lib().nxo_interpolate_insolation(_ptr(v), len(v), _ptr(t), _ptr(out), float(radius))
+    return out
+
+
+def assign_surface_temp(verts, radius, tilt):
+    v = _c(verts, np.float64)
+    out = np.empty(len(v), np.float32)
+    lib().nxo_assign_surface_temp(_ptr(v), len(v), float(radius), float(tilt), _ptr(out))
     return out
 
 

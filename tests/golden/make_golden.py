@@ -11,8 +11,8 @@ erosion.erosion_iteration3 / erode_terrain3 / find_lowest,
 climate.sample_insolation / brute_daily_insolation / calculate_seasonal_tilt /
 day2deg, util.build_adjacency / sort_adjacency / rescale / power_rescale /
 find_percent_val, terrain.make_bool_elevation_mask, climate.calc_insolation_slice /
-interpolate_insolation / calc_daily_insolation / calc_yearly_insolation,
-util.make_ll_arr / make_gray_array with scipy's KDTree query) imported through
+interpolate_insolation / calc_daily_insolation / calc_yearly_insolation /
+assign_surface_temp, util.make_ll_arr / make_gray_array with scipy's KDTree query) imported through
 ref_shim.  `python tests/golden/make_golden.py shaping` regenerates one set.  Inputs are seeded; meshes come from tests/meshref.py (the same
 construction as the GPU generator).
 """
@@ -302,6 +302,22 @@ def gen_lut_insolation(R):
     np.savez_compressed(os.path.join(HERE, "lut_insolation.npz"), **out)
 
 
+def gen_surface_temp(R):
+    """climate.assign_surface_temp (climate.py:345-411) on icosphere
+    vertices for a few radii and tilts, with varying altitudes."""
+    cl = R.climate
+    out = {}
+    p8, _ = meshref.icosphere(8)
+    rng = np.random.default_rng(31)
+    h8 = rng.normal(size=len(p8))
+    cases = [(1.0, 23.44), (1.0, 0.0), (6378100.0, -17.3), (2.5, 90.0)]
+    out["cases"] = np.array(cases)
+    out["altitudes"] = h8
+    for i, (r, t) in enumerate(cases):
+        out[f"temp_{i}"] = np.asarray(cl.assign_surface_temp(p8 * r, h8, r, t), np.float32)
+    np.savez_compressed(os.path.join(HERE, "surface_temp.npz"), **out)
+
+
 def gen_image(R):
     """Equirectangular map sampling (util.py:290-367, nixis.py:270-302):
     make_ll_arr's pixel positions, the 3 nearest vertices of each pixel from
@@ -327,7 +343,7 @@ def gen_image(R):
 
 GENERATORS = {"perm": gen_perm, "noise": gen_noise, "octaves": gen_octaves, "mesh_erosion": gen_mesh_erosion,
               "insolation": gen_insolation, "shaping": gen_shaping,
-              "lut_insolation": gen_lut_insolation, "image": gen_image}
+              "lut_insolation": gen_lut_insolation, "image": gen_image, "surface_temp": gen_surface_temp}
 
 
 def main():

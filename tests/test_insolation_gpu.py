@@ -138,6 +138,29 @@ def test_lut_interpolation_is_bit_exact_on_random_tables():
         assert np.count_nonzero(diff) <= 8, (scale, np.count_nonzero(diff))
 
 
+def test_surface_temp_matches_reference():
+    # assign_surface_temp (climate.py:345-411): one asin and one cos per
+    # vertex in binary64, stored as binary32; CUDA's and libm's last bits
+    # can move a binary32 rounding by one ulp
+    import golden_io
+    from nixis_gb300 import climate, mesh
+    g = golden_io.load("surface_temp")
+    p8, _ = meshref.icosphere(8)
+    for i, (r, t) in enumerate(g["cases"]):
+        got = climate.assign_surface_temp(p8 * r, g["altitudes"], r, t)
+        want = g[f"temp_{i}"]
+        assert got.dtype == np.float32 and got.shape == want.shape
+        diff = got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64)
+        assert np.abs(diff).max() <= 1, i
+    m = mesh.PlanetMesh(300)
+    y = climate.assign_surface_temp(m.xyz, torch.zeros(m.n, dtype=torch.float64, device="cuda"), 1.0, 23.44)
+    want = O.assign_surface_temp(m.xyz.cpu().numpy(), 1.0, 23.44)
+    diff = y.cpu().numpy().view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64)
+    assert np.abs(diff).max() <= 1 and np.count_nonzero(diff) <= m.n // 1000
+    with pytest.raises(ValueError):
+        climate.assign_surface_temp(p8, np.zeros(3), 1.0, 0.0)
+
+
 def test_lut_yearly_on_a_large_sphere_matches_oracle():
     from nixis_gb300 import climate, mesh
     m = mesh.PlanetMesh(300)

@@ -145,6 +145,14 @@ def test_lut_insolation_bit_exact():
     assert np.array_equal(O.calc_yearly_insolation(p4, 1.0, 23.44), g["yearly_k4_t23"])
 
 
+def test_surface_temp_bit_exact():
+    """assign_surface_temp (climate.py:345-411) for four radii and tilts."""
+    g = golden_io.load("surface_temp")
+    p8, _ = meshref.icosphere(8)
+    for i, (r, t) in enumerate(g["cases"]):
+        assert np.array_equal(O.assign_surface_temp(p8 * r, r, t), g[f"temp_{i}"]), i
+
+
 def test_image_sampling_matches_reference():
     """make_ll_arr, the 3 nearest vertices (equal to scipy's KD-tree except
     where two candidates are exactly as far: the KD-tree's order among ties
