@@ -311,7 +311,11 @@ int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *
  * copied to shared memory once per pass (512 or 1024; needs maxc in the
  * planet descriptors); 3: one vertex per thread, its table row held in
  * registers for the pass (512 or 1024; every tile's updatable count maxc
- * must fit the block) -- and whether batches with tilings use it (1) or
+ * must fit the block); 4: variant 0 compiled for more resident blocks per
+ * SM (256 threads: 5 blocks, 320: 4, 384: 3, 640: 2; at most 1280
+ * threads x 48 registers or 1152 x 56), for tiles whose shared memory lets
+ * that many blocks reside; 5: the same for 6 blocks of 256 (40 registers)
+ * -- and whether batches with tilings use it (1) or
  * run one iteration per launch (0).  The autotuner (nixis_gb300.autotune)
  * picks these and the tile side per device. */
 int nx_erosion_tb_config(int rings, int threads, int variant, int enabled);

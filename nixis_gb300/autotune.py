@@ -11,7 +11,10 @@ computing the current one (hides their latency, costs registers and so
 resident threads), 2 copies the tile's tables to shared memory once per
 pass (no per-iteration global reads, but more shared memory per block), 3
 runs one vertex per thread with its table row held in registers for the
-pass (small tiles only: every tile's updatable vertices must fit the block).  ``tune`` times
+pass (small tiles only: every tile's updatable vertices must fit the block),
+4 and 5 are variant 0 compiled for more resident blocks per SM (fewer
+registers per thread, more warps to hide latency; they pay off only when
+the tile's shared memory lets that many blocks reside).  ``tune`` times
 every candidate on a synthetic planet, checks that all of them give the
 same heights bit for bit (they run the same per-vertex arithmetic), keeps
 the fastest and caches it per device in a JSON file
@@ -34,13 +37,18 @@ SMEM_LIMIT_TABLES = 226 * 1024   # of variant 2 (the opt-in limit less static sh
 ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
 SIDES = (16, 20, 24, 28, 32, 40, 48)
 RINGS = (2, 3, 4, 5)
-THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2), (512, 3), (1024, 3))
+THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2), (512, 3), (1024, 3),
+           (256, 4), (320, 4), (384, 4), (640, 4), (256, 5))
+# resident blocks per SM that variants 4 and 5 are compiled for, by threads
+MIN_BLOCKS = {(256, 4): 5, (320, 4): 4, (384, 4): 3, (640, 4): 2, (256, 5): 6}
+SM_SMEM = 228 * 1024             # shared memory per SM
+BLOCK_RESERVED = 1024            # shared memory the system reserves per resident block
 # variants 2 and 3 measured slower on GB300 for every tile size (variant 2:
 # one block per SM cannot overlap its load phase with compute; variant 3:
 # tiles small enough for one vertex per thread recompute ~2x the halo):
 # tried only on request
-DEFAULT_VARIANTS = (0, 1)
-SUFFIX = {0: "", 1: "p", 2: "s", 3: "o"}
+DEFAULT_VARIANTS = (0, 1, 4, 5)
+SUFFIX = {0: "", 1: "p", 2: "s", 3: "o", 4: "d", 5: "e"}
 
 
 @dataclass(frozen=True)
@@ -65,9 +73,15 @@ def smem_bytes(cfg, maxnl, maxc):
 
 
 def fits(cfg, maxnl, maxc):
+    """Whether a launch over tiles of up to maxnl local and maxc updatable
+    vertices is possible (variants 4 and 5: with the blocks per SM they are
+    compiled for resident)."""
     if cfg.variant == 3 and maxc > cfg.threads:
         return False
-    return smem_bytes(cfg, maxnl, maxc) <= (SMEM_LIMIT_TABLES if cfg.variant == 2 else SMEM_LIMIT)
+    b = smem_bytes(cfg, maxnl, maxc)
+    if cfg.variant in (4, 5):
+        return MIN_BLOCKS[(cfg.threads, cfg.variant)] * (b + BLOCK_RESERVED) <= SM_SMEM
+    return b <= (SMEM_LIMIT_TABLES if cfg.variant == 2 else SMEM_LIMIT)
 
 
 DEFAULT = TbConfig()
@@ -128,10 +142,11 @@ def store(key, cfg, timings=None, path=None):
 def parse(label):
     """TbConfig from its label side/rings/threads, 'p' appended for variant
     1 (prefetch), 's' for variant 2 (tables in shared memory), 'o' for
-    variant 3 (one vertex per thread)."""
+    variant 3 (one vertex per thread), 'd' and 'e' for variants 4 and 5
+    (more resident blocks per SM)."""
     side, rings, thr = label.split("/")
-    v = {"p": 1, "s": 2, "o": 3}.get(thr[-1], 0)
-    return TbConfig(int(side), int(rings), int(thr.rstrip("pso")), v)
+    v = {"p": 1, "s": 2, "o": 3, "d": 4, "e": 5}.get(thr[-1], 0)
+    return TbConfig(int(side), int(rings), int(thr.rstrip("psode")), v)
 
 
 def current():

@@ -444,8 +444,12 @@ __device__ __forceinline__ void tb_update(int l, const TileRow &row, const float
 // there.  ONE: one vertex per thread (tiles whose updatable count fits the
 // block); each thread loads its table row once per pass into registers, so
 // the iterations of the pass make no global reads.
-template <int THREADS, bool PF, bool SMT = false, bool ONE = false>
-__global__ void __launch_bounds__(THREADS, (PF ? 768 : 1024) / THREADS) erosion_tb_kernel(TbArgs a)
+// MINB > 0: at least MINB resident blocks per SM (the compiler keeps the
+// registers per thread at or under 65536 / (MINB * THREADS); the per-vertex
+// arithmetic fits 48 registers without spills), so more warps hide the
+// latency of the table reads when the tiles' shared memory allows it.
+template <int THREADS, bool PF, bool SMT = false, bool ONE = false, int MINB = 0>
+__global__ void __launch_bounds__(THREADS, MINB > 0 ? MINB : (PF ? 768 : 1024) / THREADS) erosion_tb_kernel(TbArgs a)
 {
     extern __shared__ float4 tsm4[];
     const int2 bm = a.blk_map[blockIdx.x];
@@ -836,7 +840,9 @@ NX_EXPORT int nx_erosion_tb_config(int rings, int threads, int variant, int enab
     if (rings < 1 || rings > 8) return nx::fail(NX_EINVAL, "nx_erosion_tb_config: rings must be in [1, 8]");
     const bool ok = variant == 1 ? (threads == 256 || threads == 384)
                   : (variant == 2 || variant == 3) ? (threads == 512 || threads == 1024)
-                  : variant == 0 ? (threads == 256 || threads == 512 || threads == 1024) : false;
+                  : variant == 0 ? (threads == 256 || threads == 512 || threads == 1024)
+                  : variant == 4 ? (threads == 256 || threads == 320 || threads == 384 || threads == 640)
+                  : variant == 5 ? threads == 256 : false;
     if (!ok)
         return nx::fail(NX_EINVAL, "nx_erosion_tb_config: threads %d do not go with variant %d", threads, variant);
     g_tb_rings = rings;
@@ -865,6 +871,15 @@ static cudaError_t launch_tb(int64_t grid, size_t smem, cudaStream_t s, const Tb
     } else if (g_tb_variant == 3) {
         if (g_tb_threads == 512) erosion_tb_kernel<512, false, false, true><<<(unsigned)grid, 512, smem, s>>>(ta);
         else erosion_tb_kernel<1024, false, false, true><<<(unsigned)grid, 1024, smem, s>>>(ta);
+    } else if (g_tb_variant == 4) {
+        switch (g_tb_threads) {
+        case 256: erosion_tb_kernel<256, false, false, false, 5><<<(unsigned)grid, 256, smem, s>>>(ta); break;
+        case 320: erosion_tb_kernel<320, false, false, false, 4><<<(unsigned)grid, 320, smem, s>>>(ta); break;
+        case 640: erosion_tb_kernel<640, false, false, false, 2><<<(unsigned)grid, 640, smem, s>>>(ta); break;
+        default: erosion_tb_kernel<384, false, false, false, 3><<<(unsigned)grid, 384, smem, s>>>(ta); break;
+        }
+    } else if (g_tb_variant == 5) {
+        erosion_tb_kernel<256, false, false, false, 6><<<(unsigned)grid, 256, smem, s>>>(ta);
     } else {
         switch (g_tb_threads) {
         case 256: erosion_tb_kernel<256, false><<<(unsigned)grid, 256, smem, s>>>(ta); break;
@@ -894,6 +909,16 @@ static int tb_prepare()
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<1024, false, false, true>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<384, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256, false, false, false, 5>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<384, false, false, false, 3>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<256, false, false, false, 6>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<320, false, false, false, 4>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NX_CHECK_CUDA(cudaFuncSetAttribute(erosion_tb_kernel<640, false, false, false, 2>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         int optin = 0;
         NX_CHECK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
         cudaFuncAttributes fa512, fa1024;
