@@ -526,7 +526,11 @@ def bench_serve(args):
     from nixis_gb300 import autotune
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    tb, _ = autotune.tune(save=False)
+    if args.tb:
+        tb = autotune.parse(args.tb)
+        autotune.use(tb)
+    else:
+        tb, _ = autotune.tune(save=False)
     res = run_serving(args.serve)
     res["blocked_erosion"] = tb.label
     print(json.dumps({"serving": res}))
@@ -674,8 +678,8 @@ def main():
     ap.add_argument("--eager", action="store_true", help="launch without a CUDA graph (for profilers)")
     ap.add_argument("--profile", action="store_true", help="build the batch, run it once eagerly, exit (ncu)")
     ap.add_argument("--single", choices=["c1", "c2", "c3"], help="a single-planet configuration (supplementary line)")
-    ap.add_argument("--tb", help="blocked-erosion setting side/rings/threads[p] instead of autotuning (e.g. 40/4/512, "
-                                 "40/4/384p with prefetch)")
+    ap.add_argument("--tb", help="blocked-erosion setting side/rings/threads[variant letter] instead of autotuning "
+                                 "(e.g. 40/4/512, 40/4/384p with prefetch, 32/4/384d with 3 blocks per SM)")
     ap.add_argument("--tune-only", action="store_true", help="run the autotuner, print its table, exit")
     ap.add_argument("--profile-insolation", action="store_true",
                     help="one annual insolation launch on a 2,246,762-vertex sphere (ncu), exit")

@@ -53,10 +53,10 @@ SUFFIX = {0: "", 1: "p", 2: "s", 3: "o", 4: "d", 5: "e"}
 
 @dataclass(frozen=True)
 class TbConfig:
-    tile_side: int = 40
+    tile_side: int = 32
     rings: int = 4
-    threads: int = 512
-    variant: int = 0
+    threads: int = 384
+    variant: int = 4
 
     @property
     def label(self):

@@ -10,13 +10,13 @@ def test_cache_round_trip_and_bad_entries(tmp_path):
     from nixis_gb300 import autotune as A
     p = str(tmp_path / "t.json")
     assert A.lookup("gpuX", p) is None
-    A.store("gpuX", A.TbConfig(48, 3, 256), {"48/3/256": 1.5}, path=p)
+    A.store("gpuX", A.TbConfig(48, 3, 256, 0), {"48/3/256": 1.5}, path=p)
     A.store("gpuY", A.TbConfig(32, 5, 384, 1), path=p)
-    assert A.lookup("gpuX", p) == A.TbConfig(48, 3, 256)
+    assert A.lookup("gpuX", p) == A.TbConfig(48, 3, 256, 0)
     assert A.lookup("gpuY", p) == A.TbConfig(32, 5, 384, 1)
-    assert A.parse("32/5/384p") == A.TbConfig(32, 5, 384, 1) and A.parse("40/4/512") == A.DEFAULT
+    assert A.parse("32/5/384p") == A.TbConfig(32, 5, 384, 1) and A.parse("32/4/384d") == A.DEFAULT
     assert A.parse("24/4/512s") == A.TbConfig(24, 4, 512, 2) and A.parse("16/3/1024o") == A.TbConfig(16, 3, 1024, 3)
-    assert A.parse(A.TbConfig(48, 2, 1024).label) == A.TbConfig(48, 2, 1024)
+    assert A.parse(A.TbConfig(48, 2, 1024, 0).label) == A.TbConfig(48, 2, 1024, 0)
     assert A.parse("24/4/256d") == A.TbConfig(24, 4, 256, 4) and A.parse("20/5/256e") == A.TbConfig(20, 5, 256, 5)
     assert A.parse(A.TbConfig(24, 3, 384, 4).label) == A.TbConfig(24, 3, 384, 4)
     # variants 4 / 5 fit only where their blocks per SM can reside
@@ -35,7 +35,7 @@ def test_cache_round_trip_and_bad_entries(tmp_path):
 @pytest.mark.gpu
 def test_tuning_keeps_results_and_applies_the_choice():
     from nixis_gb300 import autotune as A, mesh, planets
-    cands = [A.TbConfig(32, 2, 256), A.TbConfig(40, 4, 512), A.TbConfig(48, 3, 1024), A.TbConfig(40, 4, 384, 1),
+    cands = [A.TbConfig(32, 2, 256, 0), A.TbConfig(40, 4, 512, 0), A.TbConfig(48, 3, 1024, 0), A.TbConfig(40, 4, 384, 1),
              A.TbConfig(24, 4, 512, 2), A.TbConfig(32, 3, 1024, 2), A.TbConfig(16, 4, 1024, 3),
              A.TbConfig(12, 3, 512, 3), A.TbConfig(20, 4, 256, 4), A.TbConfig(16, 3, 384, 4),
              A.TbConfig(16, 4, 256, 5), A.TbConfig(24, 3, 640, 4), A.TbConfig(20, 3, 320, 4)]

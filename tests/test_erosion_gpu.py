@@ -324,8 +324,8 @@ def test_tiling_with_fewer_rings_than_a_pass_is_reported_not_run():
     from nixis_gb300.planets import PlanetRequest
     cache = mesh.MeshCache()
     req = PlanetRequest(seed=2, divisions=40, octaves=5, erosion_iters=10)
-    bt = planets.PlanetBatch([req], cache, tb=autotune.TbConfig(40, 4, 512))
-    bt.tb = autotune.TbConfig(40, 5, 512)          # passes of 5 over 4-ring tiles
+    bt = planets.PlanetBatch([req], cache, tb=autotune.TbConfig(40, 4, 512, 0))
+    bt.tb = autotune.TbConfig(40, 5, 512, 0)       # passes of 5 over 4-ring tiles
     bt.launch()
     torch.cuda.synchronize()
     ctl = bt.ws[:32].view(torch.int32)
