@@ -59,9 +59,10 @@ __device__ __forceinline__ void interior_fij(int64_t q, int k, int &f, int &i, i
     const int64_t npf = (int64_t)(k - 1) * (k - 2) / 2;
     f = (int)(q / npf);
     const int64_t off = q - (int64_t)f * npf;
-    const double kk = (double)k;
-    const double disc = (2.0 * kk - 3.0) * (2.0 * kk - 3.0) - 8.0 * (double)off;
-    int ii = (int)floor(((2.0 * kk - 3.0) - sqrt(disc > 0 ? disc : 0.0)) / 2.0) + 1;
+    // binary32 estimate of the row; the loops below make it exact
+    const float kk = (float)k;
+    const float disc = (2.0f * kk - 3.0f) * (2.0f * kk - 3.0f) - 8.0f * (float)off;
+    int ii = (int)floorf(((2.0f * kk - 3.0f) - sqrtf(fmaxf(disc, 0.0f))) * 0.5f) + 1;
     if (ii < 1) ii = 1;
     if (ii > k - 2) ii = k - 2;
     auto start = [&](int a) -> int64_t { return (int64_t)(a - 1) * (k - 1) - (int64_t)(a - 1) * a / 2; };
@@ -89,10 +90,10 @@ __global__ void ico_vertices_kernel(int k, int64_t nv, double *__restrict__ xyz)
             int f = (int)(q / npf);
             int64_t off = q - (int64_t)f * npf;
             // row i (1..k-2) holds k-1-i points; invert the running offset
-            // (i-1)(k-1) - (i-1)i/2 with a float estimate plus correction.
-            double kk = (double)k;
-            double disc = (2.0 * kk - 3.0) * (2.0 * kk - 3.0) - 8.0 * (double)off;
-            int i0 = (int)floor(((2.0 * kk - 3.0) - sqrt(disc > 0 ? disc : 0.0)) / 2.0);
+            // (i-1)(k-1) - (i-1)i/2 with a binary32 estimate plus correction.
+            const float kk = (float)k;
+            const float disc = (2.0f * kk - 3.0f) * (2.0f * kk - 3.0f) - 8.0f * (float)off;
+            int i0 = (int)floorf(((2.0f * kk - 3.0f) - sqrtf(fmaxf(disc, 0.0f))) * 0.5f);
             int i = i0 + 1;
             if (i < 1) i = 1;
             if (i > k - 2) i = k - 2;
@@ -257,23 +258,45 @@ __device__ __forceinline__ float2 edge_pair(double d)
 // erosion.py:38-40 in binary64 (squares by multiplication), split into a
 // pair hi + lo of binary32s: el[2q] = hi, el[2q+1] = lo.  |v_i - v_j| and
 // |v_j - v_i| are the same number (the differences only change sign), so
-// the binary64 square root -- slow at GB300's binary64 rate -- is taken once
-// per edge: this pass fills the slots whose neighbour has the larger id,
-// edge_mirror_kernel copies them into the reverse slots.
-__global__ void edge_len_kernel(const double *__restrict__ xyz, const int32_t *__restrict__ nbr, int64_t nv,
-                                float2 *__restrict__ el, int *__restrict__ err)
+// the binary64 arithmetic -- slow at GB300's binary64 rate -- runs once per
+// edge: this pass fills the slots whose neighbour has the larger id (or is
+// the vertex itself), edge_mirror_kernel copies them into the reverse slots.
+// Each warp takes 64 consecutive slots at a time and gathers the ones that
+// need a distance (about half) into consecutive lanes through shared
+// memory, so the binary64 instructions run with the warp's lanes busy
+// instead of half of them masked off.
+__global__ void __launch_bounds__(256) edge_len_kernel(const double *__restrict__ xyz, const int32_t *__restrict__ nbr,
+                                                       int64_t nv, float2 *__restrict__ el, int *__restrict__ err)
 {
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 6 * nv; q += (int64_t)gridDim.x * blockDim.x) {
-        int64_t v = q / 6;
-        int32_t j = nbr[q];
-        double d = 0.0;
-        if (j >= 0 && (int64_t)j < nv && (int64_t)j < v) continue;     // the mirror pass fills it
-        if (j >= 0 && (int64_t)j < nv) {
-            d = edge_len(xyz, v, j);
-        } else if (j != -1 && err) {
-            atomicOr(err, 1);
+    __shared__ int64_t s_q[8][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nq = 6 * nv;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = wid * 64; base < nq; base += nw * 64) {
+        int cnt = 0;
+        for (int h = 0; h < 2; ++h) {
+            const int64_t q = base + 32 * h + lane;
+            bool work = false;
+            if (q < nq) {
+                const int32_t j = nbr[q];
+                if (j >= 0 && (int64_t)j < nv) {
+                    work = (int64_t)j >= q / 6;                  // j < v: filled by the mirror pass
+                } else {
+                    if (j != -1 && err) atomicOr(err, 1);
+                    el[q] = make_float2(0.0f, 0.0f);
+                }
+            }
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, work);
+            if (work) s_q[w][cnt + __popc(m & ((1u << lane) - 1u))] = q;
+            cnt += __popc(m);
         }
-        el[q] = edge_pair(d);
+        __syncwarp();
+        for (int r = lane; r < cnt; r += 32) {
+            const int64_t q = s_q[w][r];
+            el[q] = edge_pair(edge_len(xyz, q / 6, nbr[q]));
+        }
+        __syncwarp();
     }
 }
 
@@ -434,7 +457,7 @@ NX_EXPORT int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int
     if (nv < 0) return nx::fail(NX_EINVAL, "nx_edge_lengths: nv < 0");
     if (nv == 0) return NX_OK;
     if (!xyz_dev || !nbr_dev || !edge_dev) return nx::fail(NX_EINVAL, "nx_edge_lengths: null pointer");
-    edge_len_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, (float2 *)edge_dev, err_dev);
+    edge_len_kernel<<<grid1d(3 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, (float2 *)edge_dev, err_dev);
     NX_CHECK_LAUNCH("edge_len_kernel");
     edge_mirror_kernel<<<grid1d(6 * nv), 256, 0, (cudaStream_t)stream>>>(xyz_dev, nbr_dev, nv, (float2 *)edge_dev);
     NX_CHECK_LAUNCH("edge_mirror_kernel");
