@@ -457,14 +457,15 @@ def run_serving(n_requests, hbm_budget=120 * 2**30):
     erosion iterations U[0,100], insolation for half), served (a) as they
     arrive and (b) all at once, by the engine and by the plain per-planet
     path; every engine result is checked bit for bit against the plain
-    path's.  Meshes are built on demand by both (resident, LRU under the
-    budget) in the arrivals run and stay resident for the all-at-once run,
-    for both paths alike."""
+    path's.  Meshes are built on demand by both (resident, LRU under each
+    path's budget); both paths keep theirs from the arrivals run for the
+    all-at-once run."""
     import torch
     from nixis_gb300 import serve
     stream = serve.poisson_stream(2000)[:n_requests]
     out = {"requests": len(stream), "arrival_rate_per_s": 20.0, "hbm_budget_gb": hbm_budget / 2**30,
-           "meshes": "built on demand in the arrivals run, resident for the all-at-once run (both paths)"}
+           "meshes": "built on demand; each path keeps its meshes from the arrivals run for the all-at-once run "
+                     "within its HBM budget (LRU), so meshes evicted since are rebuilt"}
     eng_meshes = None
     pm = serve.ResidentMeshes(hbm_budget // 2)
     for mode, realtime in (("arrivals", True), ("all_at_once", False)):

@@ -207,8 +207,7 @@ def tune(divisions=800, iters=24, reps=3, configs=None, save=True, verbose=False
     timings, ref, best = {}, None, None
     configs.sort(key=lambda c: (c.tile_side, c.rings, c.threads, c.variant))
     for cfg in configs:
-        for key in [k for k in m._tilings if k != (cfg.tile_side, cfg.rings)]:
-            del m._tilings[key]                  # one tiling resident at a time
+        m.drop_tilings(keep=(cfg.tile_side, cfg.rings))   # one tiling resident at a time
         tl = m.tiling(cfg.tile_side, cfg.rings)
         if not fits(cfg, tl.maxnl, tl.maxc):
             continue

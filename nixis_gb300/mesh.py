@@ -156,12 +156,21 @@ class PlanetMesh:
         key = (tile_side, rings)
         if key not in self._tilings:
             self._tilings[key] = MeshTiling(self, tile_side, rings, stream)
+            self._nbytes = None
         return self._tilings[key]
+
+    def drop_tilings(self, keep=None):
+        """Free every tiling but the one keyed (tile_side, rings) = keep."""
+        for key in [k for k in self._tilings if k != keep]:
+            del self._tilings[key]
+        self._nbytes = None
 
     @property
     def nbytes(self):
-        return (self.xyz.numel() * 8 + self.nbr.numel() * 4 + self.edge.numel() * 4 +
-                sum(t.nbytes for t in self._tilings.values()))
+        if getattr(self, "_nbytes", None) is None:
+            self._nbytes = (self.xyz.numel() * 8 + self.nbr.numel() * 4 + self.edge.numel() * 4 +
+                            sum(t.nbytes for t in self._tilings.values()))
+        return self._nbytes
 
 
 class MeshTiling:

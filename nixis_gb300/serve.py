@@ -21,14 +21,16 @@ stream while the main stream keeps eroding the others; it joins the next
 tick.  Its insolation (which needs only the vertices) starts at admission on
 a third stream, beside its erosion.  A planet that finishes erosion gets
 its heights (main stream), then the copy of its results to page-locked host
-memory on the side stream.  Results are the same bits as the planet
-generated alone (planets.generate_plain).
+memory on the side stream; a host thread moves them into ordinary arrays
+(the request's results) while the engine keeps launching.  Results are the
+same bits as the planet generated alone (planets.generate_plain).
 
 ``serve_plain`` is the comparator: the same stream of requests handled one
 at a time with the plain per-planet path.
 """
 import ctypes
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -96,7 +98,7 @@ class ResidentMeshes:
         return 0 if k in self.meshes else _planets.mesh_bytes(k, self.tb)
 
     def resident_bytes(self):
-        return sum(m.nbytes for m in self.meshes.values())
+        return sum(m.nbytes for m in self.meshes.values())   # PlanetMesh caches its size
 
     def can_fit(self, k):
         need = self.bytes_for(k)
@@ -215,6 +217,8 @@ class ServeEngine:
         self.done = []
         self._inflight = []      # events of recent ticks (bounded queue depth)
         self._schedules = {}
+        self._pool = ThreadPoolExecutor(max_workers=2, thread_name_prefix="nx-deliver")
+        self._delivering = []
 
     # ------------------------------------------------------------------
     def submit(self, request, arrival, index=0):
@@ -227,7 +231,9 @@ class ServeEngine:
         if key not in self._schedules:
             rot, tilts = _climate.annual_schedule(r.axial_tilt, r.days, r.days, r.hours)
             tab, nre, pairs = _climate._plan(rot, tilts)
-            self._schedules[key] = (torch.from_numpy(tab).cuda(), nre, pairs, len(tilts),
+            # page-locked source: the upload is queued on the current stream
+            # without waiting for the work already queued there
+            self._schedules[key] = (_pinned(tab).to("cuda", non_blocking=True), nre, pairs, len(tilts),
                                     _climate.SOLAR_CONSTANT / (r.days * r.hours))
         return self._schedules[key]
 
@@ -441,22 +447,41 @@ class ServeEngine:
         it = t.request.erosion_iters
         return int(lib().nx_erosion_npass(it)) if blocked else it
 
+    def _reap_deliveries(self):
+        """Drop finished deliveries; a delivery that failed raises here."""
+        still = []
+        for f in self._delivering:
+            if f.done():
+                f.result()
+            else:
+                still.append(f)
+        self._delivering = still
+
+    @staticmethod
+    def _deliver(t, host_h, host_i):
+        """Results to ordinary host memory (numpy copies release the GIL, so
+        this runs beside the engine's loop); the page-locked buffers then go
+        back to the caching allocator for later planets.  The request is
+        finished when its arrays are in place."""
+        t.heights = host_h.numpy().copy()
+        t.insolation = host_i.numpy().copy() if host_i is not None else None
+        t.finished = time.perf_counter()
+        t.stage = "done"
+
     def _collect(self):
         still = []
         for t in self.active:
             if t.stage == "copying" and t.done_event.query():
-                t.finished = time.perf_counter()
                 t.mesh.check()
-                # results move to ordinary host memory; the page-locked
-                # buffers go back to the caching allocator for later planets
-                t.heights = t.host_h.numpy().copy()
-                t.insolation = t.host_i.numpy().copy() if t.host_i is not None else None
+                h, i = t.host_h, t.host_i
                 t.host_h = t.host_i = None
+                t.stage = "delivering"
+                self._delivering.append(self._pool.submit(self._deliver, t, h, i))
+                del h, i
                 self.arena.release(t.vbeg, t.mesh.n)
                 self.free_slots.append(t.slot)
                 self.meshes.release(t.request.divisions)
                 self.tiles_admitted -= t.tiles
-                t.stage = "done"
                 t.mesh = None
                 t.tiling = None
                 t._keep = None
@@ -484,6 +509,10 @@ class ServeEngine:
                     raise MemoryError("request does not fit the HBM budget even alone: %r" % (self.queue[0].request,))
             elif not busy:
                 time.sleep(0.0002)
+            self._reap_deliveries()
+        for f in self._delivering:
+            f.result()
+        self._delivering = []
         torch.cuda.synchronize()
         return tickets
 
