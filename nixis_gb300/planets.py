@@ -101,7 +101,8 @@ def mesh_bytes(divisions, tb=None):
 @dataclass
 class PlanetResult:
     request: PlanetRequest
-    heights: torch.Tensor               # float32 (N,), metres
+    heights: torch.Tensor               # float32 (N,), metres (+-inf beyond binary32's range: the
+                                        # reference's erosion grows without bound over long runs)
     insolation: torch.Tensor = None     # float32 (N,), mean TOA W/m^2 over the schedule
     scale_exponent: int = 0
 
