@@ -402,6 +402,11 @@ def bench_ours(args):
     plain_s = time.perf_counter() - t0
     plain = {"value": npl / plain_s, "unit": UNIT,
              "what": "one planet at a time, one launch per octave and per erosion iteration, synchronised per planet"}
+    # (outside the timed regions) every batched planet equals the planet generated alone
+    res = batch.results()
+    plain["batch_equals_plain"] = bool(all(torch.equal(a.heights, planets.generate_plain(r, cache).heights)
+                                           for r, a in zip(reqs, res)))
+    del res
 
     # end to end: per step, request tables host->device, batch, heights device->host (pinned)
     host_tab = torch.empty_like(batch.tables, device="cpu").pin_memory()

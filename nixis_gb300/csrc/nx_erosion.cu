@@ -514,13 +514,23 @@ __global__ void __launch_bounds__(THREADS, MINB > 0 ? MINB : (PF ? 768 : 1024) /
         }
         if ((int)threadIdx.x < C0) myrow = tile_row<false>(lnb, led, threadIdx.x);
     }
-    for (int l = threadIdx.x; l < NL; l += blockDim.x) {
-        const int64_t row = P.vbeg + ids[l];
-        const float4 x = ist[2 * row];
-        const float4 y = ist[2 * row + 1];
-        const Pair wr = prain(__fmul_rn(x.z, lam), __fmul_rn(x.w, lam), rain);
-        buf0[l] = make_float4(__fmul_rn(x.x, lam), __fmul_rn(x.y, lam), wr.h, wr.l);
-        sed[l] = make_float2(__fmul_rn(y.x, lam), __fmul_rn(y.y, lam));
+    // two rows per thread per round, both gathers in flight before either
+    // is stored (halves the dependent DRAM round trips of the load phase)
+    for (int l0 = threadIdx.x; l0 < NL; l0 += 2 * THREADS) {
+        const int l1 = l0 + THREADS;
+        const bool two = l1 < NL;
+        const int64_t r0 = P.vbeg + ids[l0];
+        const int64_t r1 = two ? P.vbeg + ids[l1] : r0;
+        const float4 x0 = ist[2 * r0], y0 = ist[2 * r0 + 1];
+        const float4 x1 = ist[2 * r1], y1 = ist[2 * r1 + 1];
+        const Pair w0 = prain(__fmul_rn(x0.z, lam), __fmul_rn(x0.w, lam), rain);
+        buf0[l0] = make_float4(__fmul_rn(x0.x, lam), __fmul_rn(x0.y, lam), w0.h, w0.l);
+        sed[l0] = make_float2(__fmul_rn(y0.x, lam), __fmul_rn(y0.y, lam));
+        if (two) {
+            const Pair w1 = prain(__fmul_rn(x1.z, lam), __fmul_rn(x1.w, lam), rain);
+            buf0[l1] = make_float4(__fmul_rn(x1.x, lam), __fmul_rn(x1.y, lam), w1.h, w1.l);
+            sed[l1] = make_float2(__fmul_rn(y1.x, lam), __fmul_rn(y1.y, lam));
+        }
     }
     __syncthreads();
     int C = C0;
