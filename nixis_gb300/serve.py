@@ -46,6 +46,8 @@ from ._lib import ErosionPlanet, FbmPlanet, call, lib
 
 ALIGN = 256
 ROW_BYTES = 32 + 32 + 4 + 4 + 4
+COPY_THREADS = 4           # host threads that move one result array
+COPY_SPLIT = 1 << 20       # elements from which a result array is copied in slices
 
 
 class RowArena:
@@ -218,6 +220,7 @@ class ServeEngine:
         self._inflight = []      # events of recent ticks (bounded queue depth)
         self._schedules = {}
         self._pool = ThreadPoolExecutor(max_workers=2, thread_name_prefix="nx-deliver")
+        self._copy_pool = ThreadPoolExecutor(max_workers=COPY_THREADS, thread_name_prefix="nx-copy")
         self._delivering = []
 
     # ------------------------------------------------------------------
@@ -457,14 +460,26 @@ class ServeEngine:
                 still.append(f)
         self._delivering = still
 
-    @staticmethod
-    def _deliver(t, host_h, host_i):
-        """Results to ordinary host memory (numpy copies release the GIL, so
-        this runs beside the engine's loop); the page-locked buffers then go
-        back to the caching allocator for later planets.  The request is
-        finished when its arrays are in place."""
-        t.heights = host_h.numpy().copy()
-        t.insolation = host_i.numpy().copy() if host_i is not None else None
+    def _copy_out(self, src):
+        """A page-locked tensor's contents as a new numpy array, copied in
+        slices by several host threads (numpy releases the GIL while it
+        copies): one thread does not reach the host's memory bandwidth, and
+        the copy is on the request's latency."""
+        a = src.numpy()
+        out = np.empty_like(a)
+        parts = COPY_THREADS if a.size >= COPY_SPLIT else 1
+        cuts = [a.size * q // parts for q in range(parts + 1)]
+        futs = [self._copy_pool.submit(np.copyto, out[b:e], a[b:e]) for b, e in zip(cuts[:-1], cuts[1:])]
+        for f in futs:
+            f.result()
+        return out
+
+    def _deliver(self, t, host_h, host_i):
+        """Results to ordinary host memory beside the engine's loop; the
+        page-locked buffers then go back to the caching allocator for later
+        planets.  The request is finished when its arrays are in place."""
+        t.heights = self._copy_out(host_h)
+        t.insolation = self._copy_out(host_i) if host_i is not None else None
         t.finished = time.perf_counter()
         t.stage = "done"
 
