@@ -739,8 +739,11 @@ __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_plan
     }
 }
 
-// Heights of every planet after its run: (h_hi + h_lo) * 2^K, summed in
-// binary64 and rounded once to binary32.
+// Heights of every planet after its run: (h_hi + h_lo) * 2^K rounded once
+// to binary32.  The pair's sum is exact in binary64, so its binary32 sum
+// hi + lo is that value rounded once; scaling by 2^K is then exact while
+// the result stays a normal binary32.  Only other results (zero, subnormal,
+// overflow) take the binary64 route -- GB300's binary64 rate is low.
 __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_planet *__restrict__ P, int np,
                                                               const float4 *__restrict__ st,
                                                               const nx_erosion_ctl *__restrict__ ctl,
@@ -752,7 +755,11 @@ __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_p
         const int64_t i = row - P[p].vbeg;
         if (i < 0 || i >= P[p].n) continue;
         const float4 v = st[2 * row];
-        out[row] = (float)ldexp((double)v.x + (double)v.y, ctl[P[p].slot].K[0]);
+        const int K = ctl[P[p].slot].K[0];
+        const float r = __fadd_rn(v.x, v.y);
+        const int e = (int)((__float_as_uint(r) >> 23) & 0xFFu);
+        out[row] = (e > 0 && e + K > 0 && e + K < 255) ? scalbnf(r, K)
+                                                      : (float)ldexp((double)v.x + (double)v.y, K);
     }
 }
 
