@@ -29,6 +29,7 @@ same bits as the planet generated alone (planets.generate_plain).
 at a time with the plain per-planet path.
 """
 import ctypes
+import threading
 import time
 from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
@@ -48,6 +49,7 @@ ALIGN = 256
 ROW_BYTES = 32 + 32 + 4 + 4 + 4
 COPY_THREADS = 4           # host threads that move one result array
 COPY_SPLIT = 1 << 20       # elements from which a result array is copied in slices
+HOST_PAGE = 4096           # unit of the page-locked result arena
 
 
 class RowArena:
@@ -83,6 +85,37 @@ class RowArena:
     @property
     def used(self):
         return self.capacity - sum(ln for _, ln in self.free)
+
+
+class PinnedArena:
+    """Page-locked host memory taken once, handed out as first-fit ranges:
+    results are copied into it without waiting on the page-locking of fresh
+    memory (hundreds of MB take milliseconds to lock, on the request's
+    latency).  Ranges are released from the delivery threads, hence the
+    lock."""
+
+    def __init__(self, nbytes):
+        pages = max(0, int(nbytes)) // HOST_PAGE
+        self.pages = RowArena(pages)
+        self.buf = (torch.empty(self.pages.capacity * HOST_PAGE, dtype=torch.uint8, pin_memory=True)
+                    if self.pages.capacity else None)
+        self.lock = threading.Lock()
+
+    def alloc_f32(self, n):
+        """(float32 tensor of n elements, release token), or None when full."""
+        need = (4 * n + HOST_PAGE - 1) // HOST_PAGE
+        if self.buf is None or need == 0:
+            return None
+        with self.lock:
+            start = self.pages.alloc(need)
+        if start is None:
+            return None
+        b = start * HOST_PAGE
+        return self.buf[b:b + 4 * n].view(torch.float32), (start, need)
+
+    def release(self, token):
+        with self.lock:
+            self.pages.release(*token)
 
 
 class ResidentMeshes:
@@ -155,6 +188,7 @@ class Ticket:
     tiles: int = 0
     host_h: torch.Tensor = None
     host_i: torch.Tensor = None
+    host_tokens: list = field(default_factory=list)
     done_event: object = None
     ready_event: object = None
     inso_event: object = None
@@ -182,7 +216,7 @@ class ServeEngine:
     """Continuous-batching planet generator over one GPU."""
 
     def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None, max_ticks=8,
-                 blocked=True):
+                 blocked=True, host_bytes=2 * 2**30):
         _dev.require_cuda()
         self.budget = int(hbm_budget)
         rows = arena_rows if arena_rows is not None else int(self.budget * arena_fraction) // ROW_BYTES
@@ -221,6 +255,7 @@ class ServeEngine:
         self._schedules = {}
         self._pool = ThreadPoolExecutor(max_workers=2, thread_name_prefix="nx-deliver")
         self._copy_pool = ThreadPoolExecutor(max_workers=COPY_THREADS, thread_name_prefix="nx-copy")
+        self.host = PinnedArena(host_bytes)
         self._delivering = []
 
     # ------------------------------------------------------------------
@@ -319,9 +354,6 @@ class ServeEngine:
                      ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg),
                      ctypes.c_void_p(self.st_tmp.data_ptr() + 32 * t.vbeg), s)
                 t._e_single = (e, e_dev)
-                t.host_h = torch.empty(t.mesh.n, dtype=torch.float32, pin_memory=True)
-                if r.insolation:
-                    t.host_i = torch.empty(t.mesh.n, dtype=torch.float32, pin_memory=True)
                 ev = torch.cuda.Event()
                 ev.record(self.side)
                 t.ready_event = ev
@@ -345,10 +377,19 @@ class ServeEngine:
             call("nx_insolation", _dev.ptr(t.mesh.xyz), n, float(r.radius), _dev.ptr(tab), nre, pairs, ntilt,
                  _dev.ptr(out), 0, _dev.stream_handle(self.inso_stream))
             out.mul_(scale)
-            t.host_i.copy_(out, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(self.inso_stream)
         t.inso_event = ev
+
+    def _host_buffer(self, t, n):
+        """A page-locked float32 buffer of n elements for t's results: from
+        the arena, else from torch's caching host allocator."""
+        got = self.host.alloc_f32(n)
+        if got is None:
+            return torch.empty(n, dtype=torch.float32, pin_memory=True)
+        buf, token = got
+        t.host_tokens.append(token)
+        return buf
 
     def _output(self, t, after_main):
         """Heights and their copy to the host for a finished planet."""
@@ -366,11 +407,14 @@ class ServeEngine:
         ev = torch.cuda.Event()
         ev.record(stream)
         self.side.wait_event(ev)
+        n = t.mesh.n
+        t.host_h = self._host_buffer(t, n)
+        t.host_i = self._host_buffer(t, n) if r.insolation else None
         with torch.cuda.stream(self.side):
-            n = t.mesh.n
+            t.host_h.copy_(self.heights[t.vbeg:t.vbeg + n], non_blocking=True)
             if t.inso_event is not None:
                 self.side.wait_event(t.inso_event)
-            t.host_h.copy_(self.heights[t.vbeg:t.vbeg + n], non_blocking=True)
+                t.host_i.copy_(self.inso[t.vbeg:t.vbeg + n], non_blocking=True)
             done = torch.cuda.Event()
             done.record(self.side)
         t.done_event = done
@@ -474,13 +518,16 @@ class ServeEngine:
             f.result()
         return out
 
-    def _deliver(self, t, host_h, host_i):
+    def _deliver(self, t, host_h, host_i, tokens):
         """Results to ordinary host memory beside the engine's loop; the
-        page-locked buffers then go back to the caching allocator for later
-        planets.  The request is finished when its arrays are in place."""
+        page-locked buffers then go back to the arena (or the caching
+        allocator) for later planets.  The request is finished when its
+        arrays are in place."""
         t.heights = self._copy_out(host_h)
         t.insolation = self._copy_out(host_i) if host_i is not None else None
         t.finished = time.perf_counter()
+        for tok in tokens:
+            self.host.release(tok)
         t.stage = "done"
 
     def _collect(self):
@@ -488,10 +535,11 @@ class ServeEngine:
         for t in self.active:
             if t.stage == "copying" and t.done_event.query():
                 t.mesh.check()
-                h, i = t.host_h, t.host_i
+                h, i, tok = t.host_h, t.host_i, t.host_tokens
                 t.host_h = t.host_i = None
+                t.host_tokens = []
                 t.stage = "delivering"
-                self._delivering.append(self._pool.submit(self._deliver, t, h, i))
+                self._delivering.append(self._pool.submit(self._deliver, t, h, i, tok))
                 del h, i
                 self.arena.release(t.vbeg, t.mesh.n)
                 self.free_slots.append(t.slot)

@@ -50,8 +50,25 @@ def test_admission_waits_for_memory_and_still_matches():
     stream = small_stream(10, seed=9)
     biggest = max(r.n_vertices for _, r in stream)
     # room for about two planets at a time: later arrivals wait for rows
-    eng = serve.ServeEngine(hbm_budget=4 * 2**30, arena_rows=2 * biggest + 1024, slots=8)
+    # a result arena of 1 MB: most results fall back to torch's page-locked allocator
+    eng = serve.ServeEngine(hbm_budget=4 * 2**30, arena_rows=2 * biggest + 1024, slots=8, host_bytes=1 << 20)
     tickets = eng.run(stream, realtime=False)
     check_against_alone(tickets)
     waited = [t for t in tickets if t.admitted - t.arrival > 1e-4]
     assert waited, "expected some requests to wait for memory"
+
+
+def test_pinned_arena_hands_out_and_takes_back_ranges():
+    from nixis_gb300 import serve
+    a = serve.PinnedArena(8 << 20)                 # 8 MB in 1 MB units
+    b1, t1 = a.alloc_f32(1 << 20)                  # 4 MB
+    b2, t2 = a.alloc_f32(1 << 20)
+    assert b1.is_pinned() and b1.dtype == torch.float32 and b1.numel() == 1 << 20
+    assert b2.data_ptr() == b1.data_ptr() + (4 << 20)
+    assert a.alloc_f32(10) is None                 # full
+    a.release(t1)
+    b3, t3 = a.alloc_f32(100)
+    assert b3.data_ptr() == b1.data_ptr()
+    a.release(t2)
+    a.release(t3)
+    assert a.pages.used == 0
