@@ -54,7 +54,7 @@ void note_launch(int k) { g_launches.fetch_add((unsigned long long)k, std::memor
 
 NX_EXPORT const char *nx_last_error(void) { return nx::g_err; }
 
-NX_EXPORT int nx_version(void) { return 10000; }
+NX_EXPORT int nx_version(void) { return 10100; }
 
 NX_EXPORT unsigned long long nx_launch_count(void) { return nx::g_launches.load(); }
 
