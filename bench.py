@@ -424,10 +424,29 @@ def bench_ours(args):
         batch.run()
         host_out.copy_(batch.heights, non_blocking=True)
         torch.cuda.synchronize()
+    serial_s = max_over_ranks(dist, time.perf_counter() - t0)
+    # the same copies pipelined through the public API: a step's heights go to
+    # the host on a side stream while the next step runs (PlanetBatch.run_to_host)
+    for _ in range(2):
+        batch.tables.copy_(host_tab, non_blocking=True)
+        batch.run_to_host(host_out)
+    batch.wait_host()
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.tables.copy_(host_tab, non_blocking=True)
+        batch.run_to_host(host_out)
+    batch.wait_host()
+    torch.cuda.synchronize()
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = {"value": world * npl * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(batch.tables.numel() * 4), "d2h_bytes_per_step": int(batch.heights.numel() * 4),
-           "note": "request tables in, all heights out to pinned host memory, per step"}
+           "note": "request tables in, all heights out to pinned host memory, every step; each step's heights are "
+                   "copied on a side stream while the next step runs (PlanetBatch.run_to_host), all copies complete "
+                   "inside the timed region",
+           "serial_value": world * npl * args.steps / serial_s,
+           "serial_note": "the same with a host synchronisation after every step's copy (no overlap)"}
 
     launches = batch.kernels_per_run() * args.steps
     serving = None

@@ -266,6 +266,48 @@ class PlanetBatch:
         else:
             self.launch()
 
+    def run_to_host(self, host_out):
+        """One run whose heights are copied into host_out (page-locked
+        float32, at least `total` elements, packed rows as `heights`),
+        pipelined for back-to-back calls: the heights alternate between two
+        device buffers, the copy of a run's heights goes on a side stream
+        while the next call's run proceeds, and a run waits only for the
+        copy that last read the buffer it writes.  `wait_host()` blocks until
+        the last copy is in host_out."""
+        if not host_out.is_pinned() or host_out.dtype != torch.float32 or host_out.numel() < self.total:
+            raise ValueError("host_out must be a page-locked float32 tensor of at least `total` elements")
+        if getattr(self, "_pipe", None) is None:
+            bufs = [self.heights, self.heights.clone()]      # same padding rows in both
+            graphs = []
+            for b in bufs:
+                self.heights = b
+                graphs.append(self.capture())
+            self._pipe = dict(bufs=bufs, graphs=graphs, side=torch.cuda.Stream(), copied=[None, None], next=0)
+        p = self._pipe
+        b = p["next"]
+        main = torch.cuda.current_stream()
+        if p["copied"][b] is not None:
+            main.wait_event(p["copied"][b])
+        self.heights = p["bufs"][b]
+        p["graphs"][b].replay()
+        ran = torch.cuda.Event()
+        ran.record(main)
+        side = p["side"]
+        side.wait_event(ran)
+        with torch.cuda.stream(side):
+            host_out[:self.total].copy_(self.heights, non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(side)
+        p["copied"][b] = done
+        p["next"] = 1 - b
+        self.graph = p["graphs"][b]
+
+    def wait_host(self):
+        """Block until the heights of the last run_to_host are on the host."""
+        p = getattr(self, "_pipe", None)
+        if p is not None and p["copied"][1 - p["next"]] is not None:
+            p["copied"][1 - p["next"]].synchronize()
+
     def erosion_launches(self):
         """Erosion launches per run: passes of the blocked path, or iterations."""
         if any(self.er_host[j].tiling for j in range(len(self.requests))):

@@ -48,6 +48,33 @@ def test_batched_equals_plain_bit_exact_and_graph_replay():
     assert torch.equal(one.results()[0].heights, h0[4])
 
 
+def test_run_to_host_pipelines_copies_of_every_run():
+    from nixis_gb300 import mesh, planets
+    reqs = small_requests()
+    cache = mesh.MeshCache()
+    b = planets.PlanetBatch(reqs, cache)
+    b.run()
+    torch.cuda.synchronize()
+    want = b.heights.cpu().numpy().copy()
+    host = torch.empty(b.total, dtype=torch.float32).pin_memory()
+    rows = np.concatenate([np.arange(b.vbeg[i], b.vbeg[i] + r.n_vertices) for i, r in enumerate(reqs)])
+    for _ in range(3):
+        host.zero_()
+        b.run_to_host(host)
+        b.wait_host()
+        assert np.array_equal(host.numpy()[rows], want[rows])
+    # back to back: the last call's copy completes with wait_host
+    for _ in range(4):
+        b.run_to_host(host)
+    b.wait_host()
+    assert np.array_equal(host.numpy()[rows], want[rows])
+    # results() views the buffer of the last run
+    for r, got in zip(reqs, b.results()):
+        assert torch.equal(got.heights, planets.generate_plain(r, cache).heights), r
+    with pytest.raises(ValueError):
+        b.run_to_host(torch.empty(b.total, dtype=torch.float32))       # not page-locked
+
+
 def test_pipeline_against_binary64_oracle():
     from nixis_gb300 import mesh, planets
     r = planets.PlanetRequest(seed=5, divisions=40, octaves=12, erosion_iters=30, insolation=True, days=30)
