@@ -502,6 +502,7 @@ def run_serving(n_requests, hbm_budget=120 * 2**30):
         tk = eng.run(stream, realtime=realtime, t0=t0)
         span = time.perf_counter() - t0
         eng_meshes = eng.meshes
+        eng.close()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         plain = serve.serve_plain(stream, meshes=pm, realtime=realtime, t0=t1)

@@ -554,6 +554,22 @@ class ServeEngine:
         self.active = still
 
     # ------------------------------------------------------------------
+    def close(self):
+        """Finish pending deliveries and stop the engine's host threads (the
+        engine is not used afterwards)."""
+        for f in self._delivering:
+            f.result()
+        self._delivering = []
+        self._pool.shutdown(wait=True)
+        self._copy_pool.shutdown(wait=True)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
+
     def run(self, stream, realtime=True, t0=None):
         """Serve (arrival_offset_seconds, request) pairs; returns tickets in
         request order with latencies (finish - arrival)."""

@@ -37,8 +37,8 @@ def check_against_alone(tickets):
 def test_served_results_equal_alone(blocked):
     """Ticks of blocked passes (default) or of single iterations."""
     from nixis_gb300 import serve
-    eng = serve.ServeEngine(hbm_budget=4 * 2**30, arena_rows=2_000_000, slots=64, blocked=blocked)
-    tickets = eng.run(small_stream())
+    with serve.ServeEngine(hbm_budget=4 * 2**30, arena_rows=2_000_000, slots=64, blocked=blocked) as eng:
+        tickets = eng.run(small_stream())
     assert eng.tick > 0
     check_against_alone(tickets)
     # the arena and slots are all returned
