@@ -703,11 +703,17 @@ NX_EXPORT int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, 
         return nx::fail(NX_EINVAL, "nx_tiling_shape: bad arguments");
     const int M = k / tile_side;
     const int64_t nt = (int64_t)20 * (M + 1) * (M + 2) / 2;
-    // ring r of a tile of side B has about 4B + 8r vertices; twice that for slack
-    const int64_t B = tile_side;
-    int64_t halo = 0;
-    for (int r = 1; r <= rings; ++r) halo += 2 * (4 * B + 8 * r) + 64;
-    int64_t nm = B * B + 2 * B + halo, cm = (B * B + 2 * B + halo + 3) & ~(int64_t)3;   // cm*12 B: 16-byte units
+    // A tile holds at most B x B members of one face grid.  On the lattice
+    // of the face grids (six neighbours: (+-1, 0), (0, +-1), (+1, -1),
+    // (-1, +1)) the vertices within graph distance R of a B x B square form
+    // the square widened by R on every side less two corners, fewer than
+    // (B + 2R)^2; at the twelve five-neighbour corners the count only drops.
+    // The bounds keep 4(B + 2R) of slack (overflow is still detected and
+    // reported by the build); the updatable set (rings below R) uses R - 1.
+    const int64_t B = tile_side, D = B + 2 * (int64_t)rings, Dc = D - 2;
+    int64_t nm = D * D + 4 * D;
+    int64_t cm = (Dc * Dc + 4 * Dc + 3) & ~(int64_t)3;   // cm*12 B: 16-byte units
+    if (cm > nm) cm = nm & ~(int64_t)3;
     if (nm > 4096) return nx::fail(NX_EINVAL, "nx_tiling_shape: tile too large (%lld local vertices)", (long long)nm);
     if (nt > 0x7FFFFFFF) return nx::fail(NX_EINVAL, "nx_tiling_shape: too many tiles");
     *ntiles = (int32_t)nt;
