@@ -521,14 +521,16 @@ def run_serving(n_requests, hbm_budget=120 * 2**30):
 
 def profile_extras():
     """One run of each kernel outside the batch on a mid-size sphere
-    (divisions 500, 2,500,002 vertices): mesh and tiling build, the height
+    (divisions 500, 2,500,002 vertices): mesh and tiling build (the default
+    blocked setting's tile side and rings), the height
     shaping sequence, the latitude-table year, an equirectangular map of
     1024 x 512 pixels.  The case the ncu summaries of those kernels use."""
     import torch
     from oracle import oracle as O
     from nixis_gb300 import mesh, terrain, util, climate
+    from nixis_gb300 import autotune
     m = mesh.PlanetMesh(500)
-    m.tiling(40, 4).maxnl
+    m.tiling(autotune.DEFAULT.tile_side, autotune.DEFAULT.rings).maxnl
     perm, pgi = O.init(3)
     h = terrain.sample_octaves(m.xyz, None, perm, pgi, 8, 1.0, 1.0, 2.0, 0.5, 1.0)
     shaped, _, _ = util.shape_heights(h)

@@ -525,17 +525,33 @@ __global__ void tile_assign_kernel(int k, int B, int64_t nv, int R, int nmax, in
     }
 }
 
-constexpr int HASH_BITS = 13;                 // 8192-entry set per tile
-constexpr int HASH_CAP = 1 << HASH_BITS;
+// Per-tile hash set of vertex ids in shared memory: 2^bits entries, the
+// smallest power of two with at least twice the tile's local bound (load
+// factor <= 1/2), linear probing.
+struct HashSet {
+    int bits;
+    uint32_t mask;
+};
 
-__device__ __forceinline__ uint32_t hslot(int32_t v) { return ((uint32_t)v * 2654435761u) >> (32 - HASH_BITS); }
+__host__ __device__ __forceinline__ int hash_bits_for(int nmax)
+{
+    int b = 6;
+    while ((1 << b) < 2 * nmax) ++b;
+    return b;
+}
+
+__device__ __forceinline__ uint32_t hslot(const HashSet &H, int32_t v)
+{
+    return ((uint32_t)v * 2654435761u) >> (32 - H.bits);
+}
 
 // Insert v (bounded probing); returns its local index, assigning the next
 // one if v is new.  -1 if the set or the list is full.
-__device__ __forceinline__ int hinsert(int32_t *key, int32_t *val, int32_t *list, int *cnt, int nmax, int32_t v)
+__device__ __forceinline__ int hinsert(const HashSet &H, int32_t *key, int32_t *val, int32_t *list, int *cnt, int nmax,
+                                       int32_t v)
 {
-    uint32_t h = hslot(v);
-    for (int probe = 0; probe < HASH_CAP; ++probe) {
+    uint32_t h = hslot(H, v);
+    for (uint32_t probe = 0; probe <= H.mask; ++probe) {
         const int32_t old = atomicCAS(&key[h], -1, v);
         if (old == -1) {
             const int idx = atomicAdd(cnt, 1);
@@ -545,19 +561,19 @@ __device__ __forceinline__ int hinsert(int32_t *key, int32_t *val, int32_t *list
             return idx;
         }
         if (old == v) return 0;       // present (its index is read after a barrier)
-        h = (h + 1) & (HASH_CAP - 1);
+        h = (h + 1) & H.mask;
     }
     return -1;
 }
 
-__device__ __forceinline__ int hfind(const int32_t *key, const int32_t *val, int32_t v)
+__device__ __forceinline__ int hfind(const HashSet &H, const int32_t *key, const int32_t *val, int32_t v)
 {
-    uint32_t h = hslot(v);
-    for (int probe = 0; probe < HASH_CAP; ++probe) {
+    uint32_t h = hslot(H, v);
+    for (uint32_t probe = 0; probe <= H.mask; ++probe) {
         const int32_t kk = key[h];
         if (kk == v) return val[h];
         if (kk == -1) return -1;
-        h = (h + 1) & (HASH_CAP - 1);
+        h = (h + 1) & H.mask;
     }
     return -1;
 }
@@ -568,9 +584,13 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
                                                          float *__restrict__ ledge, int *__restrict__ err)
 {
     extern __shared__ int32_t sh[];
-    int32_t *key = sh;                      // HASH_CAP
-    int32_t *val = key + HASH_CAP;          // HASH_CAP
-    int32_t *list = val + HASH_CAP;         // local vertices; list + nmax: sort scratch
+    HashSet H;
+    H.bits = hash_bits_for(nmax);
+    H.mask = (1u << H.bits) - 1u;
+    const int hcap = 1 << H.bits;
+    int32_t *key = sh;                      // hcap
+    int32_t *val = key + hcap;              // hcap
+    int32_t *list = val + hcap;             // local vertices; list + nmax: sort scratch
     __shared__ int s_cnt, s_bad;
     __shared__ int s_ring[16];
     const int64_t tile = blockIdx.x;
@@ -580,7 +600,7 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
     if (T > nmax) T = nmax;
     int P2 = 1;
     while (P2 < T) P2 <<= 1;
-    for (int q = threadIdx.x; q < HASH_CAP; q += blockDim.x) key[q] = -1;
+    for (int q = threadIdx.x; q < hcap; q += blockDim.x) key[q] = -1;
     for (int q = threadIdx.x; q < P2; q += blockDim.x) list[q] = q < T ? tid[q] : 0x7FFFFFFF;
     if (threadIdx.x == 0) { s_cnt = 0; s_bad = 0; }
     __syncthreads();
@@ -600,10 +620,10 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
     for (int q = threadIdx.x; q < T; q += blockDim.x) {
         // members take local indices 0..T-1 in sorted order
         const int32_t v = list[q];
-        uint32_t h = hslot(v);
-        for (int probe = 0; probe < HASH_CAP; ++probe) {
+        uint32_t h = hslot(H, v);
+        for (uint32_t probe = 0; probe <= H.mask; ++probe) {
             if (atomicCAS(&key[h], -1, v) == -1) { val[h] = q; break; }
-            h = (h + 1) & (HASH_CAP - 1);
+            h = (h + 1) & H.mask;
         }
     }
     if (threadIdx.x == 0) s_cnt = T;
@@ -616,7 +636,7 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
             const int32_t j = nbr[6 * (int64_t)v + (w % 6)];
             if (j < 0) continue;
             if ((int64_t)j >= nv) { s_bad = 1; continue; }
-            if (hinsert(key, val, list, &s_cnt, nmax, j) < 0) s_bad = 1;
+            if (hinsert(H, key, val, list, &s_cnt, nmax, j) < 0) s_bad = 1;
         }
         __syncthreads();
         beg = end;
@@ -653,10 +673,10 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
             for (int q = threadIdx.x; q < ln; q += blockDim.x) {
                 const int32_t v = scr[q];
                 list[rb + q] = v;
-                uint32_t h = hslot(v);
-                for (int probe = 0; probe < HASH_CAP; ++probe) {
+                uint32_t h = hslot(H, v);
+                for (uint32_t probe = 0; probe <= H.mask; ++probe) {
                     if (key[h] == v) { val[h] = rb + q; break; }
-                    h = (h + 1) & (HASH_CAP - 1);
+                    h = (h + 1) & H.mask;
                 }
             }
             __syncthreads();
@@ -676,7 +696,7 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
         // the erosion update then sees equal heights and adds nothing
         int loc = q;
         if (j >= 0) {
-            loc = hfind(key, val, j);
+            loc = hfind(H, key, val, j);
             if (loc < 0) { s_bad = 1; loc = q; }
         }
         lnbr[((int64_t)tile * cmax + q) * 6 + sl] = (uint16_t)loc;
@@ -742,7 +762,7 @@ NX_EXPORT int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nb
     int P2 = 1;
     while (P2 < nmax) P2 <<= 1;
     // hash keys + values, the local list (padded for sorting) and a scratch
-    const size_t smem = sizeof(int32_t) * (2 * (size_t)HASH_CAP + 2 * (size_t)P2);
+    const size_t smem = sizeof(int32_t) * (2 * ((size_t)1 << hash_bits_for(nmax)) + 2 * (size_t)P2);
     NX_CHECK_CUDA(cudaFuncSetAttribute(tile_rings_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     tile_rings_kernel<<<nt, 512, smem, s>>>(nbr_dev, edge_dev, nv, rings, nmax, cmax, counts_dev, ids_dev, lnbr_dev,
                                             ledge_dev, err_dev);
