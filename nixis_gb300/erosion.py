@@ -104,6 +104,12 @@ def _run_inplace(verts, neighbors, h, w, s, iters, rain, with_fields):
             continue
         if host and (not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous):
             raise ValueError("fields must be C-contiguous float64 arrays")
+    if len(verts) == 0:
+        # the reference's loop over vertices runs zero times
+        for a, name in ((h, "heights"), (w, "water"), (s, "sediment")):
+            if a is not None and tuple(a.shape) != (0,):
+                raise ValueError(f"{name}: expected shape (0,), got {tuple(a.shape)}")
+        return
     run = ErosionRun(verts, neighbors)
     hd = _dev.to_device(h, np.float64, (run.n,), "heights")
     wd = _dev.to_device(w, np.float64, (run.n,), "water") if w is not None else None
