@@ -68,3 +68,13 @@ def test_replica_timing_takes_the_max_over_ranks():
         p.join(120)
     assert all(p.exitcode == 0 for p in ps)
     assert out[0] == out[1] == 11.0
+
+
+def test_divisions_limits():
+    # vertex ids are int32: 10 k^2 + 2 <= 2^31 - 1 holds up to k = 14654
+    import pytest
+    from nixis_gb300 import icosphere
+    assert icosphere.check_divisions(14654) == 14654
+    for bad in (0, -1, 14655):
+        with pytest.raises(ValueError):
+            icosphere.check_divisions(bad)
