@@ -118,9 +118,28 @@ class PinnedArena:
             self.pages.release(*token)
 
 
+def _victim(lru, refs, upcoming=None):
+    """The mesh to evict: among the unreferenced resident ones (`lru`,
+    least recently used first), one that no known upcoming request needs,
+    else the one needed last (Belady's rule over the requests that have
+    arrived); the least recently used among equals.  None if all are in
+    use."""
+    free = [q for q in lru if refs.get(q, 0) == 0]
+    if not free:
+        return None
+    if not upcoming:
+        return free[0]
+    first = {}
+    for i, k in enumerate(upcoming):
+        first.setdefault(k, i)
+    never = len(upcoming)
+    return max(free, key=lambda q: first.get(q, never))    # max keeps the first of equals
+
+
 class ResidentMeshes:
-    """Meshes in HBM with reference counts; unreferenced ones are evicted
-    least recently used when the budget requires it."""
+    """Meshes in HBM with reference counts; when the budget requires it,
+    unreferenced ones are evicted, those not needed by the requests that
+    have arrived (`upcoming`, divisions in order of expected use) first."""
 
     def __init__(self, budget_bytes, tb=None):
         self.budget = budget_bytes
@@ -128,6 +147,7 @@ class ResidentMeshes:
         self.meshes = {}
         self.refs = {}
         self.lru = []
+        self.upcoming = None
 
     def bytes_for(self, k):
         return 0 if k in self.meshes else _planets.mesh_bytes(k, self.tb)
@@ -147,7 +167,7 @@ class ResidentMeshes:
         if k not in self.meshes:
             need = _planets.mesh_bytes(k, self.tb)
             while self.resident_bytes() + need > self.budget:
-                victim = next((q for q in self.lru if self.refs.get(q, 0) == 0), None)
+                victim = _victim(self.lru, self.refs, self.upcoming)
                 if victim is None:
                     break
                 self.lru.remove(victim)
@@ -277,6 +297,8 @@ class ServeEngine:
 
     def _admit(self, now):
         admitted = []
+        if self.queue and self.queue[0].arrival <= now:
+            self.meshes.upcoming = [t.request.divisions for t in self.queue if t.arrival <= now]
         while self.queue and self.queue[0].arrival <= now:
             t = self.queue[0]
             r = t.request
@@ -602,11 +624,14 @@ def serve_plain(stream, meshes=None, realtime=True, t0=None):
     meshes = meshes if meshes is not None else ResidentMeshes(80 * 2**30)
     t0 = time.perf_counter() if t0 is None else t0
     out = []
-    for a, r in stream:
+    for idx, (a, r) in enumerate(stream):
         arrival = t0 + a if realtime else t0
         now = time.perf_counter()
         if now < arrival:
             time.sleep(arrival - now)
+            now = time.perf_counter()
+        # the same mesh eviction as the engine: requests that have arrived
+        meshes.upcoming = [r2.divisions for a2, r2 in stream[idx:] if (t0 + a2 if realtime else t0) <= now]
         res = _planets.generate_plain(r, meshes, sync=False)
         h = res.heights.cpu()
         i = res.insolation.cpu() if res.insolation is not None else None

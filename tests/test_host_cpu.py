@@ -78,3 +78,15 @@ def test_divisions_limits():
     for bad in (0, -1, 14655):
         with pytest.raises(ValueError):
             icosphere.check_divisions(bad)
+
+
+def test_mesh_eviction_prefers_meshes_no_arrived_request_needs():
+    from nixis_gb300.serve import _victim
+    lru = [100, 200, 300, 400]                       # least recently used first
+    refs = {300: 1}                                  # in use: never evicted
+    assert _victim(lru, refs) == 100                 # no queue: least recently used
+    assert _victim(lru, refs, [100, 200]) == 400     # not needed by any arrived request
+    assert _victim(lru, refs, [400, 100, 200]) == 200    # needed last
+    assert _victim(lru, refs, [100, 200, 400]) == 400
+    assert _victim([300], refs, [100]) is None
+    assert _victim(lru, {}, [999]) == 100            # none needed: least recently used
