@@ -196,6 +196,8 @@ class Ticket:
     arrival: float
     index: int
     admitted: float = None
+    ready: float = None          # host time the planet joined the erosion ticks (or went to output)
+    eroded: float = None         # host time its last tick was launched
     finished: float = None
     heights: np.ndarray = None
     insolation: np.ndarray = None
@@ -384,6 +386,7 @@ class ServeEngine:
                     self._insolation(t, ev)
                 if r.erosion_iters == 0:
                     t.stage = "output"
+                    t.ready = t.eroded = time.perf_counter()
                 else:
                     t.stage = "waiting"
 
@@ -482,6 +485,7 @@ class ServeEngine:
                 t.mesh.check()
                 self.main.wait_event(t.ready_event)
                 t.stage = "eroding"
+                t.ready = time.perf_counter()
                 t.t_start = self.tick
             elif t.stage == "output":
                 self._output(t, after_main=False)
@@ -502,6 +506,7 @@ class ServeEngine:
             for t in er:
                 if self.tick - t.t_start == self._ticks_of(t, blocked):
                     t.stage = "finishing"
+                    t.eroded = time.perf_counter()
                     self._output(t, after_main=True)
             ev = torch.cuda.Event()
             ev.record(self.main)
@@ -576,6 +581,20 @@ class ServeEngine:
         self.active = still
 
     # ------------------------------------------------------------------
+    def warmup(self):
+        """Serve two tiny requests (divisions 2; one with erosion and
+        insolation, one without) so that every kernel the engine launches is
+        loaded and configured before real requests arrive: the first launch
+        of a kernel loads its module, and setting the blocked kernels'
+        shared-memory limits touches all of them, which otherwise lands on
+        the first requests' latency."""
+        tiny = [(0.0, _planets.PlanetRequest(seed=0, divisions=2, octaves=2, erosion_iters=3, insolation=True,
+                                              days=2, hours=24)),
+                (0.0, _planets.PlanetRequest(seed=1, divisions=2, octaves=2, erosion_iters=0))]
+        self.run(tiny, realtime=False)
+        self.done = []
+        return self
+
     def close(self):
         """Finish pending deliveries and stop the engine's host threads (the
         engine is not used afterwards)."""

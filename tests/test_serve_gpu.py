@@ -38,6 +38,8 @@ def test_served_results_equal_alone(blocked):
     """Ticks of blocked passes (default) or of single iterations."""
     from nixis_gb300 import serve
     with serve.ServeEngine(hbm_budget=4 * 2**30, arena_rows=2_000_000, slots=64, blocked=blocked) as eng:
+        eng.warmup()
+        assert eng.done == [] and eng.arena.used == 0
         tickets = eng.run(small_stream())
     assert eng.tick > 0
     check_against_alone(tickets)
