@@ -264,7 +264,7 @@ def bench_reference(args):
     wall = time.perf_counter() - t0
     T = rates.batch_seconds(reqs)
     v = len(reqs) / T
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": config(reqs), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
