@@ -273,7 +273,8 @@ class PlanetBatch:
         device buffers, the copy of a run's heights goes on a side stream
         while the next call's run proceeds, and a run waits only for the
         copy that last read the buffer it writes.  `wait_host()` blocks until
-        the last copy is in host_out."""
+        the last copy is in host_out.  The first call captures the two CUDA
+        graphs (one per buffer; an eager run and a synchronisation each)."""
         if not host_out.is_pinned() or host_out.dtype != torch.float32 or host_out.numel() < self.total:
             raise ValueError("host_out must be a page-locked float32 tensor of at least `total` elements")
         if getattr(self, "_pipe", None) is None:
