@@ -302,6 +302,11 @@ int nx_erosion_npass(int iters);
  * nx_erosion_heights_batch). */
 int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
 
+/* The same after each listed planet's last blocked pass (nx_erosion_passes,
+ * with the rings currently configured): the control slots rotate per pass,
+ * so the final exponent and maximum are those of the planet's pass count. */
+int nx_erosion_finish_passes(const nx_erosion_planet *planets_dev, int nplanets, void *workspace, void *stream);
+
 /* Temporal blocking settings (process wide, default 4 rings, 512 threads,
  * variant 0, enabled): the ring count of the tilings that batches use
  * (passes have up to that many iterations), threads per block of the

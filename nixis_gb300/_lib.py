@@ -49,6 +49,7 @@ SIGNATURES = {
     "nx_erosion_steps_noalloc": (_i32, [_p, _p, _i64, _p, _i32, ctypes.c_float, _p, _p, _p]),
     "nx_erosion_tick": (_i32, [_p, _p, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_finish": (_i32, [_p, _i32, _p, _p]),
+    "nx_erosion_finish_passes": (_i32, [_p, _i32, _p, _p]),
     "nx_erosion_ticks": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_passes": (_i32, [_p, _p, _i32, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_npass": (_i32, [_i32]),

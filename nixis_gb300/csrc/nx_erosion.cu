@@ -1210,6 +1210,21 @@ NX_EXPORT int nx_erosion_finish(const nx_erosion_planet *planets_dev, int nplane
     return NX_OK;
 }
 
+// The same after a planet's last blocked pass (nx_erosion_passes): its
+// control slots rotate per pass, so the final ones are those of its pass
+// count, not of its iteration count.
+NX_EXPORT int nx_erosion_finish_passes(const nx_erosion_planet *planets_dev, int nplanets, void *workspace,
+                                       void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !workspace) return nx::fail(NX_EINVAL, "nx_erosion_finish_passes: null pointer");
+    erosion_tb_rebase_kernel<<<(nplanets + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+        planets_dev, nplanets, g_tb_rings, (nx_erosion_ctl *)workspace);
+    NX_CHECK_LAUNCH("erosion_tb_rebase_kernel");
+    nx::note_launch(1);
+    return NX_OK;
+}
+
 NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *st_dev,
                                float *st_tmp_dev, int iters, float rain, nx_erosion_planet *planet_dev,
                                double *mass_dev, uint16_t *flow_dev, void *workspace, size_t ws_bytes, void *stream)

@@ -425,7 +425,7 @@ class ServeEngine:
         s = _dev.stream_handle(stream)
         with torch.cuda.stream(stream):
             if r.erosion_iters > 0:
-                call("nx_erosion_finish", _dev.ptr(e_dev), 1, ws, s)
+                call("nx_erosion_finish_passes" if self.blocked else "nx_erosion_finish", _dev.ptr(e_dev), 1, ws, s)
             call("nx_erosion_heights_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
                  ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg), ws,
                  ctypes.c_void_p(self.heights.data_ptr() + 4 * t.vbeg), s)
