@@ -66,6 +66,47 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
     const float x = (float)X, y = (float)Y, z = (float)Z;
     float tot = 0.0f, comp = 0.0f;          // Kahan over tilts
     const int nr = HP > 0 ? HP : a.n_rot;
+    if (on_sphere && HP > 0 && (HP & 1) == 0 && a.pairs) {
+        // u = A cos(theta) + B sin(theta) = k U(theta) with k = cos(tau) and
+        // U = x cos(theta) - y sin(theta) the same for every day, so per day
+        //   sum_h max(|C|, |u_h|) = |k| sum_h max(|C| / |k|, |U_h|)
+        // (exact in real arithmetic): |U_h| is formed once per vertex and a
+        // day costs a max and an add per rotation pair.  Days with |k| near 0
+        // take the direct form.
+        float au[HP > 0 ? HP : 2];
+#pragma unroll
+        for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
+            const float2 q = a.rot[h];
+            au[h] = fabsf(fmaf(x, q.x, -(y * q.y)));
+        }
+        for (int d = 0; d < a.n_tilt; ++d) {
+            const float2 t = a.tilt[d];
+            const float C = z * t.y, aC = fabsf(C), ak = fabsf(t.x);
+            float s;
+            if (ak >= 0x1p-20f) {
+                const float c = __fdividef(aC, ak);
+                float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 2); h += 2)
+                    acc = __fadd2_rn(acc, make_float2(fmaxf(c, au[h]), fmaxf(c, au[h + 1])));
+                s = fmaf(ak, acc.x + acc.y, (float)HP * C);
+            } else {
+                const float A = x * t.x, B = -(y * t.x);
+                s = 0.0f;
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
+                    const float2 q = a.rot[h];
+                    s += fmaxf(aC, fabsf(fmaf(A, q.x, B * q.y)));
+                }
+                s = fmaf((float)HP, C, s);
+            }
+            float yk = s - comp;
+            float tk = tot + yk;
+            comp = (tk - tot) - yk;
+            tot = tk;
+        }
+        return tot * inv_r;
+    }
     if (on_sphere) {
         float2 rt[HP > 0 ? HP : 1];
         if (HP > 0) {
