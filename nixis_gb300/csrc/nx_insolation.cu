@@ -57,8 +57,25 @@ __device__ __forceinline__ float general_term(float x, float y, float z, float i
 }
 
 // Sum over the schedule for one vertex.
+// Tilts whose per-day constants a block stages in shared memory (16 B each).
+constexpr int TILT_STAGE_MAX = 2048;
+
+// Per-day constants of the factored pair sum: (|cos tau|, |sin tau| / |cos
+// tau| or -1 when |cos tau| < 2^-20, HP sin tau, sin tau).
 template <int HP>
-__device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double Y, double Z, double r, float inv_r)
+__device__ __forceinline__ void stage_tilts(const InsoArgs &a, float4 *tt)
+{
+    for (int d = threadIdx.x; d < a.n_tilt; d += blockDim.x) {
+        const float2 t = a.tilt[d];
+        const float ak = fabsf(t.x);
+        tt[d] = make_float4(ak, ak >= 0x1p-20f ? __fdiv_rn(fabsf(t.y), ak) : -1.0f, (float)HP * t.y, t.y);
+    }
+    __syncthreads();
+}
+
+template <int HP>
+__device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double Y, double Z, double r, float inv_r,
+                                             const float4 *tt = nullptr)
 {
     const double rho2 = X * X + Y * Y + Z * Z;
     const double r2 = r * r;
@@ -78,6 +95,38 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
         for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
             const float2 q = a.rot[h];
             au[h] = fabsf(fmaf(x, q.x, -(y * q.y)));
+        }
+        if (tt) {
+            // constants staged by the block: per day a shared load, one
+            // multiply for the threshold and the max / add of each pair
+            const float az = fabsf(z);
+            for (int d = 0; d < a.n_tilt; ++d) {
+                const float4 k = tt[d];
+                float s;
+                if (k.y >= 0.0f) {
+                    const float c = az * k.y;
+                    float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+                    for (int h = 0; h < (HP > 0 ? HP : 2); h += 2)
+                        acc = __fadd2_rn(acc, make_float2(fmaxf(c, au[h]), fmaxf(c, au[h + 1])));
+                    s = fmaf(k.x, acc.x + acc.y, z * k.z);
+                } else {
+                    const float2 t = a.tilt[d];
+                    const float A = x * t.x, B = -(y * t.x), C = z * t.y, aC = fabsf(C);
+                    s = 0.0f;
+#pragma unroll
+                    for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
+                        const float2 q = a.rot[h];
+                        s += fmaxf(aC, fabsf(fmaf(A, q.x, B * q.y)));
+                    }
+                    s = fmaf((float)HP, C, s);
+                }
+                float yk = s - comp;
+                float tk = tot + yk;
+                comp = (tk - tot) - yk;
+                tot = tk;
+            }
+            return tot * inv_r;
         }
         for (int d = 0; d < a.n_tilt; ++d) {
             const float2 t = a.tilt[d];
@@ -165,8 +214,12 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
 template <int HP>
 __global__ void __launch_bounds__(256) insolation_kernel(InsoArgs a)
 {
+    extern __shared__ float4 s_tilt[];
+    const bool staged = HP > 0 && a.pairs && a.n_tilt <= TILT_STAGE_MAX;
+    if (staged) stage_tilts<HP>(a, s_tilt);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
-        float tot = inso_vertex<HP>(a, a.xyz[3 * i], a.xyz[3 * i + 1], a.xyz[3 * i + 2], a.r, a.inv_r);
+        float tot = inso_vertex<HP>(a, a.xyz[3 * i], a.xyz[3 * i + 1], a.xyz[3 * i + 2], a.r, a.inv_r,
+                                    staged ? s_tilt : nullptr);
         a.out[i] = a.accumulate ? a.out[i] + tot : tot;
     }
 }
@@ -177,6 +230,9 @@ template <int HP>
 __global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const nx_inso_planet *__restrict__ P, int np,
                                                                int64_t total_rows)
 {
+    extern __shared__ float4 s_tilt[];
+    const bool staged = HP > 0 && a.pairs && a.n_tilt <= TILT_STAGE_MAX;
+    if (staged) stage_tilts<HP>(a, s_tilt);
     for (int64_t blk = blockIdx.x; blk * 256 < total_rows; blk += gridDim.x) {
         const int64_t row = blk * 256 + threadIdx.x;
         int lo = 0, hi = np - 1;
@@ -188,7 +244,8 @@ __global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const
         const int64_t i = row - pl.vbeg;
         if (i < 0 || i >= pl.n) continue;
         const double r = pl.radius;
-        float tot = inso_vertex<HP>(a, pl.xyz[3 * i], pl.xyz[3 * i + 1], pl.xyz[3 * i + 2], r, (float)(1.0 / r));
+        float tot = inso_vertex<HP>(a, pl.xyz[3 * i], pl.xyz[3 * i + 1], pl.xyz[3 * i + 2], r, (float)(1.0 / r),
+                                    staged ? s_tilt : nullptr);
         a.out[row] = tot;
     }
 }
@@ -317,6 +374,12 @@ __global__ void __launch_bounds__(256) surface_temp_kernel(const double *__restr
     }
 }
 
+// Dynamic shared memory of the 12-pair kernels: the staged tilt constants.
+size_t tilt_smem(const InsoArgs &a)
+{
+    return (a.pairs && a.n_tilt <= TILT_STAGE_MAX) ? sizeof(float4) * (size_t)a.n_tilt : 0;
+}
+
 int grid_for(int64_t n)
 {
     int64_t g = (n + 255) / 256;
@@ -386,7 +449,7 @@ NX_EXPORT int nx_insolation(const double *xyz_dev, int64_t n, double radius, con
     a.out = out_dev;
     a.accumulate = accumulate;
     if (a.pairs && n_rot_entries == 12)
-        insolation_kernel<12><<<grid_for(n), 256, 0, s>>>(a);
+        insolation_kernel<12><<<grid_for(n), 256, tilt_smem(a), s>>>(a);
     else
         insolation_kernel<0><<<grid_for(n), 256, 0, s>>>(a);
     NX_CHECK_LAUNCH("insolation_kernel");
@@ -423,7 +486,7 @@ NX_EXPORT int nx_insolation_batch(const nx_inso_planet *planets_dev, const nx_in
     cudaStream_t s = (cudaStream_t)stream;
     int grid = grid_for(total);
     if (a.pairs && n_rot_entries == 12)
-        insolation_batch_kernel<12><<<grid, 256, 0, s>>>(a, planets_dev, nplanets, total);
+        insolation_batch_kernel<12><<<grid, 256, tilt_smem(a), s>>>(a, planets_dev, nplanets, total);
     else
         insolation_batch_kernel<0><<<grid, 256, 0, s>>>(a, planets_dev, nplanets, total);
     NX_CHECK_LAUNCH("insolation_batch_kernel");
