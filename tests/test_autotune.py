@@ -52,3 +52,18 @@ def test_tuning_keeps_results_and_applies_the_choice():
         torch.cuda.synchronize()
         assert torch.equal(bt.results()[0].heights, plain), c
     A.use(A.DEFAULT)
+
+
+def test_candidates_cover_the_default_and_fit_the_limits():
+    # nx_tiling_shape is host-only: candidates need only the mesh's divisions
+    from types import SimpleNamespace
+    from nixis_gb300 import autotune as A
+    c = A.candidates(SimpleNamespace(k=800))
+    assert A.DEFAULT in c
+    assert {cfg.variant for cfg in c} == set(A.DEFAULT_VARIANTS)
+    for cfg in c:
+        assert cfg.tile_side in A.SIDES and cfg.rings in A.RINGS
+        assert (cfg.threads, cfg.variant) in A.THREADS
+    # variants 4 and 5 only where their resident blocks' shared memory fits
+    assert not A.fits(A.TbConfig(48, 4, 256, 5), (48 + 8) ** 2, (48 + 6) ** 2)
+    assert A.fits(A.DEFAULT, (32 + 8) ** 2, (32 + 6) ** 2)
