@@ -2,7 +2,10 @@
  * nixis_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the Nixis
  * per-vertex terrain hot path: fractal OpenSimplex-3D noise, erosion
  * (variant 3) and insolation accumulation, plus the icosphere/adjacency
- * generator that feeds them.
+ * generator that feeds them, the batched and served multi-planet paths,
+ * and the next functions around them: height shaping (rescale,
+ * power_rescale, percentiles, masks), latitude-table insolation, starting
+ * surface temperatures and equirectangular map sampling.
  *
  * Conventions
  *  - Every function returns an int status: NX_OK (0) or one of the NX_E*
