@@ -127,7 +127,12 @@ class PlanetMesh:
     def __init__(self, divisions, stream=None, defer_checks=False):
         self.k = ico.check_divisions(divisions)
         self.n = ico.counts(self.k)[0]
+        s = stream if stream is not None else torch.cuda.current_stream()
         xyz, tris = icosphere(self.k, stream=stream)
+        # the vertices alone are ready here (work that needs only them, like
+        # the noise, can start on another stream while the rest is built)
+        self.xyz_ready = torch.cuda.Event()
+        self.xyz_ready.record(s)
         adj, aerr = _adjacency(tris, stream)
         del tris
         nbr = torch.empty_like(adj)

@@ -16,12 +16,14 @@ frees up:
 * admission is first-come first-served against the HBM budget (arena +
   meshes).
 
-A newly admitted planet's fBm, rescale and initial state run on a side
-stream while the main stream keeps eroding the others; it joins the next
-tick.  Its insolation (which needs only the vertices) starts at admission on
+A newly admitted planet's mesh and tiling (when not resident) are built on
+a side stream; its fBm, rescale and initial state run on a noise stream
+that starts as soon as the vertices exist (the noise needs nothing else),
+while the main stream keeps eroding the others; it joins the next tick once
+both are done.  Its insolation (which needs only the vertices) starts at admission on
 a third stream, beside its erosion.  A planet that finishes erosion gets
 its heights (main stream), then the copy of its results to page-locked host
-memory on the side stream; a host thread moves them into ordinary arrays
+memory on a copy stream; a host thread moves them into ordinary arrays
 (the request's results) while the engine keeps launching.  Results are the
 same bits as the planet generated alone (planets.generate_plain).
 
@@ -211,6 +213,7 @@ class Ticket:
     host_h: torch.Tensor = None
     host_i: torch.Tensor = None
     host_tokens: list = field(default_factory=list)
+    mesh_done: object = None
     done_event: object = None
     ready_event: object = None
     inso_event: object = None
@@ -261,7 +264,9 @@ class ServeEngine:
         self.free_slots = list(range(slots))
         self.meshes = ResidentMeshes(self.budget - R * ROW_BYTES - self.ws.numel(), self.tb)
         self.main = torch.cuda.Stream()
-        self.side = torch.cuda.Stream()
+        self.side = torch.cuda.Stream()            # meshes and tilings
+        self.fbm_stream = torch.cuda.Stream()      # new planets' noise and initial state
+        self.copy_stream = torch.cuda.Stream()     # results to the host
         self.inso_stream = torch.cuda.Stream()
         self.desc_dev = torch.empty(slots * ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device=dev)
         self.chunk = int(lib().nx_fbm_chunk_size())
@@ -326,19 +331,27 @@ class ServeEngine:
                 t.mesh = self.meshes.acquire(r.divisions)
                 t.tiling = (t.mesh.tiling(self.tb.tile_side, self.tb.rings, stream=self.side)
                             if self.blocked and r.erosion_iters > 0 else None)
+                t.mesh_done = torch.cuda.Event()
+                t.mesh_done.record(self.side)
             admitted.append(t)
         return admitted
 
     def _launch_new(self, new):
-        """fBm + rescale + initial state of newly admitted planets (side stream)."""
-        s = _dev.stream_handle(self.side)
+        """fBm + rescale + initial state of newly admitted planets, on their
+        own stream: the noise needs only the vertices, so it starts as soon
+        as they exist and overlaps the rest of a new mesh's build (adjacency,
+        edge lengths, tiling) on the side stream."""
+        fs = self.fbm_stream
+        s = _dev.stream_handle(fs)
         n = len(new)
+        for t in new:
+            fs.wait_event(t.mesh.xyz_ready)
         fb = (FbmPlanet * n)()
         c0 = 0
         tabs = np.zeros((n, 2, 256), np.int32)
         for j, t in enumerate(new):
             tabs[j, 0], tabs[j, 1] = _osx.init(t.request.seed)
-        with torch.cuda.stream(self.side):
+        with torch.cuda.stream(fs):
             tab_dev = _pinned(tabs).to("cuda", non_blocking=True)
             mm = torch.tensor([[-1, 0]] * n, dtype=torch.int64).to(torch.int32)
             mm[:, 0] = -1
@@ -378,8 +391,11 @@ class ServeEngine:
                      ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg),
                      ctypes.c_void_p(self.st_tmp.data_ptr() + 32 * t.vbeg), s)
                 t._e_single = (e, e_dev)
+                # ready: its noise and state (this stream) and its mesh and
+                # tiling (side stream) are done
+                fs.wait_event(t.mesh_done)
                 ev = torch.cuda.Event()
-                ev.record(self.side)
+                ev.record(fs)
                 t.ready_event = ev
                 t._keep = (tab_dev, mm_dev, fb_dev, fb)
                 if r.insolation:
@@ -421,7 +437,9 @@ class ServeEngine:
         r = t.request
         e, e_dev = t._e_single
         ws = _dev.ptr(self.ws)
-        stream = self.main if after_main else self.side
+        stream = self.main if after_main else self.copy_stream
+        if not after_main:
+            stream.wait_event(t.ready_event)     # state written on the noise stream
         s = _dev.stream_handle(stream)
         with torch.cuda.stream(stream):
             if r.erosion_iters > 0:
@@ -431,17 +449,18 @@ class ServeEngine:
                  ctypes.c_void_p(self.heights.data_ptr() + 4 * t.vbeg), s)
         ev = torch.cuda.Event()
         ev.record(stream)
-        self.side.wait_event(ev)
+        cs = self.copy_stream
+        cs.wait_event(ev)
         n = t.mesh.n
         t.host_h = self._host_buffer(t, n)
         t.host_i = self._host_buffer(t, n) if r.insolation else None
-        with torch.cuda.stream(self.side):
+        with torch.cuda.stream(cs):
             t.host_h.copy_(self.heights[t.vbeg:t.vbeg + n], non_blocking=True)
             if t.inso_event is not None:
-                self.side.wait_event(t.inso_event)
+                cs.wait_event(t.inso_event)
                 t.host_i.copy_(self.inso[t.vbeg:t.vbeg + n], non_blocking=True)
             done = torch.cuda.Event()
-            done.record(self.side)
+            done.record(cs)
         t.done_event = done
         t.stage = "copying"
 
