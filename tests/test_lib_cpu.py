@@ -59,3 +59,28 @@ def test_descriptor_layouts_match_the_header():
     assert ctypes.sizeof(_lib.ErosionPlanet) == 72
     assert ctypes.sizeof(_lib.Tiling) == 48
     assert _lib.ErosionPlanet.maxc.offset == 64
+
+
+def test_host_only_entry_points_reject_bad_arguments():
+    """Argument checks of the host-only functions: status codes and
+    messages, no exceptions, nothing launched."""
+    from nixis_gb300 import _lib
+    L = _lib.lib()
+    i32 = ctypes.c_int32
+    nt, nm, cm = i32(), i32(), i32()
+    ok = L.nx_tiling_shape(800, 32, 4, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm))
+    assert ok == 0 and nm.value >= (32 + 8) ** 2 and cm.value >= (32 + 6) ** 2 and cm.value <= nm.value
+    assert cm.value % 4 == 0
+    assert L.nx_tiling_shape(800, 32, 9, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm)) == 1   # rings
+    assert L.nx_tiling_shape(800, 1, 4, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm)) == 1    # side
+    assert L.nx_tiling_shape(4000, 200, 4, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm)) == 1  # too large
+    assert b"too large" in L.nx_last_error()
+    # blocked-kernel settings: threads must go with the variant
+    assert L.nx_erosion_tb_config(4, 384, 4, 1) == 0
+    assert L.nx_erosion_tb_config(4, 384, 0, 1) == 1
+    assert b"do not go with" in L.nx_last_error()
+    assert L.nx_erosion_tb_config(0, 512, 0, 1) == 1
+    assert L.nx_erosion_tb_config(4, 384, 4, 1) == 0
+    # passes of a blocked run: ceil(iters / 4) made to the parity of iters
+    for it, want in ((0, 0), (1, 1), (4, 2), (5, 3), (8, 2), (9, 3), (100, 26), (101, 27)):
+        assert L.nx_erosion_npass(it) == want, it
