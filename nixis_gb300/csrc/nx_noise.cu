@@ -238,6 +238,60 @@ __device__ __forceinline__ void decide(T xins, T yins, T zins, T in_sum, Cmp<T, 
 }
 
 
+// Octahedron extra points (opensimplex.py:535-700) from the six comparison
+// outcomes g1 = p1 > 1, g2 = p2 > 1, t3 = p3 > 1, ale = |p1-1| <= |p2-1|,
+// a_lt = |p1-1| < |p3-1|, b_lt = |p2-1| < |p3-1| (bit k of b).  Offsets are
+// in {-1, 0, 1, 2}; a block tabulates all 64 cases once (s_olut) and the
+// per-lane decision looks its case up.
+__device__ __forceinline__ uint32_t octa_case(int b)
+{
+    const bool g1 = b & 1, g2 = b & 2, t3 = b & 4, ale = b & 8, a_lt = b & 16, b_lt = b & 32;
+    const bool swa = ale && a_lt, swb = !ale && b_lt;
+    const int oap = swa ? (t3 ? 6 : 1) : (g1 ? 3 : 4);
+    const int obp = swb ? (t3 ? 6 : 1) : (g2 ? 5 : 2);
+    const bool af = swa ? t3 : g1, bf = swb ? t3 : g2;
+    float o0x, o0y, o0z, o1x, o1y, o1z;
+    if (af == bf) {
+        const int c = af ? (oap & obp) : (oap | obp);
+        const float b = af ? 1.f : 0.f;
+        o0x = b; o0y = b; o0z = b;
+        // af: the single bit of c picks the axis that gets 2; otherwise the
+        // first axis whose bit is clear gets -1 and the others 1
+        const bool c1 = (c & 1) != 0, c2 = (c & 2) != 0;
+        const bool ax = af ? c1 : !c1, ay = af ? (!c1 && c2) : (c1 && !c2);
+        const bool az = !ax && !ay;
+        const float hit = af ? 2.f : -1.f, miss = af ? 0.f : 1.f;
+        o1x = ax ? hit : miss; o1y = ay ? hit : miss; o1z = az ? hit : miss;
+    } else {
+        const int c1 = af ? oap : obp, c2 = af ? obp : oap;
+        const bool bx = (c1 & 1) == 0, by = !bx && (c1 & 2) == 0;
+        const bool bz = !bx && !by;
+        o0x = bx ? -1.f : 1.f; o0y = by ? -1.f : 1.f; o0z = bz ? -1.f : 1.f;
+        const bool qx = (c2 & 1) != 0, qy = !qx && (c2 & 2) != 0;
+        const bool qz = !qx && !qy;
+        o1x = qx ? 2.f : 0.f; o1y = qy ? 2.f : 0.f; o1z = qz ? 2.f : 0.f;
+    }
+    const float o[6] = {o0x, o0y, o0z, o1x, o1y, o1z};
+    uint32_t w = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w |= (uint32_t)((int)o[k] + 1) << (2 * k);
+    return w;
+}
+
+__shared__ uint32_t s_olut[64];
+
+// Fill s_olut (the caller synchronises the block before use).
+__device__ __forceinline__ void init_octa_lut()
+{
+    if (threadIdx.x < 64) s_olut[threadIdx.x] = octa_case((int)threadIdx.x);
+}
+
+// Offset k of a table word: ((w >> 2k) & 3) - 1, formed in binary32.
+__device__ __forceinline__ float lut_offset(uint32_t w, int k)
+{
+    return __uint_as_float(0x4B000000u | ((w >> (2 * k)) & 3u)) - 8388609.0f;
+}
+
 // The same decision for the binary32 path without data-dependent branches
 // (lanes of a warp sit in different regions at high octaves).  Regions 0
 // and 1 are mirror images: region 1's comparisons are region 0's with both
@@ -283,31 +337,12 @@ __device__ __forceinline__ void decide_sel(float x, float y, float z, float in_s
     const float score = t3 ? p3 - 1.0f : 1.0f - p3;
     const bool ale = C.le(oas, obs);
     const bool a_lt = C.lt(oas, score), b_lt = C.lt(obs, score);
-    const bool swa = ale && a_lt, swb = !ale && b_lt;
-    const int oap = swa ? (t3 ? 6 : 1) : (g1 ? 3 : 4);
-    const int obp = swb ? (t3 ? 6 : 1) : (g2 ? 5 : 2);
-    const bool af = swa ? t3 : g1, bf = swb ? t3 : g2;
-    float o0x, o0y, o0z, o1x, o1y, o1z;
-    if (af == bf) {
-        const int c = af ? (oap & obp) : (oap | obp);
-        const float b = af ? 1.f : 0.f;
-        o0x = b; o0y = b; o0z = b;
-        // af: the single bit of c picks the axis that gets 2; otherwise the
-        // first axis whose bit is clear gets -1 and the others 1
-        const bool c1 = (c & 1) != 0, c2 = (c & 2) != 0;
-        const bool ax = af ? c1 : !c1, ay = af ? (!c1 && c2) : (c1 && !c2);
-        const bool az = !ax && !ay;
-        const float hit = af ? 2.f : -1.f, miss = af ? 0.f : 1.f;
-        o1x = ax ? hit : miss; o1y = ay ? hit : miss; o1z = az ? hit : miss;
-    } else {
-        const int c1 = af ? oap : obp, c2 = af ? obp : oap;
-        const bool bx = (c1 & 1) == 0, by = !bx && (c1 & 2) == 0;
-        const bool bz = !bx && !by;
-        o0x = bx ? -1.f : 1.f; o0y = by ? -1.f : 1.f; o0z = bz ? -1.f : 1.f;
-        const bool qx = (c2 & 1) != 0, qy = !qx && (c2 & 2) != 0;
-        const bool qz = !qx && !qy;
-        o1x = qx ? 2.f : 0.f; o1y = qy ? 2.f : 0.f; o1z = qz ? 2.f : 0.f;
-    }
+    // the octahedron's two extra points are a function of the six
+    // comparison outcomes: one lookup in the block's table (octa_lut)
+    const uint32_t w = s_olut[(g1 ? 1u : 0u) | (g2 ? 2u : 0u) | (t3 ? 4u : 0u) | (ale ? 8u : 0u) |
+                              (a_lt ? 16u : 0u) | (b_lt ? 32u : 0u)];
+    const float o0x = lut_offset(w, 0), o0y = lut_offset(w, 1), o0z = lut_offset(w, 2);
+    const float o1x = lut_offset(w, 3), o1y = lut_offset(w, 4), o1z = lut_offset(w, 5);
     const bool tet = r0 || r1;
     D.region = r0 ? 0 : (r1 ? 1 : 2);
     D.e0x = tet ? t0x : o0x; D.e0y = tet ? t0y : o0y; D.e0z = tet ? t0z : o0z;
@@ -509,6 +544,7 @@ __global__ void __launch_bounds__(256) fbm_kernel(const double *__restrict__ xyz
 {
     extern __shared__ __align__(16) uint32_t smem[];
     build_table(smem, perm, pgi);
+    init_octa_lut();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
     unsigned nfb = 0;
@@ -544,6 +580,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const double *__restrict__ x
 {
     extern __shared__ __align__(16) uint32_t smem[];
     build_table(smem, perm, pgi);
+    init_octa_lut();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
     float sh, sl;
@@ -599,6 +636,8 @@ __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__r
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint32_t s_mm[2][8];
+    init_octa_lut();
+    __syncthreads();
     const uint32_t lb = lane_base(smem);
     int cur = -1;
     unsigned nfb = 0;
