@@ -278,12 +278,43 @@ __device__ __forceinline__ uint32_t octa_case(int b)
     return w;
 }
 
-__shared__ uint32_t s_olut[64];
+// Tetrahedron extra points (opensimplex.py:302-533) from the comparison
+// outcomes, in the mirrored form the binary32 decision uses (region 1's
+// comparisons are region 0's with both sides negated): bit 0 x >= y, 1
+// z > y, 2 z > x, 3 wins > as, 4 wins > bs, 5 bs > as (as, bs the scores
+// the first three select), 6 region 1 (offsets t become 1 - t).
+__device__ __forceinline__ uint32_t tetra_case(int b)
+{
+    const bool xy = b & 1, zb = b & 2, za = b & 4, n1 = b & 8, n2 = b & 16, cnb = b & 32, r1 = b & 64;
+    const bool repb = xy && zb, repa = !xy && za;
+    const int ap = repa ? 4 : 1, bp = repb ? 4 : 2;
+    const bool near = n1 || n2;
+    const int cn = cnb ? bp : ap;
+    const int cf = ap | bp;
+    const bool cn1 = (cn & 1) != 0, cn2 = (cn & 2) != 0, cn4 = (cn & 4) != 0;
+    float t[6];
+    t[0] = near ? (cn1 ? 1.f : -1.f) : ((cf & 1) ? 1.f : 0.f);
+    t[3] = near ? (cn1 ? 1.f : 0.f) : ((cf & 1) ? 1.f : -1.f);
+    t[1] = near ? (cn2 ? 1.f : (cn1 ? -1.f : 0.f)) : ((cf & 2) ? 1.f : 0.f);
+    t[4] = near ? (cn2 ? 1.f : (cn1 ? 0.f : -1.f)) : ((cf & 2) ? 1.f : -1.f);
+    t[2] = near ? (cn4 ? 1.f : 0.f) : ((cf & 4) ? 1.f : 0.f);
+    t[5] = near ? (cn4 ? 1.f : -1.f) : ((cf & 4) ? 1.f : -1.f);
+    uint32_t w = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w |= (uint32_t)((int)(r1 ? 1.f - t[k] : t[k]) + 1) << (2 * k);
+    return w;
+}
+
+// Extra-point table of a block: [0, 64) octahedron cases, [64, 192)
+// tetrahedron cases; each word holds the six offsets (e0x, e0y, e0z, e1x,
+// e1y, e1z) + 1 in two bits each.
+__shared__ uint32_t s_olut[192];
 
 // Fill s_olut (the caller synchronises the block before use).
 __device__ __forceinline__ void init_octa_lut()
 {
-    if (threadIdx.x < 64) s_olut[threadIdx.x] = octa_case((int)threadIdx.x);
+    for (int i = threadIdx.x; i < 192; i += blockDim.x)
+        s_olut[i] = i < 64 ? octa_case(i) : tetra_case(i - 64);
 }
 
 // Offset k of a table word: ((w >> 2k) & 3) - 1, formed in binary32.
@@ -311,24 +342,10 @@ __device__ __forceinline__ void decide_sel(float x, float y, float z, float in_s
     const bool za = C.gt(s * z, s * x);
     const bool repb = xy && zb, repa = !xy && za;
     const float as = repa ? z : x, bs = repb ? z : y;
-    const int ap = repa ? 4 : 1, bp = repb ? 4 : 2;
     const float wins = (r1 ? 3.0f : 1.0f) - in_sum;
     const bool n1 = C.gt(s * wins, s * as);
     const bool n2 = C.gt(s * wins, s * bs);
-    const bool near = n1 || n2;
-    const int cn = C.gt(s * bs, s * as) ? bp : ap;
-    const int cf = ap | bp;
-    const bool cn1 = (cn & 1) != 0, cn2 = (cn & 2) != 0, cn4 = (cn & 4) != 0;
-    float t0x = near ? (cn1 ? 1.f : -1.f) : ((cf & 1) ? 1.f : 0.f);
-    float t1x = near ? (cn1 ? 1.f : 0.f) : ((cf & 1) ? 1.f : -1.f);
-    float t0y = near ? (cn2 ? 1.f : (cn1 ? -1.f : 0.f)) : ((cf & 2) ? 1.f : 0.f);
-    float t1y = near ? (cn2 ? 1.f : (cn1 ? 0.f : -1.f)) : ((cf & 2) ? 1.f : -1.f);
-    float t0z = near ? (cn4 ? 1.f : 0.f) : ((cf & 4) ? 1.f : 0.f);
-    float t1z = near ? (cn4 ? 1.f : -1.f) : ((cf & 4) ? 1.f : -1.f);
-    if (r1) {
-        t0x = 1.f - t0x; t1x = 1.f - t1x; t0y = 1.f - t0y;
-        t1y = 1.f - t1y; t0z = 1.f - t0z; t1z = 1.f - t1z;
-    }
+    const bool cnb = C.gt(s * bs, s * as);
     // octahedron
     const float p1 = x + y, p2 = x + z, p3 = y + z;
     const bool g1 = C.gt(p1, 1.0f), g2 = C.gt(p2, 1.0f), t3 = C.gt(p3, 1.0f);
@@ -337,16 +354,18 @@ __device__ __forceinline__ void decide_sel(float x, float y, float z, float in_s
     const float score = t3 ? p3 - 1.0f : 1.0f - p3;
     const bool ale = C.le(oas, obs);
     const bool a_lt = C.lt(oas, score), b_lt = C.lt(obs, score);
-    // the octahedron's two extra points are a function of the six
-    // comparison outcomes: one lookup in the block's table (octa_lut)
-    const uint32_t w = s_olut[(g1 ? 1u : 0u) | (g2 ? 2u : 0u) | (t3 ? 4u : 0u) | (ale ? 8u : 0u) |
-                              (a_lt ? 16u : 0u) | (b_lt ? 32u : 0u)];
-    const float o0x = lut_offset(w, 0), o0y = lut_offset(w, 1), o0z = lut_offset(w, 2);
-    const float o1x = lut_offset(w, 3), o1y = lut_offset(w, 4), o1z = lut_offset(w, 5);
+    // the two extra points are a function of the region's comparison
+    // outcomes: one lookup in the block's table (tetrahedron or octahedron
+    // case, see tetra_case / octa_case)
     const bool tet = r0 || r1;
+    const uint32_t ot = (g1 ? 1u : 0u) | (g2 ? 2u : 0u) | (t3 ? 4u : 0u) | (ale ? 8u : 0u) | (a_lt ? 16u : 0u) |
+                        (b_lt ? 32u : 0u);
+    const uint32_t tt = 64u + ((xy ? 1u : 0u) | (zb ? 2u : 0u) | (za ? 4u : 0u) | (n1 ? 8u : 0u) | (n2 ? 16u : 0u) |
+                               (cnb ? 32u : 0u) | (r1 ? 64u : 0u));
+    const uint32_t w = s_olut[tet ? tt : ot];
     D.region = r0 ? 0 : (r1 ? 1 : 2);
-    D.e0x = tet ? t0x : o0x; D.e0y = tet ? t0y : o0y; D.e0z = tet ? t0z : o0z;
-    D.e1x = tet ? t1x : o1x; D.e1y = tet ? t1y : o1y; D.e1z = tet ? t1z : o1z;
+    D.e0x = lut_offset(w, 0); D.e0y = lut_offset(w, 1); D.e0z = lut_offset(w, 2);
+    D.e1x = lut_offset(w, 3); D.e1y = lut_offset(w, 4); D.e1z = lut_offset(w, 5);
 }
 
 // opensimplex.py:18-21 in binary64
