@@ -114,7 +114,9 @@ __device__ __forceinline__ void split_f64(double v, float &hi, float &lo)
 // cell origin (components in {-1,0,1,2}).
 struct Decision {
     int region;
-    float e0x, e0y, e0z, e1x, e1y, e1z;
+    float e0x, e0y, e0z, e1x, e1y, e1z;   // decide() only
+    uint32_t w;                           // the offsets + 1, two bits each (e0x, e0y, e0z, e1x, e1y, e1z)
+    float E[6];                           // displacement offsets e + (ex + ey + ez) / 3 of both points
 };
 
 template <typename T, bool TRACK>
@@ -241,7 +243,7 @@ __device__ __forceinline__ void decide(T xins, T yins, T zins, T in_sum, Cmp<T, 
 // Octahedron extra points (opensimplex.py:535-700) from the six comparison
 // outcomes g1 = p1 > 1, g2 = p2 > 1, t3 = p3 > 1, ale = |p1-1| <= |p2-1|,
 // a_lt = |p1-1| < |p3-1|, b_lt = |p2-1| < |p3-1| (bit k of b).  Offsets are
-// in {-1, 0, 1, 2}; a block tabulates all 64 cases once (s_olut) and the
+// in {-1, 0, 1, 2}; a block tabulates all 64 cases once (s_extra) and the
 // per-lane decision looks its case up.
 __device__ __forceinline__ uint32_t octa_case(int b)
 {
@@ -305,22 +307,58 @@ __device__ __forceinline__ uint32_t tetra_case(int b)
     return w;
 }
 
-// Extra-point table of a block: [0, 64) octahedron cases, [64, 192)
-// tetrahedron cases; each word holds the six offsets (e0x, e0y, e0z, e1x,
-// e1y, e1z) + 1 in two bits each.
-__shared__ uint32_t s_olut[192];
-
-// Fill s_olut (the caller synchronises the block before use).
-__device__ __forceinline__ void init_octa_lut()
+// Offset k of a case word: ((w >> 2k) & 3) - 1.
+__device__ __forceinline__ int word_offset(uint32_t w, int k)
 {
-    for (int i = threadIdx.x; i < 192; i += blockDim.x)
-        s_olut[i] = i < 64 ? octa_case(i) : tetra_case(i - 64);
+    return (int)((w >> (2 * k)) & 3u) - 1;
 }
 
-// Offset k of a table word: ((w >> 2k) & 3) - 1, formed in binary32.
-__device__ __forceinline__ float lut_offset(uint32_t w, int k)
+// The displacement offsets of an extra point o: o + (ox + oy + oz) / 3
+// per component (the point's skewed position relative to the cell
+// origin's), rounded step by step.
+__device__ __forceinline__ void extra_disp(float ox, float oy, float oz, float *E)
 {
-    return __uint_as_float(0x4B000000u | ((w >> (2 * k)) & 3u)) - 8388609.0f;
+    const float s = __fmul_rn(__fadd_rn(__fadd_rn(ox, oy), oz), THIRD);
+    E[0] = __fadd_rn(ox, s);
+    E[1] = __fadd_rn(oy, s);
+    E[2] = __fadd_rn(oz, s);
+}
+
+// Case word and displacement offsets of a decision from its six offsets
+// (the binary64 path).
+__device__ __forceinline__ void pack_extra(Decision &D)
+{
+    const float o[6] = {D.e0x, D.e0y, D.e0z, D.e1x, D.e1y, D.e1z};
+    uint32_t w = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w |= (uint32_t)((int)o[k] + 1) << (2 * k);
+    D.w = w;
+    extra_disp(o[0], o[1], o[2], D.E);
+    extra_disp(o[3], o[4], o[5], D.E + 3);
+}
+
+// Extra-point table of a block: [0, 64) octahedron cases, [64, 192)
+// tetrahedron cases.  Entry i is two float4s: the six displacement offsets
+// (E0x, E0y, E0z, E1x), (E1y, E1z, case word as bits, 0).
+__shared__ float4 s_extra[2 * 192];
+
+// Fill s_extra (the caller synchronises the block before use).
+__device__ __forceinline__ void init_extra_table()
+{
+    for (int i = threadIdx.x; i < 192; i += blockDim.x) {
+        const uint32_t w = i < 64 ? octa_case(i) : tetra_case(i - 64);
+        float E[6];
+        extra_disp((float)word_offset(w, 0), (float)word_offset(w, 1), (float)word_offset(w, 2), E);
+        extra_disp((float)word_offset(w, 3), (float)word_offset(w, 4), (float)word_offset(w, 5), E + 3);
+        s_extra[2 * i] = make_float4(E[0], E[1], E[2], E[3]);
+        s_extra[2 * i + 1] = make_float4(E[4], E[5], __uint_as_float(w), 0.0f);
+    }
+}
+
+// (offset k of a case word + 1) * 128: the offset's step in a hash address.
+__device__ __forceinline__ int word_step(uint32_t w, int k)
+{
+    return (int)((k < 4 ? w << (7 - 2 * k) : w >> (2 * k - 7)) & 0x180u);
 }
 
 // The same decision for the binary32 path without data-dependent branches
@@ -362,10 +400,11 @@ __device__ __forceinline__ void decide_sel(float x, float y, float z, float in_s
                         (b_lt ? 32u : 0u);
     const uint32_t tt = 64u + ((xy ? 1u : 0u) | (zb ? 2u : 0u) | (za ? 4u : 0u) | (n1 ? 8u : 0u) | (n2 ? 16u : 0u) |
                                (cnb ? 32u : 0u) | (r1 ? 64u : 0u));
-    const uint32_t w = s_olut[tet ? tt : ot];
+    const float4 *t = s_extra + 2 * (tet ? tt : ot);
+    const float4 a = t[0], b = t[1];
     D.region = r0 ? 0 : (r1 ? 1 : 2);
-    D.e0x = lut_offset(w, 0); D.e0y = lut_offset(w, 1); D.e0z = lut_offset(w, 2);
-    D.e1x = lut_offset(w, 3); D.e1y = lut_offset(w, 4); D.e1z = lut_offset(w, 5);
+    D.w = __float_as_uint(b.z);
+    D.E[0] = a.x; D.E[1] = a.y; D.E[2] = a.z; D.E[3] = a.w; D.E[4] = b.x; D.E[5] = b.y;
 }
 
 // opensimplex.py:18-21 in binary64
@@ -385,8 +424,12 @@ struct Cell {
 
 // Binary64 decisions with the reference's operation order (opensimplex.py:
 // 270-300 and the region code).  No FMA contraction: explicit _rn ops.
-__device__ __noinline__ void decide_f64(double X, double Y, double Z, double s, Cell &c)
+// Returns the cell by value: a cell passed by reference would be
+// address-taken in the caller, which then keeps it in local memory on the
+// common binary32 path too.
+__device__ __noinline__ Cell decide_f64(double X, double Y, double Z, double s)
 {
+    Cell c;
     double x = __dmul_rn(X, s), y = __dmul_rn(Y, s), z = __dmul_rn(Z, s);
     double so = __dmul_rn(__dadd_rn(__dadd_rn(x, y), z), -1.0 / 6);
     double xs = __dadd_rn(x, so), ys = __dadd_rn(y, so), zs = __dadd_rn(z, so);
@@ -398,6 +441,7 @@ __device__ __noinline__ void decide_f64(double X, double Y, double Z, double s, 
     Cmp<double, false> C;
     C.m = 0.f;
     decide<double, false>(xins, yins, zins, in_sum, C, c.D);
+    pack_extra(c.D);
     c.dx0 = (float)__dsub_rn(x, xb);
     c.dy0 = (float)__dsub_rn(y, yb);
     c.dz0 = (float)__dsub_rn(z, zb);
@@ -405,6 +449,7 @@ __device__ __noinline__ void decide_f64(double X, double Y, double Z, double s, 
     c.xb7 = (int)((unsigned)xsb << 7);
     c.yb7 = (int)((unsigned)ysb << 7);
     c.zb7 = (int)((unsigned)zsb << 7);
+    return c;
 }
 
 // Binary32 path.  Returns false when binary64 must decide.
@@ -492,7 +537,7 @@ __device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float y
 {
     Cell c;
     if (!decide_f32(xh, xl, yh, yl, zh, zl, sh, sl, c)) {
-        decide_f64(X, Y, Z, s, c);
+        c = decide_f64(X, Y, Z, s);
         ++nfb;
     }
     const int r = c.D.region;
@@ -512,13 +557,10 @@ __device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float y
     uint32_t w110 = lk(lb, (int)h11 + z0), w101 = lk(lb, (int)h10 + z1), w011 = lk(lb, (int)h01 + z1);
     // extra points
     const Decision &D = c.D;
-    float s0 = ((D.e0x + D.e0y) + D.e0z) * THIRD, s1 = ((D.e1x + D.e1y) + D.e1z) * THIRD;
-    int ox0 = __float_as_int(D.e0x + MAGIC) << 7, oy0 = __float_as_int(D.e0y + MAGIC) << 7,
-        oz0 = __float_as_int(D.e0z + MAGIC) << 7;
-    int ox1 = __float_as_int(D.e1x + MAGIC) << 7, oy1 = __float_as_int(D.e1y + MAGIC) << 7,
-        oz1 = __float_as_int(D.e1z + MAGIC) << 7;
-    uint32_t we0 = lk(lb, (int)lk(lb, (int)lk(lb, c.xb7 + ox0) + c.yb7 + oy0) + c.zb7 + oz0);
-    uint32_t we1 = lk(lb, (int)lk(lb, (int)lk(lb, c.xb7 + ox1) + c.yb7 + oy1) + c.zb7 + oz1);
+    const uint32_t ew = D.w;
+    const int xm = c.xb7 - 128, ym = c.yb7 - 128, zm = c.zb7 - 128;
+    uint32_t we0 = lk(lb, (int)lk(lb, (int)lk(lb, xm + word_step(ew, 0)) + ym + word_step(ew, 1)) + zm + word_step(ew, 2));
+    uint32_t we1 = lk(lb, (int)lk(lb, (int)lk(lb, xm + word_step(ew, 3)) + ym + word_step(ew, 4)) + zm + word_step(ew, 5));
     const float2 X0 = f2(dx0, dx0), Y0 = f2(dy0, dy0), Z0 = f2(dz0, dz0);
     const float fon0 = on0 ? 1.0f : 0.0f, fA = onA ? 1.0f : 0.0f, fB = onB ? 1.0f : 0.0f;
     float2 acc = f2(0.0f, 0.0f);
@@ -528,16 +570,17 @@ __device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float y
                    __fadd2_rn(Z0, f2(-THIRD, -c1)), f2(fA, fA), acc);
     acc = contrib2(w110, w101, __fadd2_rn(X0, f2(-c3, -c3)), __fadd2_rn(Y0, f2(-c3, -c2)),
                    __fadd2_rn(Z0, f2(-c2, -c3)), f2(fB, fB), acc);
-    acc = contrib2(w011, we0, __fadd2_rn(X0, f2(-c2, -(D.e0x + s0))), __fadd2_rn(Y0, f2(-c3, -(D.e0y + s0))),
-                   __fadd2_rn(Z0, f2(-c3, -(D.e0z + s0))), f2(fB, 1.0f), acc);
-    float v = (acc.x + acc.y) + contrib(we1, dx0 - (D.e1x + s1), dy0 - (D.e1y + s1), dz0 - (D.e1z + s1), true);
+    acc = contrib2(w011, we0, __fadd2_rn(X0, f2(-c2, -D.E[0])), __fadd2_rn(Y0, f2(-c3, -D.E[1])),
+                   __fadd2_rn(Z0, f2(-c3, -D.E[2])), f2(fB, 1.0f), acc);
+    float v = (acc.x + acc.y) + contrib(we1, dx0 - D.E[3], dy0 - D.E[4], dz0 - D.E[5], true);
     if (TRACE) {
         tr[0] = c.xsb; tr[1] = c.ysb; tr[2] = c.zsb; tr[3] = r;
-        tr[4] = c.xsb + (int)D.e0x; tr[5] = c.ysb + (int)D.e0y; tr[6] = c.zsb + (int)D.e0z;
-        tr[7] = c.xsb + (int)D.e1x; tr[8] = c.ysb + (int)D.e1y; tr[9] = c.zsb + (int)D.e1z;
+        int e[6];
+        for (int k = 0; k < 6; ++k) e[k] = word_offset(ew, k);
+        tr[4] = c.xsb + e[0]; tr[5] = c.ysb + e[1]; tr[6] = c.zsb + e[2];
+        tr[7] = c.xsb + e[3]; tr[8] = c.ysb + e[4]; tr[9] = c.zsb + e[5];
         const int o[9][3] = {{r == 1, r == 1, r == 1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0},
-                             {1, 0, 1}, {0, 1, 1}, {(int)D.e0x, (int)D.e0y, (int)D.e0z},
-                             {(int)D.e1x, (int)D.e1y, (int)D.e1z}};
+                             {1, 0, 1}, {0, 1, 1}, {e[0], e[1], e[2]}, {e[3], e[4], e[5]}};
         const uint32_t w[9] = {w0, w100, w010, w001, w110, w101, w011, we0, we1};
         const bool on[9] = {on0, onA, onA, onA, onB, onB, onB, true, true};
         for (int k = 0; k < 9; ++k) {
@@ -563,7 +606,7 @@ __global__ void __launch_bounds__(256) fbm_kernel(const double *__restrict__ xyz
 {
     extern __shared__ __align__(16) uint32_t smem[];
     build_table(smem, perm, pgi);
-    init_octa_lut();
+    init_extra_table();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
     unsigned nfb = 0;
@@ -599,7 +642,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const double *__restrict__ x
 {
     extern __shared__ __align__(16) uint32_t smem[];
     build_table(smem, perm, pgi);
-    init_octa_lut();
+    init_extra_table();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
     float sh, sl;
@@ -655,7 +698,7 @@ __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__r
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint32_t s_mm[2][8];
-    init_octa_lut();
+    init_extra_table();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
     int cur = -1;
