@@ -186,6 +186,13 @@ __global__ void adj_records_kernel(const int32_t *__restrict__ tris, int64_t nt,
     }
 }
 
+__device__ __forceinline__ void cswap(unsigned long long &a, unsigned long long &b)
+{
+    const unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
+    a = lo;
+    b = hi;
+}
+
 __global__ void adj_rows_kernel(int64_t nv, const unsigned *__restrict__ cnt,
                                 const unsigned long long *__restrict__ rec, int32_t *__restrict__ adj)
 {
@@ -193,13 +200,16 @@ __global__ void adj_rows_kernel(int64_t nv, const unsigned *__restrict__ cnt,
         unsigned c = cnt[v];
         if (c > 6) c = 6;
         unsigned long long r[6];
+#pragma unroll
         for (int s = 0; s < 6; ++s) r[s] = s < (int)c ? rec[6 * v + s] : ~0ull;
-        for (int a = 1; a < 6; ++a) {       // insertion sort by triangle index
-            unsigned long long x = r[a];
-            int b = a - 1;
-            while (b >= 0 && r[b] > x) { r[b + 1] = r[b]; --b; }
-            r[b + 1] = x;
-        }
+        // by triangle index: a 12-comparator sorting network for 6 keys
+        // (fixed indices, so the keys stay in registers)
+        cswap(r[0], r[5]); cswap(r[1], r[3]); cswap(r[2], r[4]);
+        cswap(r[1], r[2]); cswap(r[3], r[4]);
+        cswap(r[0], r[3]); cswap(r[2], r[5]);
+        cswap(r[0], r[1]); cswap(r[2], r[3]); cswap(r[4], r[5]);
+        cswap(r[1], r[2]); cswap(r[3], r[4]);
+#pragma unroll
         for (int s = 0; s < 6; ++s) adj[6 * v + s] = s < (int)c ? (int32_t)(uint32_t)r[s] : -1;
     }
 }
@@ -654,22 +664,15 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
         for (int r = 1; r <= R; ++r) {
             const int re = rb + s_ring[r];
             const int ln = re - rb;
-            int p2 = 1;
-            while (p2 < ln) p2 <<= 1;
-            for (int q = threadIdx.x; q < p2; q += blockDim.x) scr[q] = q < ln ? list[rb + q] : 0x7FFFFFFF;
+            // rank sort (the ids of a ring are distinct): each entry's
+            // position is the number of smaller ids, read as broadcasts
+            for (int q = threadIdx.x; q < ln; q += blockDim.x) {
+                const int32_t v = list[rb + q];
+                int rank = 0;
+                for (int x = 0; x < ln; ++x) rank += list[rb + x] < v ? 1 : 0;
+                scr[rank] = v;
+            }
             __syncthreads();
-            for (int size = 2; size <= p2; size <<= 1)
-                for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                    for (int q = threadIdx.x; q < p2; q += blockDim.x) {
-                        const int o = q ^ stride;
-                        if (o > q) {
-                            const bool upw = (q & size) == 0;
-                            const int32_t x = scr[q], y = scr[o];
-                            if ((x > y) == upw) { scr[q] = y; scr[o] = x; }
-                        }
-                    }
-                    __syncthreads();
-                }
             for (int q = threadIdx.x; q < ln; q += blockDim.x) {
                 const int32_t v = scr[q];
                 list[rb + q] = v;
