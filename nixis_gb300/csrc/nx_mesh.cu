@@ -641,12 +641,22 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
     int beg = 0, end = T;
     for (int r = 1; r <= R; ++r) {
         const int nwork = (end - beg) * 6;
-        for (int w = threadIdx.x; w < nwork; w += blockDim.x) {
-            const int32_t v = list[beg + w / 6];
-            const int32_t j = nbr[6 * (int64_t)v + (w % 6)];
-            if (j < 0) continue;
-            if ((int64_t)j >= nv) { s_bad = 1; continue; }
-            if (hinsert(H, key, val, list, &s_cnt, nmax, j) < 0) s_bad = 1;
+        // two slots per thread per round, both reads issued first (the
+        // ring's order is fixed by the sort below, not by insertion order)
+        for (int w0 = threadIdx.x; w0 < nwork; w0 += 2 * blockDim.x) {
+            int32_t jv[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int w = w0 + u * blockDim.x;
+                jv[u] = w < nwork ? nbr[6 * (int64_t)list[beg + w / 6] + (w % 6)] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int32_t j = jv[u];
+                if (j < 0) continue;
+                if ((int64_t)j >= nv) { s_bad = 1; continue; }
+                if (hinsert(H, key, val, list, &s_cnt, nmax, j) < 0) s_bad = 1;
+            }
         }
         __syncthreads();
         beg = end;
@@ -691,20 +701,39 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
     if (C0 > cmax) { if (threadIdx.x == 0) s_bad = 1; C0 = cmax; }
     __syncthreads();
     for (int q = threadIdx.x; q < NL; q += blockDim.x) tid[q] = list[q];
-    for (int w = threadIdx.x; w < C0 * 6; w += blockDim.x) {
-        const int q = w / 6, sl = w % 6;
-        const int32_t v = list[q];
-        const int32_t j = nbr[6 * (int64_t)v + sl];
-        // a missing neighbour (-1, pentagon slot) points at the vertex itself:
-        // the erosion update then sees equal heights and adds nothing
-        int loc = q;
-        if (j >= 0) {
-            loc = hfind(H, key, val, j);
-            if (loc < 0) { s_bad = 1; loc = q; }
+    // four slots per thread per round, their global reads issued before any
+    // hash probe (independent loads in flight instead of a dependent chain)
+    constexpr int U = 4;
+    const int nslot = C0 * 6;
+    for (int w0 = threadIdx.x; w0 < nslot; w0 += U * blockDim.x) {
+        int32_t jv[U];
+        float2 ev[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int w = w0 + u * blockDim.x;
+            if (w < nslot) {
+                const int64_t g = 6 * (int64_t)list[w / 6] + w % 6;
+                jv[u] = nbr[g];
+                ev[u] = reinterpret_cast<const float2 *>(edge)[g];
+            }
         }
-        lnbr[((int64_t)tile * cmax + q) * 6 + sl] = (uint16_t)loc;
-        reinterpret_cast<float2 *>(ledge)[((int64_t)tile * cmax + q) * 6 + sl] =
-            reinterpret_cast<const float2 *>(edge)[6 * (int64_t)v + sl];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int w = w0 + u * blockDim.x;
+            if (w < nslot) {
+                const int q = w / 6, sl = w % 6;
+                // a missing neighbour (-1, pentagon slot) points at the vertex
+                // itself: the erosion update then sees equal heights and adds
+                // nothing
+                int loc = q;
+                if (jv[u] >= 0) {
+                    loc = hfind(H, key, val, jv[u]);
+                    if (loc < 0) { s_bad = 1; loc = q; }
+                }
+                lnbr[((int64_t)tile * cmax + q) * 6 + sl] = (uint16_t)loc;
+                reinterpret_cast<float2 *>(ledge)[((int64_t)tile * cmax + q) * 6 + sl] = ev[u];
+            }
+        }
     }
     if (threadIdx.x == 0) {
         tc[0] = T;
