@@ -705,6 +705,40 @@ def bench_single(name):
     print(json.dumps(line))
 
 
+def bench_mesh_prep(args):
+    """Mesh preparation of the workload (supplementary line): the distinct
+    divisions' meshes (icosphere, adjacency, edge lengths) and then their
+    blocked-erosion tilings, each phase timed with CUDA events, twice after
+    a warm-up build (the batch keeps them resident, so this is not part of
+    its step)."""
+    import torch
+    from nixis_gb300 import autotune, mesh
+    cfg = autotune.DEFAULT
+    divs = sorted({r.divisions for r in workload(args.workload)})
+    m = mesh.PlanetMesh(20)
+    m.tiling(cfg.tile_side, cfg.rings)
+    torch.cuda.synchronize()
+    del m
+    reps = []
+    for _ in range(2):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        e0.record()
+        meshes = [mesh.PlanetMesh(k, defer_checks=True) for k in divs]
+        e1.record()
+        tilings = [x.tiling(cfg.tile_side, cfg.rings) for x in meshes]
+        e2.record()
+        torch.cuda.synchronize()
+        for x in meshes:
+            x.check()
+        reps.append((e0.elapsed_time(e1), e1.elapsed_time(e2)))
+        nv = sum(x.n for x in meshes)
+        del meshes, tilings
+    print(json.dumps({"mesh_prep": args.workload, "meshes": len(divs), "vertices": nv,
+                      "tiling": f"{cfg.tile_side}/{cfg.rings}",
+                      "mesh_ms": [round(a, 2) for a, _ in reps], "tiling_ms": [round(b, 2) for _, b in reps]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -728,7 +762,12 @@ def main():
                     help="with --profile: one launch per erosion iteration instead of blocked passes")
     ap.add_argument("--serve", type=int, default=0, help="serving comparison on the first N stream requests, exit")
     ap.add_argument("--serve-requests", type=int, default=200, help="stream requests in the default line's serving leg")
+    ap.add_argument("--mesh-prep", action="store_true",
+                    help="time the workload's mesh and tiling builds (CUDA events), print one line, exit")
     args = ap.parse_args()
+    if args.mesh_prep:
+        bench_mesh_prep(args)
+        return
     if args.single:
         bench_single(args.single)
         return
