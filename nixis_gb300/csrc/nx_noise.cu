@@ -16,12 +16,14 @@
 //    split into an integer A and a fraction a in [-1/2, 1/2], and with
 //    T = Ax+Ay+Az = 6q + r the skewed coordinate becomes
 //    xs = (Ax - q) + (a_x - (r + a_x + a_y + a_z)/6), whose second term is
-//    O(1) and carries an absolute error below 3e-7 (derivation in the design
-//    notes).  Every comparison that decides the cell or region records its
-//    margin; when the smallest margin is below TAU (>= 4x the error bound),
-//    or |x*scale| >= 2^16, that lane recomputes the decisions in binary64
-//    with the reference's operation order (decide_f64), so the decisions
-//    always equal the reference's.
+//    O(1) and carries an absolute error of at most 2.2e-7 for
+//    |x*scale| < 2^16 (the bound is worked through at decide_f32).  Every
+//    comparison that decides the cell or region records its margin; the
+//    compared quantities combine up to three such terms with a few more
+//    roundings (errors below 1.3e-6), and when the smallest margin is below
+//    TAU = 4e-6 (> 3x that), or |x*scale| >= 2^16, that lane recomputes the
+//    decisions in binary64 with the reference's operation order
+//    (decide_f64), so the decisions always equal the reference's.
 //  * The 6 or 8 contributions are evaluated branch-free as 9 slots: the
 //    corner (0,0,0)|(1,1,1), the six mixed corners, and the two extra points,
 //    with masks per region; hash prefixes of the fixed slots are shared.
@@ -453,6 +455,24 @@ __device__ __noinline__ Cell decide_f64(double X, double Y, double Z, double s)
 }
 
 // Binary32 path.  Returns false when binary64 must decide.
+//
+// Error of b = a - u/6 (the skewed coordinate less its integer part Ax - q)
+// for |x*scale| < 2^16, each step's rounding in absolute terms:
+//  * p + e = x*scale within 2^-45 |x*scale| < 2e-9: the coordinate and the
+//    scale are binary32 pairs (2^-47 and 2^-48 relative), the lo*lo term is
+//    dropped and the three cross terms are fused;
+//  * A = round(p) and p - A are exact; a = (p - A) + e rounds once,
+//    |a| < 1: <= 2^-25 (3.0e-8);
+//  * T = Ax + Ay + Az is an exact integer and q = floor(T/6 + 1/12) is exact
+//    (T/6 + 1/12 lies at least 1/12 from an integer; the fused product's
+//    error is below |T| 2^-24 < 0.02), so r = T - 6q in 0..5 is exact;
+//  * the sum of the three a (two roundings, values < 1.5): <= 1.2e-7,
+//    entering b divided by 6: 2.0e-8; u = r + that, |u| < 8: 2.4e-7 / 6 =
+//    4.0e-8; the errors of the a themselves: 3.0e-8 * (5/6 + 2/6) = 3.5e-8;
+//  * SIXTH = 1/6 rounded, off by 5.0e-9, times |u| <= 6.5: 3.2e-8; the
+//    fused b = a - u*SIXTH, |b| < 2: <= 2^-24 (6.0e-8).
+// Total <= 1.9e-7 (checked by simulating these operations on random
+// coordinates and scales: largest 1.3e-7).  xins = b - floor(b) is exact.
 __device__ __forceinline__ bool decide_f32(float xh, float xl, float yh, float yl, float zh, float zl,
                                            float sh, float sl, Cell &c)
 {
