@@ -454,10 +454,13 @@ int nx_shape_heights(const double *h_dev, int64_t n, double min_alt, double max_
  * the state is updated in place, mass_dev (optional) as in
  * nx_erosion_steps, status_dev (optional, device int32[2]) gets the final
  * scale exponent K and the neighbour-range error flag.  The first call on
- * each device looks up the array's device address (make that first call
- * before any stream capture).  All calls share the one array and each call
- * resets what must start at zero; calls whose work overlaps on the GPU
- * (other streams, other threads) race on it and must be serialised. */
+ * each device looks up the array's device address in that device's
+ * primary context and keeps it for the life of the process (make that
+ * first call before any stream capture; after cudaDeviceReset the cached
+ * address is stale, so do not call it on that device again).  All calls
+ * share the one array and each call resets what must start at zero; calls
+ * whose work overlaps on the GPU (other streams, other threads) race on it
+ * and must be serialised by the caller. */
 #define NX_NOALLOC_MAX_VERTICES 262144
 int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge_dev, int64_t n, float *st_dev, int iters,
                              float rain, double *mass_dev, int32_t *status_dev, void *stream);

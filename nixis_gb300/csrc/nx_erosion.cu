@@ -953,10 +953,13 @@ static int tb_prepare()
 }
 
 // Batch: planets packed by non-increasing iteration count, so the planets
-// still running at iteration t are a prefix of the block map.
+// still running at iteration t are a prefix of the block map.  allow_tb:
+// whether the descriptors' tiling fields may be read at all (the
+// single-planet entry points build descriptors without a tiling and pass 0,
+// so their runs never depend on those fields).
 static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
                      float *st_dev, float *st_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace,
-                     size_t ws_bytes, cudaStream_t s)
+                     size_t ws_bytes, cudaStream_t s, bool allow_tb)
 {
     if (np <= 0) return NX_OK;
     if (!planets_dev || !planets_host || !st_dev || !st_tmp || !workspace)
@@ -976,7 +979,7 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
     }
     // temporally blocked when every planet has a tiling and nothing per
     // iteration (mass sums, flow bits) is requested
-    bool tb = !mass_dev && !flow_dev && g_tb_enabled;
+    bool tb = allow_tb && !mass_dev && !flow_dev && g_tb_enabled;
     int R = 0, maxnl = 0, maxc = 0;
     int64_t ntiles_all = 0;
     for (int p = 0; p < np && tb; ++p) {
@@ -1231,7 +1234,7 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
 {
     if (n <= 0 || iters < 0) return nx::fail(NX_EINVAL, "nx_erosion_steps: bad n or iters");
     if (!planet_dev) return nx::fail(NX_EINVAL, "nx_erosion_steps: planet descriptor (device) required");
-    nx_erosion_planet P;
+    nx_erosion_planet P = {};   // no tiling: every field not set below is zero
     P.vbeg = 0;
     P.n = n;
     P.nbr = nbr_dev;
@@ -1245,7 +1248,7 @@ NX_EXPORT int nx_erosion_steps(const int32_t *nbr_dev, const float *edge_dev, in
     // state enters in buffer 0; with an odd count the first iteration reads buffer 1
     if (iters & 1)
         NX_CHECK_CUDA(cudaMemcpyAsync(st_tmp_dev, st_dev, 2 * sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    return run_batch(planet_dev, &P, 1, st_dev, st_tmp_dev, mass_dev, flow_dev, workspace, ws_bytes, s);
+    return run_batch(planet_dev, &P, 1, st_dev, st_tmp_dev, mass_dev, flow_dev, workspace, ws_bytes, s, false);
 }
 
 NX_EXPORT int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
@@ -1253,7 +1256,7 @@ NX_EXPORT int nx_erosion_batch(const nx_erosion_planet *planets_dev, const nx_er
                                void *stream)
 {
     return run_batch(planets_dev, planets_host, nplanets, st_dev, st_tmp_dev, mass_dev, nullptr, workspace, ws_bytes,
-                     (cudaStream_t)stream);
+                     (cudaStream_t)stream, true);
 }
 
 NX_EXPORT int nx_erosion_ctl_init(void *workspace, size_t ws_bytes, int nplanets, void *stream)
@@ -1364,7 +1367,10 @@ std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[64] = {nullptr};
 
 // Device address of g_noalloc_scratch on the current device (looked up once
-// per device; the host-side symbol is only a stand-in for it).
+// per device; the host-side symbol is only a stand-in for it).  The cached
+// address belongs to the device's primary context: it stays valid for the
+// life of the process unless that context is destroyed (cudaDeviceReset),
+// after which the library must not be called on that device again.
 int noalloc_scratch(unsigned char **out)
 {
     int dev = 0;
@@ -1422,7 +1428,7 @@ NX_EXPORT int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge
     nx_erosion_planet *desc = (nx_erosion_planet *)base;
     nx_erosion_ctl *ctl = (nx_erosion_ctl *)(base + 256);
     float *st_tmp = (float *)(base + NOALLOC_HEAD + NOALLOC_PARTIALS);
-    nx_erosion_planet P;
+    nx_erosion_planet P = {};   // no tiling: every field not set below is zero
     P.vbeg = 0;
     P.n = n;
     P.nbr = nbr_dev;
@@ -1441,7 +1447,7 @@ NX_EXPORT int nx_erosion_steps_noalloc(const int32_t *nbr_dev, const float *edge
     static_assert(256 + sizeof(nx_erosion_ctl) + 16 + NOALLOC_PARTIALS <= NOALLOC_HEAD + NOALLOC_PARTIALS,
                   "partials fit before the second state buffer");
     static_assert((NOALLOC_HEAD + NOALLOC_PARTIALS) % 256 == 0, "state buffer alignment");
-    rc = run_batch(desc, &P, 1, st_dev, st_tmp, mass_dev, nullptr, (void *)ctl, ws_bytes, s);
+    rc = run_batch(desc, &P, 1, st_dev, st_tmp, mass_dev, nullptr, (void *)ctl, ws_bytes, s, false);
     if (rc) return rc;
     if (status_dev) {
         noalloc_status_kernel<<<1, 1, 0, s>>>(ctl, status_dev);

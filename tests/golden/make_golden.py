@@ -1,9 +1,8 @@
 """Generate the golden vectors in tests/golden/ by executing the reference.
 
-Run in a container that has the reference sources (default location set in
-ref_shim.py, override with NIXIS_REFERENCE_DIR):
+Run where the reference sources are, naming their directory:
 
-    python tests/golden/make_golden.py
+    NIXIS_REFERENCE_DIR=<nixis checkout> python tests/golden/make_golden.py
 
 Every expected value in the output comes from the reference's own Python
 functions (opensimplex.init / noise3d, terrain.sample_noise / sample_octaves,

@@ -30,7 +30,8 @@ import os
 import sys
 import types
 
-REFERENCE_DIR = os.environ.get("NIXIS_REFERENCE_DIR", "/root/reference")
+# The reference's source directory (the nixis checkout); required, no default.
+REFERENCE_DIR = os.environ.get("NIXIS_REFERENCE_DIR", "")
 
 
 def _int32_wrap(x):
@@ -75,6 +76,8 @@ def load():
     global _loaded
     if _loaded is not None:
         return _loaded
+    if not REFERENCE_DIR:
+        raise RuntimeError("set NIXIS_REFERENCE_DIR to the nixis source directory")
     if not os.path.isdir(REFERENCE_DIR):
         raise RuntimeError(f"reference sources not found at {REFERENCE_DIR}")
     _install_stubs()

@@ -335,3 +335,33 @@ def test_tiling_with_fewer_rings_than_a_pass_is_reported_not_run():
     ok.run()
     torch.cuda.synchronize()
     assert torch.equal(ok.results()[0].heights, planets.generate_plain(req, cache).heights)
+
+
+def test_steps_without_mass_sums_equal_steps_with_them():
+    """nx_erosion_steps with mass_dev = flow_dev = NULL (the plain path's
+    call) runs the same arithmetic as with mass sums: same bits, odd and
+    even iteration counts."""
+    import ctypes
+    from nixis_gb300 import _dev, _lib, mesh
+    m = mesh.PlanetMesh(60)
+    pts = m.xyz.cpu().numpy()
+    perm, pgi = O.init(4)
+    h = O.rescale(O.sample_octaves(pts, None, perm, pgi, 8, 1.0, 1.0, 2.0, 0.5, 1.0), -8000.0, 8000.0)
+    st0 = torch.from_numpy(O.pair_rows(h, np.full(len(pts), 1e-3), np.zeros(len(pts)))).cuda()
+    n = m.n
+    for iters in (11, 6):
+        outs = []
+        for with_mass in (True, False):
+            st = st0.clone()
+            tmp = torch.empty_like(st)
+            ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
+            pd = torch.full((ctypes.sizeof(_lib.ErosionPlanet),), 0xA5, dtype=torch.uint8, device="cuda")
+            mass = torch.empty((iters, 3), dtype=torch.float64, device="cuda") if with_mass else None
+            _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), 1, _dev.stream_handle())
+            _lib.call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(st), _dev.ptr(tmp), iters,
+                      ctypes.c_float(0.0), _dev.ptr(pd), _dev.ptr(mass) if with_mass else None, None, _dev.ptr(ws),
+                      ws.numel(), _dev.stream_handle())
+            torch.cuda.synchronize()
+            assert int(ws[:32].view(torch.int32)[6].item()) == 0       # no error flag
+            outs.append(st)
+        assert torch.equal(outs[0], outs[1])

@@ -26,29 +26,31 @@ def _state(pts, seed, octaves):
     return torch.from_numpy(st).cuda()
 
 
-def _allocating(m, st, iters, rain):
+def _allocating(m, st, iters, rain, with_mass=True):
     from nixis_gb300 import _dev, _lib
     n = m.n
     st = st.clone()
     tmp = torch.empty_like(st)
     ws = torch.zeros(int(_lib.lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
     pd = torch.zeros(ctypes.sizeof(_lib.ErosionPlanet), dtype=torch.uint8, device="cuda")
-    mass = torch.empty((max(iters, 1), 3), dtype=torch.float64, device="cuda")
+    mass = torch.empty((max(iters, 1), 3), dtype=torch.float64, device="cuda") if with_mass else None
     _lib.call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), 1, _dev.stream_handle())
     _lib.call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(st), _dev.ptr(tmp), iters,
-              ctypes.c_float(rain), _dev.ptr(pd), _dev.ptr(mass), None, _dev.ptr(ws), ws.numel(), _dev.stream_handle())
+              ctypes.c_float(rain), _dev.ptr(pd), _dev.ptr(mass) if with_mass else None, None, _dev.ptr(ws),
+              ws.numel(), _dev.stream_handle())
     K = int(ws[:32].view(torch.int32)[3].item())
-    return st, mass[:iters], K
+    return st, (mass[:iters] if with_mass else None), K
 
 
-def _noalloc(m, st, iters, rain):
+def _noalloc(m, st, iters, rain, with_mass=True, with_status=True):
     from nixis_gb300 import _dev, _lib
     st = st.clone()
-    mass = torch.empty((max(iters, 1), 3), dtype=torch.float64, device="cuda")
-    status = torch.full((2,), -7, dtype=torch.int32, device="cuda")
+    mass = torch.empty((max(iters, 1), 3), dtype=torch.float64, device="cuda") if with_mass else None
+    status = torch.full((2,), -7, dtype=torch.int32, device="cuda") if with_status else None
     _lib.call("nx_erosion_steps_noalloc", _dev.ptr(m.nbr), _dev.ptr(m.edge), m.n, _dev.ptr(st), iters,
-              ctypes.c_float(rain), _dev.ptr(mass), _dev.ptr(status), _dev.stream_handle())
-    return st, mass[:iters], status.cpu().numpy()
+              ctypes.c_float(rain), _dev.ptr(mass) if with_mass else None,
+              _dev.ptr(status) if with_status else None, _dev.stream_handle())
+    return st, (mass[:iters] if with_mass else None), (status.cpu().numpy() if with_status else None)
 
 
 def test_noalloc_matches_allocating_entry_point_twice():
@@ -64,6 +66,22 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert torch.equal(a, b)
         assert torch.equal(ma, mb)
         assert status[0] == Ka and status[1] == 0
+
+
+def test_noalloc_without_mass_sums_or_status_matches_allocating_entry_point():
+    """mass_dev and status_dev are optional: without them the run takes the
+    same per-iteration kernel and gives the same bits as the allocating
+    entry point called without mass sums, and as a call with them."""
+    from nixis_gb300 import mesh
+    m = mesh.PlanetMesh(100)
+    st = _state(m.xyz.cpu().numpy(), 5, 9)
+    for iters in (13, 8):                   # two calls in a row, odd and even counts
+        a, _, _ = _allocating(m, st, iters, 0.0, with_mass=False)
+        b, _, _ = _noalloc(m, st, iters, 0.0, with_mass=False, with_status=False)
+        c, _, _ = _noalloc(m, st, iters, 0.0)
+        torch.cuda.synchronize()
+        assert torch.equal(a, b)
+        assert torch.equal(b, c)
 
 
 def test_noalloc_rejects_meshes_above_its_fixed_scratch():
