@@ -360,7 +360,7 @@ def bench_ours(args):
     call("nx_fbm_batch", _dev.ptr(batch.fb_dev), ctypes.cast(batch.fb_host, ctypes.c_void_p), np_, None, s)
     ev[1].record(stream)
     call("nx_erosion_init_batch", _dev.ptr(batch.er_dev), ctypes.cast(batch.er_host, ctypes.c_void_p), np_,
-         _dev.ptr(batch.raw), _dev.ptr(batch.minmax), ctypes.c_float(-8000.0), ctypes.c_float(8000.0),
+         _dev.ptr(batch.raw), _dev.ptr(batch.minmax), -8000.0, 8000.0,
          ctypes.c_double(1e-3), _dev.ptr(batch.st), _dev.ptr(batch.st_tmp), s)
     call("nx_erosion_ctl_init", _dev.ptr(batch.ws), batch.ws.numel(), np_, s)
     ev[2].record(stream)
@@ -411,7 +411,7 @@ def bench_ours(args):
     # end to end: per step, request tables host->device, batch, heights device->host (pinned)
     host_tab = torch.empty_like(batch.tables, device="cpu").pin_memory()
     host_tab.copy_(batch.tables)
-    host_out = torch.empty(batch.heights.numel(), dtype=torch.float32).pin_memory()
+    host_out = torch.empty(batch.heights.numel(), dtype=torch.float64).pin_memory()
     for _ in range(2):
         batch.tables.copy_(host_tab, non_blocking=True)
         batch.run()
@@ -441,7 +441,7 @@ def bench_ours(args):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = {"value": world * npl * args.steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(batch.tables.numel() * 4), "d2h_bytes_per_step": int(batch.heights.numel() * 4),
+           "h2d_bytes_per_step": int(batch.tables.numel() * 4), "d2h_bytes_per_step": int(batch.heights.numel() * 8),
            "note": "request tables in, all heights out to pinned host memory, every step; each step's heights are "
                    "copied on a side stream while the next step runs (PlanetBatch.run_to_host), all copies complete "
                    "inside the timed region",

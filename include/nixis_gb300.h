@@ -99,20 +99,49 @@ int nx_noise3d_trace(const double *xyz_dev, int64_t n, const int32_t *perm_dev,
                      int32_t *slots_dev, unsigned long long *n_fallback_dev, void *stream);
 
 
-/* One planet of a batched fBm launch (device-resident array of these). */
+/* fBm in pair precision: the kernel behind the planet paths (batched,
+ * plain, served) and terrain.sample_octaves' binary64 output.  Same sum as
+ * nx_fbm, with the same exactly-decided lattice cells, regions and extra
+ * points, but every continuous quantity carried as an unevaluated pair
+ * hi + lo of binary32s: results lie within ~1e-13 of the binary64
+ * reference's sums (eroded planets need this: the erosion update branches
+ * on the sign of neighbour height differences, which binary32 noise flips).
+ * pair_dev (optional, 8-byte aligned): float[2n], vertex v's running sum as
+ * (hi, lo) -- written (accumulate = 0) or added to (accumulate = 1);
+ * elev_f64_dev (optional): the sum as binary64 (= hi + lo exactly), or
+ * added to it when accumulate = 1 and pair_dev is NULL.  minmax_dev
+ * (optional, device uint64[2], caller sets {~0, 0}): atomically folded
+ * min and max ordered keys of the resulting pair sums, key(h, l) =
+ * (fkey(h) << 32) | fkey(l) with fkey(f) = f >= 0 ? bits ^ 0x80000000 :
+ * ~bits.  A running sum is renormalised after every octave, so one launch
+ * over all octaves and one launch per octave give the same bits, given the
+ * same amp_ref: octaves whose amplitude 0.5*strength*radius is below
+ * amp_ref/8 take a cheaper displacement form (amp_ref <= 0: the largest
+ * amplitude among this call's octaves; a planet evaluated one octave per
+ * call passes its first octave's amplitude). */
+int nx_fbm_pair(const double *xyz_dev, int64_t n, const int32_t *perm_dev, const int32_t *pgi_dev, int n_octaves,
+                const double *scale, const double *strength, double radius, double amp_ref, float *pair_dev,
+                double *elev_f64_dev, int accumulate, unsigned long long *minmax_dev,
+                unsigned long long *n_fallback_dev, void *stream);
+
+/* One planet of a batched fBm launch (device-resident array of these);
+ * the batch runs the pair path of nx_fbm_pair. */
 typedef struct nx_fbm_planet {
     const double *xyz;      /* (n,3) float64 vertices (its mesh) */
     int64_t n;
     const int32_t *perm;    /* device int32[256] tables of its seed */
     const int32_t *pgi;
-    float *out;             /* n binary32 sums over octaves */
-    uint32_t *minmax;       /* optional: 2 ordered keys, caller sets {0xFFFFFFFF, 0}; */
-                            /* key(f) = f >= 0 ? bits ^ 0x80000000 : ~bits        */
+    float *out;             /* float[2n], 8-byte aligned: (hi, lo) pair sums over octaves */
+    unsigned long long *minmax; /* optional: min, max ordered keys as in nx_fbm_pair; caller sets {~0, 0} */
     int32_t n_octaves;
     int32_t chunk0;         /* index of its first chunk: sum of ceil(n/chunk) of earlier planets */
-    float s_hi[NX_MAX_OCTAVES];   /* filled by nx_fbm_planet_fill */
-    float s_lo[NX_MAX_OCTAVES];
-    float amp[NX_MAX_OCTAVES];
+    int32_t pow2;           /* filled: 1 when every scale is a power of two */
+    uint32_t norm_mask;     /* filled: bit o set when octave o renormalises (amplitude >= 1/8 of the largest) */
+    float s1[NX_MAX_OCTAVES];     /* filled by nx_fbm_planet_fill: scale[o] = s1 + s2 + s3 exactly */
+    float s2[NX_MAX_OCTAVES];
+    float s3[NX_MAX_OCTAVES];
+    float amp_hi[NX_MAX_OCTAVES]; /* 0.5 * strength[o] * radius as a pair */
+    float amp_lo[NX_MAX_OCTAVES];
     double s[NX_MAX_OCTAVES];
 } nx_fbm_planet;
 
@@ -346,18 +375,22 @@ typedef struct nx_erosion_ctl {
     int32_t pad;
 } nx_erosion_ctl;
 
-/* Initial state of a batch from raw fBm sums (nx_fbm_batch output rows
- * and min/max keys, 2 per planet): h = util.rescale(raw, elev_lo, elev_hi)
- * (util.py:110-140), w = water0 (as a pair), s = 0, written to buffer
+/* Initial state of a batch from raw fBm pair sums (nx_fbm_batch /
+ * nx_fbm_pair output rows, float[2 * rows], and their min/max keys, 2 per
+ * planet): h = util.rescale(raw, elev_lo, elev_hi) (util.py:110-140) as a
+ * pair, (raw - min) * ((hi - lo) / (max - min)) + lo with the factor
+ * formed in binary64, w = water0 (as a pair), s = 0, written to buffer
  * (iters & 1). */
 int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
-                          int nplanets, const float *raw_dev, const uint32_t *minmax_dev, float elev_lo,
-                          float elev_hi, double water0, float *st_dev, float *st_tmp_dev, void *stream);
+                          int nplanets, const float *raw_dev, const unsigned long long *minmax_dev, double elev_lo,
+                          double elev_hi, double water0, float *st_dev, float *st_tmp_dev, void *stream);
 
 /* Heights of every planet of a finished batch into out_dev (packed rows):
- * (h_hi + h_lo) * 2^K, binary32. */
+ * (h_hi + h_lo) * 2^K in binary64, finite for every iteration count (the
+ * reference's heights grow without bound: binary32 metres overflow past
+ * ~130 iterations). */
 int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
-                             int nplanets, const float *st_dev, const void *workspace, float *out_dev,
+                             int nplanets, const float *st_dev, const void *workspace, double *out_dev,
                              void *stream);
 
 /* Latitude-table insolation (climate.py:503-597).  Tables for n_tilts

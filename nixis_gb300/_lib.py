@@ -43,8 +43,8 @@ SIGNATURES = {
     "nx_fbm_planet_fill": (_i32, [_p, _i32, _p, _p, _d]),
     "nx_fbm_chunk_size": (_i32, []),
     "nx_fbm_batch": (_i32, [_p, _p, _i32, _p, _p]),
-    "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_double, _p, _p,
-                                     _p]),
+    "nx_fbm_pair": (_i32, [_p, _i64, _p, _p, _i32, _p, _p, _d, _d, _p, _p, _i32, _p, _p, _p]),
+    "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, _d, _d, _d, _p, _p, _p]),
     "nx_erosion_heights_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p]),
     "nx_erosion_steps_noalloc": (_i32, [_p, _p, _i64, _p, _i32, ctypes.c_float, _p, _p, _p]),
     "nx_erosion_tick": (_i32, [_p, _p, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
@@ -76,9 +76,11 @@ class FbmPlanet(ctypes.Structure):
     """nx_fbm_planet (include/nixis_gb300.h)."""
     _fields_ = [("xyz", ctypes.c_void_p), ("n", ctypes.c_int64), ("perm", ctypes.c_void_p),
                 ("pgi", ctypes.c_void_p), ("out", ctypes.c_void_p), ("minmax", ctypes.c_void_p),
-                ("n_octaves", ctypes.c_int32), ("chunk0", ctypes.c_int32),
-                ("s_hi", ctypes.c_float * NX_MAX_OCTAVES), ("s_lo", ctypes.c_float * NX_MAX_OCTAVES),
-                ("amp", ctypes.c_float * NX_MAX_OCTAVES), ("s", ctypes.c_double * NX_MAX_OCTAVES)]
+                ("n_octaves", ctypes.c_int32), ("chunk0", ctypes.c_int32), ("pow2", ctypes.c_int32),
+                ("norm_mask", ctypes.c_uint32),
+                ("s1", ctypes.c_float * NX_MAX_OCTAVES), ("s2", ctypes.c_float * NX_MAX_OCTAVES),
+                ("s3", ctypes.c_float * NX_MAX_OCTAVES), ("amp_hi", ctypes.c_float * NX_MAX_OCTAVES),
+                ("amp_lo", ctypes.c_float * NX_MAX_OCTAVES), ("s", ctypes.c_double * NX_MAX_OCTAVES)]
 
 
 class InsoPlanet(ctypes.Structure):

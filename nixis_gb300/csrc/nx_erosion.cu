@@ -714,40 +714,79 @@ __device__ __forceinline__ int block_planet(const nx_erosion_planet *P, int np, 
     return find_planet(P, np, row);
 }
 
-// util.rescale (util.py:110-140) of the raw fBm sums to [lo, hi], and the
-// initial state (h, 0, water0 as a pair | 0, 0, 0, 0) in the buffer the
-// planet's first iteration reads: B[iters & 1].
+// util.rescale (util.py:110-140) of the raw fBm pair sums to [lo, hi], and
+// the initial state (h as a pair, water0 as a pair | 0, 0, 0, 0) in the
+// buffer the planet's first iteration reads: B[iters & 1].  The reference
+// computes ((x - min) / (max - min)) * (hi - lo) + lo in binary64; here
+// (x - min) * f + lo with f = (hi - lo) / (max - min) formed once per block
+// in binary64 (min and max are exact as binary64) and the per-vertex
+// arithmetic in pairs, within ~2^-47 of the value.  A constant field
+// (max == min) gives NaN, as the reference's division does.
 __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_planet *__restrict__ P, int np,
-                                                           const float *__restrict__ raw,
-                                                           const uint32_t *__restrict__ minmax, float lo, float hi,
-                                                           float w0h, float w0l, float4 *__restrict__ st0,
-                                                           float4 *__restrict__ st1, int64_t total)
+                                                           const float2 *__restrict__ raw,
+                                                           const unsigned long long *__restrict__ minmax,
+                                                           double lo, double hi, float w0h, float w0l,
+                                                           float4 *__restrict__ st0, float4 *__restrict__ st1,
+                                                           int64_t total)
 {
+    __shared__ float s_c[6];
+    const float loh = (float)lo, lol = (float)(lo - (double)(float)lo);
     for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
         const int p = block_planet(P, np, blk * 256);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned long long kmn = minmax[2 * p], kmx = minmax[2 * p + 1];
+            const float mnh = unkey((uint32_t)(kmn >> 32)), mnl = unkey((uint32_t)kmn);
+            const float mxh = unkey((uint32_t)(kmx >> 32)), mxl = unkey((uint32_t)kmx);
+            const double mn = (double)mnh + (double)mnl, mx = (double)mxh + (double)mxl;
+            const double f = (hi - lo) / (mx - mn);
+            const float fh = (float)f;
+            s_c[0] = mnh;
+            s_c[1] = mnl;
+            s_c[2] = fh;
+            s_c[3] = (float)(f - (double)fh);
+        }
+        __syncthreads();
         const int64_t row = blk * 256 + threadIdx.x;
         const int64_t i = row - P[p].vbeg;
         if (i < 0 || i >= P[p].n) continue;
-        const float mn = unkey(minmax[2 * p]), mx = unkey(minmax[2 * p + 1]);
-        const float range = __fsub_rn(mx, mn);
-        const float sc = __fdiv_rn(__fsub_rn(hi, lo), range);
-        // ((x - min) * ((hi - lo) / (max - min))) + lo, unfused
-        const float h = __fadd_rn(__fmul_rn(__fsub_rn(raw[row], mn), sc), lo);
+        const float2 r = raw[row];
+        const float mnh = s_c[0], mnl = s_c[1], fh = s_c[2], fl = s_c[3];
+        // t = raw - min
+        float th, te;
+        {
+            th = __fsub_rn(r.x, mnh);
+            const float bb = __fsub_rn(th, r.x);
+            te = __fadd_rn(__fsub_rn(r.x, __fsub_rn(th, bb)), __fsub_rn(-mnh, bb));
+        }
+        const float tl = __fadd_rn(te, __fsub_rn(r.y, mnl));
+        // t * f
+        const float ph = __fmul_rn(th, fh);
+        float pl = __fmaf_rn(th, fh, -ph);
+        pl = __fmaf_rn(th, fl, __fmaf_rn(tl, fh, pl));
+        // + lo, renormalised
+        float sh, se;
+        {
+            sh = __fadd_rn(ph, loh);
+            const float bb = __fsub_rn(sh, ph);
+            se = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bb)), __fsub_rn(loh, bb));
+        }
+        const float sl = __fadd_rn(se, __fadd_rn(pl, lol));
+        const float h = __fadd_rn(sh, sl);
+        const float hl = __fsub_rn(sl, __fsub_rn(h, sh));
         float4 *dst = (P[p].iters & 1) ? st1 : st0;
-        dst[2 * row] = make_float4(h, 0.0f, w0h, w0l);
+        dst[2 * row] = make_float4(h, hl, w0h, w0l);
         dst[2 * row + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
-// Heights of every planet after its run: (h_hi + h_lo) * 2^K rounded once
-// to binary32.  The pair's sum is exact in binary64, so its binary32 sum
-// hi + lo is that value rounded once; scaling by 2^K is then exact while
-// the result stays a normal binary32.  Only other results (zero, subnormal,
-// overflow) take the binary64 route -- GB300's binary64 rate is low.
+// Heights of every planet after its run: (h_hi + h_lo) * 2^K in binary64.
+// The pair's sum is exact in binary64 and scaling by 2^K is exact, so the
+// value is the state's to the last bit of the pair.
 __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_planet *__restrict__ P, int np,
                                                               const float4 *__restrict__ st,
                                                               const nx_erosion_ctl *__restrict__ ctl,
-                                                              float *__restrict__ out, int64_t total)
+                                                              double *__restrict__ out, int64_t total)
 {
     for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
         const int p = block_planet(P, np, blk * 256);
@@ -756,10 +795,7 @@ __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_p
         if (i < 0 || i >= P[p].n) continue;
         const float4 v = st[2 * row];
         const int K = ctl[P[p].slot].K[0];
-        const float r = __fadd_rn(v.x, v.y);
-        const int e = (int)((__float_as_uint(r) >> 23) & 0xFFu);
-        out[row] = (e > 0 && e + K > 0 && e + K < 255) ? scalbnf(r, K)
-                                                      : (float)ldexp((double)v.x + (double)v.y, K);
+        out[row] = ldexp((double)v.x + (double)v.y, K);
     }
 }
 
@@ -1302,8 +1338,9 @@ static int check_packed(const nx_erosion_planet *ph, int np, int64_t *total)
 }
 
 NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
-                                    int nplanets, const float *raw_dev, const uint32_t *minmax_dev, float elev_lo,
-                                    float elev_hi, double water0, float *st_dev, float *st_tmp_dev, void *stream)
+                                    int nplanets, const float *raw_dev, const unsigned long long *minmax_dev,
+                                    double elev_lo, double elev_hi, double water0, float *st_dev, float *st_tmp_dev,
+                                    void *stream)
 {
     if (nplanets <= 0) return NX_OK;
     if (!planets_dev || !planets_host || !raw_dev || !minmax_dev || !st_dev || !st_tmp_dev)
@@ -1313,7 +1350,9 @@ NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const 
     if (rc) return rc;
     if (total == 0) return NX_OK;
     const float w0h = (float)water0, w0l = (float)(water0 - (double)w0h);
-    erosion_init_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(planets_dev, nplanets, raw_dev, minmax_dev,
+    if ((uintptr_t)raw_dev & 7u) return nx::fail(NX_EINVAL, "nx_erosion_init_batch: raw pairs must be 8-byte aligned");
+    erosion_init_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(planets_dev, nplanets, (const float2 *)raw_dev,
+                                                                         minmax_dev,
                                                                          elev_lo, elev_hi, w0h, w0l, (float4 *)st_dev,
                                                                          (float4 *)st_tmp_dev, total);
     NX_CHECK_LAUNCH("erosion_init_kernel");
@@ -1322,7 +1361,7 @@ NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const 
 }
 
 NX_EXPORT int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
-                                       int nplanets, const float *st_dev, const void *workspace, float *out_dev,
+                                       int nplanets, const float *st_dev, const void *workspace, double *out_dev,
                                        void *stream)
 {
     if (nplanets <= 0) return NX_OK;

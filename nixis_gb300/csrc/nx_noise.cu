@@ -61,6 +61,8 @@ struct FbmParams {
     double s[NX_MAX_OCTAVES];     // scale[o] (binary64 decision path)
 };
 
+static_assert(sizeof(nx_fbm_planet) == 960, "fBm planet descriptor layout");
+
 constexpr int TABLE_WORDS = 256 * 32;
 constexpr int TABLE_BYTES = TABLE_WORDS * 4;
 
@@ -76,6 +78,30 @@ __device__ __forceinline__ void build_table(uint32_t *T, const int32_t *__restri
                      ((uint32_t)(c_grad3[g] + 16) << 16) | ((uint32_t)(c_grad3[g + 1] + 16) << 24);
         T[i] = w;
     }
+}
+
+// The pair path's table: the same layout with the gradient's index (0-23,
+// perm_grad_index_3D / 3) in bits 0-4 instead of the gradient bytes; the
+// gradients themselves come as binary32 from s_grad.
+__device__ __forceinline__ void build_table_pair(uint32_t *T, const int32_t *__restrict__ perm,
+                                                 const int32_t *__restrict__ pgi)
+{
+    for (int i = threadIdx.x; i < TABLE_WORDS; i += blockDim.x) {
+        int k = i >> 5;
+        uint32_t p = (uint32_t)perm[k] & 255u;
+        int g = pgi[k];
+        g = g < 0 ? 0 : (g > 69 ? 69 : g);
+        T[i] = (uint32_t)(g / 3) | (p << 7);
+    }
+}
+
+// GRADIENTS_3D as binary32 (x, y, z, 0), filled per block.
+__shared__ float4 s_grad[24];
+
+__device__ __forceinline__ void init_grad_table()
+{
+    for (int i = threadIdx.x; i < 24; i += blockDim.x)
+        s_grad[i] = make_float4((float)c_grad3[3 * i], (float)c_grad3[3 * i + 1], (float)c_grad3[3 * i + 2], 0.0f);
 }
 
 // Hash table load: bits 7-14 of a select the entry; lb = this lane's byte
@@ -371,7 +397,7 @@ __device__ __forceinline__ int word_step(uint32_t w, int k)
 // evaluated and the region selects.  Every comparison evaluated records its
 // margin (a superset of those the branching form records), so a lane keeps
 // its binary32 decision only when all of them clear the margin.
-__device__ __forceinline__ void decide_sel(float x, float y, float z, float in_sum, Cmp<float, true> &C, Decision &D)
+__device__ __forceinline__ int decide_sel(float x, float y, float z, float in_sum, Cmp<float, true> &C, int &region)
 {
     const bool r0 = C.le(in_sum, 1.0f);
     const bool r1 = !r0 && C.ge(in_sum, 2.0f);
@@ -402,9 +428,16 @@ __device__ __forceinline__ void decide_sel(float x, float y, float z, float in_s
                         (b_lt ? 32u : 0u);
     const uint32_t tt = 64u + ((xy ? 1u : 0u) | (zb ? 2u : 0u) | (za ? 4u : 0u) | (n1 ? 8u : 0u) | (n2 ? 16u : 0u) |
                                (cnb ? 32u : 0u) | (r1 ? 64u : 0u));
-    const float4 *t = s_extra + 2 * (tet ? tt : ot);
+    region = r0 ? 0 : (r1 ? 1 : 2);
+    return (int)(tet ? tt : ot);
+}
+
+// Decision of a binary32-path lane from its case-table entry.
+__device__ __forceinline__ void case_decision(int ci, int region, Decision &D)
+{
+    const float4 *t = s_extra + 2 * ci;
     const float4 a = t[0], b = t[1];
-    D.region = r0 ? 0 : (r1 ? 1 : 2);
+    D.region = region;
     D.w = __float_as_uint(b.z);
     D.E[0] = a.x; D.E[1] = a.y; D.E[2] = a.z; D.E[3] = a.w; D.E[4] = b.x; D.E[5] = b.y;
 }
@@ -422,6 +455,7 @@ struct Cell {
     int xb7, yb7, zb7;       // cell origin << 7 (hash base)
     int xsb, ysb, zsb;       // cell origin (trace only)
     Decision D;
+    double dxd, dyd, dzd;    // binary64 path only: the displacement before rounding to binary32
 };
 
 // Binary64 decisions with the reference's operation order (opensimplex.py:
@@ -444,14 +478,56 @@ __device__ __noinline__ Cell decide_f64(double X, double Y, double Z, double s)
     C.m = 0.f;
     decide<double, false>(xins, yins, zins, in_sum, C, c.D);
     pack_extra(c.D);
-    c.dx0 = (float)__dsub_rn(x, xb);
-    c.dy0 = (float)__dsub_rn(y, yb);
-    c.dz0 = (float)__dsub_rn(z, zb);
+    c.dxd = __dsub_rn(x, xb);
+    c.dyd = __dsub_rn(y, yb);
+    c.dzd = __dsub_rn(z, zb);
+    c.dx0 = (float)c.dxd;
+    c.dy0 = (float)c.dyd;
+    c.dz0 = (float)c.dzd;
     c.xsb = (int)xsb; c.ysb = (int)ysb; c.zsb = (int)zsb;
     c.xb7 = (int)((unsigned)xsb << 7);
     c.yb7 = (int)((unsigned)ysb << 7);
     c.zb7 = (int)((unsigned)zsb << 7);
     return c;
+}
+
+// What the decision from a coordinate split leaves for the displacement:
+// the floors f of the skewed fractions and G = r + fx + fy + fz, so that
+// dx0 = a_x - (3 fx + G) / 3 (and likewise y, z), and the case-table index.
+struct Core {
+    int xsb, ysb, zsb;
+    int xb7, yb7, zb7;
+    float fx, fy, fz, G;
+    int region, ci;
+};
+
+// The decision from the split of x*scale into integers A (binary32, |A| <
+// 2^22) and fractions a (|a| < 1) for each axis; `big` = max |x*scale|.
+// Returns false when binary64 must decide.  The error analysis is at
+// decide_f32 (a within 3.1e-8 of x*scale - A).
+__device__ __forceinline__ bool decide_core(float Ax, float ax, float Ay, float ay, float Az, float az, float big,
+                                            Core &o)
+{
+    const float T = __fadd_rn(__fadd_rn(Ax, Ay), Az);
+    const float q = floorf(__fmaf_rn(T, SIXTH, 1.0f / 12.0f));
+    const float r = __fmaf_rn(-6.0f, q, T);
+    const float u = __fadd_rn(r, __fadd_rn(__fadd_rn(ax, ay), az));
+    const float bx = __fmaf_rn(-u, SIXTH, ax), by = __fmaf_rn(-u, SIXTH, ay), bz = __fmaf_rn(-u, SIXTH, az);
+    const float fx = floorf(bx), fy = floorf(by), fz = floorf(bz);
+    const float xins = __fsub_rn(bx, fx), yins = __fsub_rn(by, fy), zins = __fsub_rn(bz, fz);
+    const float xsbf = __fadd_rn(__fsub_rn(Ax, q), fx), ysbf = __fadd_rn(__fsub_rn(Ay, q), fy),
+                zsbf = __fadd_rn(__fsub_rn(Az, q), fz);
+    const int xi = __float_as_int(__fadd_rn(xsbf, MAGIC)), yi = __float_as_int(__fadd_rn(ysbf, MAGIC)),
+              zi = __float_as_int(__fadd_rn(zsbf, MAGIC));
+    o.xsb = xi - MAGIC_BITS; o.ysb = yi - MAGIC_BITS; o.zsb = zi - MAGIC_BITS;
+    o.xb7 = xi << 7; o.yb7 = yi << 7; o.zb7 = zi << 7;
+    o.fx = fx; o.fy = fy; o.fz = fz;
+    o.G = __fadd_rn(r, __fadd_rn(__fadd_rn(fx, fy), fz));
+    Cmp<float, true> C;
+    C.m = fminf(fminf(fminf(xins, 1.0f - xins), fminf(yins, 1.0f - yins)), fminf(zins, 1.0f - zins));
+    const float in_sum = __fadd_rn(__fadd_rn(xins, yins), zins);
+    o.ci = decide_sel(xins, yins, zins, in_sum, C, o.region);
+    return C.m >= TAU && big < PMAX;
 }
 
 // Binary32 path.  Returns false when binary64 must decide.
@@ -483,24 +559,16 @@ __device__ __forceinline__ bool decide_f32(float xh, float xl, float yh, float y
     float big = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
     float Ax = (px + MAGIC) - MAGIC, Ay = (py + MAGIC) - MAGIC, Az = (pz + MAGIC) - MAGIC;
     float ax = (px - Ax) + ex, ay = (py - Ay) + ey, az = (pz - Az) + ez;
-    float T = (Ax + Ay) + Az;
-    float q = floorf(fmaf(T, SIXTH, 1.0f / 12.0f));
-    float r = fmaf(-6.0f, q, T);
-    float u = r + ((ax + ay) + az);
-    float bx = fmaf(-u, SIXTH, ax), by = fmaf(-u, SIXTH, ay), bz = fmaf(-u, SIXTH, az);
-    float fx = floorf(bx), fy = floorf(by), fz = floorf(bz);
-    float xins = bx - fx, yins = by - fy, zins = bz - fz;
-    float xsbf = (Ax - q) + fx, ysbf = (Ay - q) + fy, zsbf = (Az - q) + fz;
-    int xi = __float_as_int(xsbf + MAGIC), yi = __float_as_int(ysbf + MAGIC), zi = __float_as_int(zsbf + MAGIC);
-    c.xsb = xi - MAGIC_BITS; c.ysb = yi - MAGIC_BITS; c.zsb = zi - MAGIC_BITS;
-    c.xb7 = xi << 7; c.yb7 = yi << 7; c.zb7 = zi << 7;
-    float g = (r + ((fx + fy) + fz)) * THIRD;
-    c.dx0 = (ax - fx) - g; c.dy0 = (ay - fy) - g; c.dz0 = (az - fz) - g;
-    Cmp<float, true> C;
-    C.m = fminf(fminf(fminf(xins, 1.0f - xins), fminf(yins, 1.0f - yins)), fminf(zins, 1.0f - zins));
-    float in_sum = (xins + yins) + zins;
-    decide_sel(xins, yins, zins, in_sum, C, c.D);
-    return C.m >= TAU && big < PMAX;
+    Core o;
+    const bool ok = decide_core(Ax, ax, Ay, ay, Az, az, big, o);
+    c.xsb = o.xsb; c.ysb = o.ysb; c.zsb = o.zsb;
+    c.xb7 = o.xb7; c.yb7 = o.yb7; c.zb7 = o.zb7;
+    const float g = __fmul_rn(o.G, THIRD);
+    c.dx0 = __fsub_rn(__fsub_rn(ax, o.fx), g);
+    c.dy0 = __fsub_rn(__fsub_rn(ay, o.fy), g);
+    c.dz0 = __fsub_rn(__fsub_rn(az, o.fz), g);
+    case_decision(o.ci, o.region, c.D);
+    return ok;
 }
 
 // One lattice contribution: attn^4 * (grad . d) if attn > 0.
@@ -613,6 +681,391 @@ __device__ __forceinline__ float noise_raw(float xh, float xl, float yh, float y
     return v;
 }
 
+
+// ---------------------------------------------------------------------------
+// Pair-precision noise (the batched, plain and served planet paths).
+//
+// Eroded planets need elevations much closer to binary64 than binary32
+// gives: the erosion update branches on the sign of every neighbour height
+// difference, and starting heights off by binary32 rounding (3e-7 relative)
+// flip near-ties, after which water, sediment and heights leave the binary64
+// trajectory (0.4 % of max |h| after 30 iterations, 13 % after 60, on a
+// 100,002-vertex sphere; random errors of 1e-11 in the raw fBm sum flipped
+// nothing in 100 iterations on 900,002 vertices, 1e-10 did).  This path
+// takes the same decisions as the binary32 one and carries every
+// continuous quantity as an unevaluated pair hi + lo of binary32s:
+//  * x*scale = A + a1 + a2 + a3 exactly (A an integer): for a power-of-two
+//    scale the vertex's binary32 triple scaled, otherwise the product of
+//    the vertex and scale triples to ~2^-70 relative;
+//  * dx0 = a - (3f + G)/3 (f, G from the decision) and every slot's offset
+//    K = m/3 are anchored: hi on the 2^-21 grid, so the hi part of d =
+//    dx0 - K is exact and only the lo parts round (~2^-46); d is then
+//    renormalised (|lo| <= ulp(hi)/2), which keeps the cross terms 2 hi lo
+//    of |d|^2 small enough to sum to ~2^-46;
+//  * attn = 2 - |d|^2, attn^4, grad . d and their product with error-free
+//    transforms (fma-exact products, two-sums; the running 2 - dx^2 - dy^2
+//    - dz^2 uses fast two-sums, exact whenever attn > 0), two slots at a
+//    time in paired binary32 lanes;
+//  * the contributions, the division by 103 and the octave's
+//    (noise + 1) * 0.5 * strength * radius term are summed in pairs; the
+//    running sum over octaves is renormalised after every octave, so a
+//    vertex gives the same bits whether its octaves run in one launch or
+//    one launch each.
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// Knuth's two-sum per lane: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &e)
+{
+    s = add2(a, b);
+    const float2 bb = sub2(s, a);
+    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+__device__ __forceinline__ void two_sum1(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Anchored thirds m/3, m = 0..6: hi = rint(m 2^21 / 3) 2^-21, lo = m/3 - hi
+// (+-1/(3 2^21) or 0).
+constexpr float ANC = 6.0f;                         // (v + 6) - 6 rounds v in [-2, 2) to the 2^-21 grid
+constexpr float T1H = 699051.0f / 2097152.0f;       // 1/3
+constexpr float T2H = 1398101.0f / 2097152.0f;      // 2/3
+constexpr float T4H = 2796203.0f / 2097152.0f;      // 4/3
+constexpr float T5H = 3495253.0f / 2097152.0f;      // 5/3
+constexpr float C3L = (float)(1.0 / (3.0 * 2097152.0));   // 2^-21 / 3: |lo| of the thirds above
+constexpr float C3L2 = 2.0f * C3L;
+
+// Anchored m/3 for an integer m (|m| < 2^9): hi on the 2^-21 grid, lo.
+__device__ __forceinline__ void anchor_third(int m, float &H, float &L)
+{
+    const int N = m * 2097152;
+    const int q = N >= 0 ? (N + 1) / 3 : -((1 - N) / 3);
+    H = __fmul_rn((float)q, 1.0f / 2097152.0f);
+    L = __fmul_rn((float)(N - 3 * q), C3L);
+}
+
+// Pair case table of a block: entry i (as s_extra) is four float4s: the two
+// extra points' offsets e + (ex + ey + ez)/3 anchored, hi parts
+// (E0x, E0y, E0z, E1x), (E1y, E1z, case word, 0), doubled lo parts
+// (E0x, E0y, E0z, E1x), (E1y, E1z, 0, 0).
+__shared__ float4 s_extra_p[4 * 192];
+
+__device__ __forceinline__ void anchored_offsets(uint32_t w, float *H, float *L)
+{
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+        const int ox = word_offset(w, 3 * p), oy = word_offset(w, 3 * p + 1), oz = word_offset(w, 3 * p + 2);
+        const int t = ox + oy + oz;
+        anchor_third(3 * ox + t, H[3 * p], L[3 * p]);
+        anchor_third(3 * oy + t, H[3 * p + 1], L[3 * p + 1]);
+        anchor_third(3 * oz + t, H[3 * p + 2], L[3 * p + 2]);
+    }
+}
+
+__device__ __forceinline__ void init_extra_table_pair()
+{
+    for (int i = threadIdx.x; i < 192; i += blockDim.x) {
+        const uint32_t w = i < 64 ? octa_case(i) : tetra_case(i - 64);
+        float H[6], L[6];
+        anchored_offsets(w, H, L);
+        s_extra_p[4 * i] = make_float4(H[0], H[1], H[2], H[3]);
+        s_extra_p[4 * i + 1] = make_float4(H[4], H[5], __uint_as_float(w), 0.0f);
+        s_extra_p[4 * i + 2] = make_float4(2.0f * L[0], 2.0f * L[1], 2.0f * L[2], 2.0f * L[3]);
+        s_extra_p[4 * i + 3] = make_float4(2.0f * L[4], 2.0f * L[5], 0.0f, 0.0f);
+    }
+}
+
+// d = dx0 - K for one axis of two slots, from the anchored dx0 (hi X0H,
+// doubled lo X0L2) and offsets (K, doubled lo KL2): the hi part dx0 - K is
+// exact (both on the 2^-21 grid); then renormalised by a fast two-sum
+// (|hi| >= 2^-21 > |lo| or hi = 0), H + L2/2 == d with |L2/2| <=
+// ulp(H)/2.  L2 = 2 lo (exact: twice the fast two-sum's exact error).
+// Without NORM the anchored pair is used as it is (|lo| up to 2^-20): the
+// cross terms then carry ~2^-42 of error, which octaves of small amplitude
+// can afford (see noise_pair).
+template <bool NORM>
+__device__ __forceinline__ void slot_disp(float X0H, float X0L2, float2 K, float2 KL2, float2 &H, float2 &L2)
+{
+    const float2 h0 = sub2(f2(X0H, X0H), K);
+    const float2 l2 = sub2(f2(X0L2, X0L2), KL2);
+    if (NORM) {
+        H = fma2(f2(0.5f, 0.5f), l2, h0);
+        L2 = fma2(f2(-2.0f, -2.0f), sub2(H, h0), l2);
+    } else {
+        H = h0;
+        L2 = l2;
+    }
+}
+
+// Two lattice contributions (slots a, b in the lanes) in pair arithmetic,
+// added to the pair accumulator (AH, AL).  X0H, X0L2: the anchored dx0 (hi,
+// 2 lo); KX/KXL2 the slots' anchored offsets (hi, 2 lo); ON 1/0 masks.
+template <bool NORM>
+__device__ __forceinline__ void contrib2_pair(uint32_t wa, uint32_t wb, float X0H, float X0L2, float Y0H, float Y0L2,
+                                              float Z0H, float Z0L2, float2 KX, float2 KXL2, float2 KY, float2 KYL2,
+                                              float2 KZ, float2 KZL2, float2 ON, float2 &AH, float2 &AL)
+{
+    float2 Xh, X2, Yh, Y2, Zh, Z2;
+    slot_disp<NORM>(X0H, X0L2, KX, KXL2, Xh, X2);
+    slot_disp<NORM>(Y0H, Y0L2, KY, KYL2, Yh, Y2);
+    slot_disp<NORM>(Z0H, Z0L2, KZ, KZL2, Zh, Z2);
+    // attn = 2 - |d|^2: squares of the hi parts exact as p + pe, plus the
+    // cross terms 2 hi lo
+    const float2 px = mul2(Xh, Xh), py = mul2(Yh, Yh), pz = mul2(Zh, Zh);
+    const float2 pxe = fma2(Xh, Xh, f2(-px.x, -px.y)), pye = fma2(Yh, Yh, f2(-py.x, -py.y)),
+                 pze = fma2(Zh, Zh, f2(-pz.x, -pz.y));
+    float2 L = add2(pxe, add2(pye, pze));
+    L = fma2(Xh, X2, L);
+    L = fma2(Yh, Y2, L);
+    L = fma2(Zh, Z2, L);
+    const float2 two = f2(2.0f, 2.0f);
+    const float2 r1 = sub2(two, px), r2 = sub2(r1, py), r3 = sub2(r2, pz);
+    const float2 e1 = sub2(sub2(two, r1), px), e2 = sub2(sub2(r1, r2), py), e3 = sub2(sub2(r2, r3), pz);
+    const float2 al = sub2(add2(add2(e1, e2), e3), L);
+    // only attn > 0 counts, and only in the region (ah = 0 zeroes the rest)
+    const float2 ah = mul2(f2(fmaxf(r3.x, 0.0f), fmaxf(r3.y, 0.0f)), ON);
+    // attn^2, attn^4 as pairs
+    const float2 h2 = mul2(ah, ah);
+    float2 l2 = fma2(ah, ah, f2(-h2.x, -h2.y));
+    l2 = fma2(add2(ah, ah), al, l2);
+    const float2 h4 = mul2(h2, h2);
+    float2 l4 = fma2(h2, h2, f2(-h4.x, -h4.y));
+    l4 = fma2(add2(h2, h2), l2, l4);
+    // grad . d
+    const float4 ga = s_grad[wa & 31u], gb = s_grad[wb & 31u];
+    const float2 gx = f2(ga.x, gb.x), gy = f2(ga.y, gb.y), gz = f2(ga.z, gb.z);
+    const float2 qx = mul2(gx, Xh), qy = mul2(gy, Yh), qz = mul2(gz, Zh);
+    const float2 qxe = fma2(gx, Xh, f2(-qx.x, -qx.y)), qye = fma2(gy, Yh, f2(-qy.x, -qy.y)),
+                 qze = fma2(gz, Zh, f2(-qz.x, -qz.y));
+    float2 s1, t1, dh, t2;
+    two_sum2(qx, qy, s1, t1);
+    two_sum2(s1, qz, dh, t2);
+    const float2 gl = fma2(gx, X2, fma2(gy, Y2, mul2(gz, Z2)));     // 2 (grad . lo)
+    const float2 dl = fma2(f2(0.5f, 0.5f), gl, add2(add2(add2(qxe, qye), qze), add2(t1, t2)));
+    // attn^4 * (grad . d)
+    const float2 ch = mul2(h4, dh);
+    float2 cl = fma2(h4, dh, f2(-ch.x, -ch.y));
+    cl = fma2(h4, dl, fma2(l4, dh, cl));
+    float2 s, e;
+    two_sum2(AH, ch, s, e);
+    AH = s;
+    AL = add2(AL, add2(e, cl));
+}
+
+// x*scale = A + a1 + a2 + a3 for one axis: x = x1 + x2 + x3 and scale =
+// s1 + s2 + s3 exact binary32 triples; |x*scale| < 2^22 for A to be exact.
+__device__ __forceinline__ void coord_split(float x1, float x2, float x3, float s1, float s2, float s3, bool pow2,
+                                            float &A, float &a1, float &a2, float &a3)
+{
+    const float p = __fmul_rn(x1, s1);
+    A = __fsub_rn(__fadd_rn(p, MAGIC), MAGIC);
+    a1 = __fsub_rn(p, A);
+    if (pow2) {                       // scale = s1, a power of two: exact scaling
+        a2 = __fmul_rn(x2, s1);
+        a3 = __fmul_rn(x3, s1);
+        return;
+    }
+    const float e11 = __fmaf_rn(x1, s1, -p);
+    const float p12 = __fmul_rn(x1, s2), e12 = __fmaf_rn(x1, s2, -p12);
+    const float p21 = __fmul_rn(x2, s1), e21 = __fmaf_rn(x2, s1, -p21);
+    const float q = __fmaf_rn(x1, s3, __fmaf_rn(x2, s2, __fmul_rn(x3, s1)));
+    float b, c, b2, c2;
+    two_sum1(p12, p21, b, c);
+    two_sum1(b, e11, b2, c2);
+    a2 = b2;
+    a3 = __fadd_rn(__fadd_rn(c, c2), __fadd_rn(__fadd_rn(e12, e21), q));
+}
+
+// Anchor a pair (h, l) with h in [-2, 2): hi on the 2^-21 grid, lo.
+__device__ __forceinline__ void anchor_pair(float h, float l, float &H, float &L)
+{
+    H = __fsub_rn(__fadd_rn(h, ANC), ANC);
+    L = __fadd_rn(__fsub_rn(h, H), l);
+}
+
+// A binary64 value in [-2, 2) anchored (binary64 decision path).
+__device__ __forceinline__ void anchor_f64(double d, float &H, float &L)
+{
+    const float h = __double2float_rn(d);
+    anchor_pair(h, __double2float_rn(__dsub_rn(d, (double)h)), H, L);
+}
+
+// Per-octave constants of the pair path.
+struct OctP {
+    float s1, s2, s3;     // scale as a binary32 triple
+    float amph, ampl;     // 0.5 * strength * radius as a pair
+    double s;             // scale (binary64 decision path)
+    bool norm;            // renormalise the displacements (noise_pair<true>)
+};
+
+// noise3d(x * s) as a pair (vh, vl) of 103 * noise, for one vertex and
+// octave.  x1..z3: the vertex's binary32 triples (x1 + x2 + x3 == x).
+//
+// A lane evaluates at most 8 lattice points: its region's fixed corners
+// (tetrahedra: the corner at 0 or 1 and its three neighbours; octahedron:
+// the six mixed corners) and the two extra points.  The corners are
+// assigned to lanes per region (selects), so a warp runs four slot pairs:
+// X1..X4 (every region), X5/X6 (octahedron only) and the extra points.
+//
+// NORM: renormalise the slots' displacements.  Without it the value carries
+// up to ~1.5e-13 * (0.5 strength radius) of extra error, so the planet
+// paths skip it only for octaves whose amplitude is at most 1/8 of the
+// first one's (|error| <= 2e-14 of a field whose range is ~2 amp_0).
+template <bool NORM>
+__device__ __forceinline__ void noise_pair(float x1, float x2, float x3, float y1, float y2, float y3, float z1,
+                                           float z2, float z3, const OctP &O, bool pow2, uint32_t lb, unsigned &nfb,
+                                           float &vh, float &vl)
+{
+    float Ax, ax1, ax2, ax3, Ay, ay1, ay2, ay3, Az, az1, az2, az3;
+    coord_split(x1, x2, x3, O.s1, O.s2, O.s3, pow2, Ax, ax1, ax2, ax3);
+    coord_split(y1, y2, y3, O.s1, O.s2, O.s3, pow2, Ay, ay1, ay2, ay3);
+    coord_split(z1, z2, z3, O.s1, O.s2, O.s3, pow2, Az, az1, az2, az3);
+    const float ax = __fadd_rn(ax1, ax2), ay = __fadd_rn(ay1, ay2), az = __fadd_rn(az1, az2);
+    const float big = fmaxf(fabsf(__fadd_rn(Ax, ax)), fmaxf(fabsf(__fadd_rn(Ay, ay)), fabsf(__fadd_rn(Az, az))));
+    Core o;
+    int region, xb7, yb7, zb7;
+    uint32_t ew;
+    float X0H, X0L2, Y0H, Y0L2, Z0H, Z0L2;
+    float EH[6], EL2[6];
+    if (decide_core(Ax, ax, Ay, ay, Az, az, big, o)) {
+        region = o.region;
+        xb7 = o.xb7; yb7 = o.yb7; zb7 = o.zb7;
+        // the fraction anchored, then dx0 = a - (f + G/3)
+        float GH, GL;
+        anchor_third((int)o.G, GH, GL);
+        const float GL2 = __fmul_rn(2.0f, GL);
+        const float FXH = __fsub_rn(__fadd_rn(ax, ANC), ANC), FYH = __fsub_rn(__fadd_rn(ay, ANC), ANC),
+                    FZH = __fsub_rn(__fadd_rn(az, ANC), ANC);
+        const float FXL = __fadd_rn(__fadd_rn(__fsub_rn(ax1, FXH), ax2), ax3);
+        const float FYL = __fadd_rn(__fadd_rn(__fsub_rn(ay1, FYH), ay2), ay3);
+        const float FZL = __fadd_rn(__fadd_rn(__fsub_rn(az1, FZH), az2), az3);
+        X0H = __fsub_rn(FXH, __fadd_rn(o.fx, GH));
+        Y0H = __fsub_rn(FYH, __fadd_rn(o.fy, GH));
+        Z0H = __fsub_rn(FZH, __fadd_rn(o.fz, GH));
+        X0L2 = __fmaf_rn(2.0f, FXL, -GL2);
+        Y0L2 = __fmaf_rn(2.0f, FYL, -GL2);
+        Z0L2 = __fmaf_rn(2.0f, FZL, -GL2);
+        const float4 *t = s_extra_p + 4 * o.ci;
+        const float4 t0 = t[0], t1 = t[1], t2 = t[2], t3 = t[3];
+        EH[0] = t0.x; EH[1] = t0.y; EH[2] = t0.z; EH[3] = t0.w; EH[4] = t1.x; EH[5] = t1.y;
+        ew = __float_as_uint(t1.z);
+        EL2[0] = t2.x; EL2[1] = t2.y; EL2[2] = t2.z; EL2[3] = t2.w; EL2[4] = t3.x; EL2[5] = t3.y;
+    } else {
+        // the vertex as binary64 (the triple's sum is exact)
+        const double X = (double)x1 + (double)x2 + (double)x3, Y = (double)y1 + (double)y2 + (double)y3,
+                     Z = (double)z1 + (double)z2 + (double)z3;
+        const Cell c = decide_f64(X, Y, Z, O.s);
+        ++nfb;
+        region = c.D.region;
+        xb7 = c.xb7; yb7 = c.yb7; zb7 = c.zb7;
+        float L;
+        anchor_f64(c.dxd, X0H, L);
+        X0L2 = __fmul_rn(2.0f, L);
+        anchor_f64(c.dyd, Y0H, L);
+        Y0L2 = __fmul_rn(2.0f, L);
+        anchor_f64(c.dzd, Z0H, L);
+        Z0L2 = __fmul_rn(2.0f, L);
+        ew = c.D.w;
+        float EL[6];
+        anchored_offsets(ew, EH, EL);
+        for (int k = 0; k < 6; ++k) EL2[k] = __fmul_rn(2.0f, EL[k]);
+    }
+    const bool r1 = region == 1, r2 = region == 2;
+    uint32_t h0 = lk(lb, xb7), h1 = lk(lb, xb7 + 128);
+    uint32_t h00 = lk(lb, (int)h0 + yb7), h01 = lk(lb, (int)h0 + yb7 + 128);
+    uint32_t h10 = lk(lb, (int)h1 + yb7), h11 = lk(lb, (int)h1 + yb7 + 128);
+    const int zo0 = zb7, zo1 = zb7 + 128;
+    const uint32_t w0 = lk(lb, r1 ? (int)h11 + zo1 : (int)h00 + zo0);
+    const uint32_t w100 = lk(lb, (int)h10 + zo0), w010 = lk(lb, (int)h01 + zo0), w001 = lk(lb, (int)h00 + zo1);
+    const uint32_t w110 = lk(lb, (int)h11 + zo0), w101 = lk(lb, (int)h10 + zo1), w011 = lk(lb, (int)h01 + zo1);
+    const int xm = xb7 - 128, ym = yb7 - 128, zm = zb7 - 128;
+    const uint32_t we0 = lk(lb, (int)lk(lb, (int)lk(lb, xm + word_step(ew, 0)) + ym + word_step(ew, 1)) + zm + word_step(ew, 2));
+    const uint32_t we1 = lk(lb, (int)lk(lb, (int)lk(lb, xm + word_step(ew, 3)) + ym + word_step(ew, 4)) + zm + word_step(ew, 5));
+    // fixed corners per lane (offsets o + (ox + oy + oz)/3 in thirds: A1 =
+    // (1,0,0) -> (4,1,1)/3, A2 (1,4,1)/3, A3 (1,1,4)/3, B1 = (1,1,0) ->
+    // (5,5,2)/3, B2 (5,2,5)/3, B3 (2,5,5)/3; corner 0: (0,0,0) or (2,2,2));
+    // A-corners' anchored lo is -C3L, B-corners' +C3L, the corner's 0
+    const float k0 = r1 ? 2.0f : 0.0f;
+    const float nL2 = -C3L2, pL2 = C3L2;
+    //   X1: r2 ? A1 : corner 0       X2: r2 ? A2 : (r1 ? B1 : A1)
+    //   X3: r2 ? A3 : (r1 ? B2 : A2) X4: r2 ? B1 : (r1 ? B3 : A3)
+    //   X5: B2, X6: B3 (octahedron only)
+    const uint32_t wX1 = r2 ? w100 : w0, wX2 = r2 ? w010 : (r1 ? w110 : w100);
+    const uint32_t wX3 = r2 ? w001 : (r1 ? w101 : w010), wX4 = r2 ? w110 : (r1 ? w011 : w001);
+    const float2 X1X2x = f2(r2 ? T4H : k0, r2 ? T1H : (r1 ? T5H : T4H));
+    const float2 X1X2y = f2(r2 ? T1H : k0, r2 ? T4H : (r1 ? T5H : T1H));
+    const float2 X1X2z = f2(r2 ? T1H : k0, r2 ? T1H : (r1 ? T2H : T1H));
+    const float2 X1X2l = f2(r2 ? nL2 : 0.0f, r1 ? pL2 : nL2);
+    const float2 X3X4x = f2(r2 ? T1H : (r1 ? T5H : T1H), r2 ? T5H : (r1 ? T2H : T1H));
+    const float2 X3X4y = f2(r2 ? T1H : (r1 ? T2H : T4H), r2 ? T5H : (r1 ? T5H : T1H));
+    const float2 X3X4z = f2(r2 ? T4H : (r1 ? T5H : T1H), r2 ? T2H : (r1 ? T5H : T4H));
+    const float2 X3X4l = f2(r1 ? pL2 : nL2, (r1 || r2) ? pL2 : nL2);
+    const float fr2 = r2 ? 1.0f : 0.0f;
+    float2 AH = f2(0.0f, 0.0f), AL = f2(0.0f, 0.0f);
+    contrib2_pair<NORM>(wX1, wX2, X0H, X0L2, Y0H, Y0L2, Z0H, Z0L2, X1X2x, X1X2l, X1X2y, X1X2l, X1X2z, X1X2l, f2(1.0f, 1.0f),
+                  AH, AL);
+    contrib2_pair<NORM>(wX3, wX4, X0H, X0L2, Y0H, Y0L2, Z0H, Z0L2, X3X4x, X3X4l, X3X4y, X3X4l, X3X4z, X3X4l, f2(1.0f, 1.0f),
+                  AH, AL);
+    contrib2_pair<NORM>(w101, w011, X0H, X0L2, Y0H, Y0L2, Z0H, Z0L2, f2(T5H, T2H), f2(pL2, pL2), f2(T2H, T5H), f2(pL2, pL2),
+                  f2(T5H, T5H), f2(pL2, pL2), f2(fr2, fr2), AH, AL);
+    contrib2_pair<NORM>(we0, we1, X0H, X0L2, Y0H, Y0L2, Z0H, Z0L2, f2(EH[0], EH[3]), f2(EL2[0], EL2[3]), f2(EH[1], EH[4]),
+                  f2(EL2[1], EL2[4]), f2(EH[2], EH[5]), f2(EL2[2], EL2[5]), f2(1.0f, 1.0f), AH, AL);
+    float e;
+    two_sum1(AH.x, AH.y, vh, e);
+    vl = __fadd_rn(e, __fadd_rn(AL.x, AL.y));
+}
+
+// The octave's term (v/103 + 1) * amp added to the running pair (rh, rl),
+// then renormalised (|rl| <= ulp(rh)/2).
+__device__ __forceinline__ void octave_accumulate(float vh, float vl, float amph, float ampl, float &rh, float &rl)
+{
+    constexpr float R103 = 1.0f / 103.0f;
+    const float wq = __fmul_rn(vh, R103);
+    const float rem = __fmaf_rn(-wq, 103.0f, vh);                 // exact
+    const float wl = __fmul_rn(__fadd_rn(rem, vl), R103);
+    const float s = __fadd_rn(1.0f, wq);                          // |wq| <= 1: fast two-sum
+    const float lo = __fadd_rn(__fadd_rn(__fsub_rn(1.0f, s), wq), wl);
+    const float th = __fmul_rn(s, amph);
+    float tl = __fmaf_rn(s, amph, -th);
+    tl = __fmaf_rn(s, ampl, __fmaf_rn(lo, amph, tl));
+    float sh, se;
+    two_sum1(rh, th, sh, se);
+    const float sl = __fadd_rn(rl, __fadd_rn(se, tl));
+    rh = __fadd_rn(sh, sl);
+    rl = __fsub_rn(sl, __fsub_rn(rh, sh));
+}
+
+// Split a binary64 into three binary32s x1 + x2 + x3 == v exactly (normal
+// range, |v| in [2^-100, 2^100]; others give x1 = (float)v and the rest 0,
+// and such lanes decide in binary64 anyway).
+__device__ __forceinline__ void split3_f64(double v, float &x1, float &x2, float &x3)
+{
+    x1 = __double2float_rz(v);
+    const double r1 = __dsub_rn(v, (double)x1);     // exact: x1 is v truncated to 24 bits
+    x2 = __double2float_rz(r1);
+    x3 = __double2float_rn(__dsub_rn(r1, (double)x2));   // at most 5 bits left: exact
+}
+
+// Ordered-key transform: unsigned comparisons of keys follow float order.
+__device__ __forceinline__ uint32_t fkey(float f)
+{
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b ^ 0x80000000u);
+}
+
+// Ordered 64-bit key of a normalised pair: unsigned key order = value order.
+__device__ __forceinline__ unsigned long long pair_key(float h, float l)
+{
+    return ((unsigned long long)fkey(h) << 32) | (unsigned long long)fkey(l);
+}
+
 __device__ __forceinline__ uint32_t lane_base(const uint32_t *T)
 {
     return (uint32_t)__cvta_generic_to_shared(T) + ((threadIdx.x & 31u) << 2);
@@ -689,12 +1142,6 @@ __global__ void __launch_bounds__(256) trace_kernel(const double *__restrict__ x
     }
 }
 
-// Ordered-key transform: unsigned comparisons of keys follow float order.
-__device__ __forceinline__ uint32_t fkey(float f)
-{
-    uint32_t b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ~b : (b ^ 0x80000000u);
-}
 
 constexpr int CHUNK = 2048;   // vertices per work item of the batched kernel
 
@@ -710,15 +1157,16 @@ __device__ __forceinline__ int chunk_planet(const nx_fbm_planet *P, int np, int 
 
 // Many planets in one persistent launch: work items are chunks of CHUNK
 // vertices of one planet, handed out round-robin; a block rebuilds its
-// shared table when its next chunk belongs to another planet.  Each chunk
-// also folds its min/max into the planet's ordered keys (for the rescale
-// to metres that follows).
+// shared table when its next chunk belongs to another planet.  Sums are
+// pairs (pair path above); each chunk also folds the ordered keys of its
+// sums into the planet's min/max (for the rescale to metres that follows).
 __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__restrict__ planets, int np,
                                                         int total_chunks, unsigned long long *nfb_out)
 {
     extern __shared__ __align__(16) uint32_t smem[];
-    __shared__ uint32_t s_mm[2][8];
-    init_extra_table();
+    __shared__ unsigned long long s_mm[2][8];
+    init_extra_table_pair();
+    init_grad_table();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
     int cur = -1;
@@ -728,43 +1176,146 @@ __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__r
         const nx_fbm_planet &P = planets[p];
         if (p != cur) {
             __syncthreads();
-            build_table(smem, P.perm, P.pgi);
+            build_table_pair(smem, P.perm, P.pgi);
             __syncthreads();
             cur = p;
         }
         const int64_t base = (int64_t)(c - P.chunk0) * CHUNK;
-        float mn = INFINITY, mx = -INFINITY;
+        const bool pow2 = P.pow2 != 0;
+        unsigned long long kmn = ~0ull, kmx = 0ull;
         for (int64_t i = base + threadIdx.x; i < base + CHUNK && i < P.n; i += blockDim.x) {
-            double X = P.xyz[3 * i], Y = P.xyz[3 * i + 1], Z = P.xyz[3 * i + 2];
-            float xh, xl, yh, yl, zh, zl;
-            split_f64(X, xh, xl);
-            split_f64(Y, yh, yl);
-            split_f64(Z, zh, zl);
-            float acc = 0.0f;
+            const double X = P.xyz[3 * i], Y = P.xyz[3 * i + 1], Z = P.xyz[3 * i + 2];
+            float x1, x2, x3, y1, y2, y3, z1, z2, z3;
+            split3_f64(X, x1, x2, x3);
+            split3_f64(Y, y1, y2, y3);
+            split3_f64(Z, z1, z2, z3);
+            float rh = 0.0f, rl = 0.0f;
             for (int o = 0; o < P.n_octaves; ++o) {
-                float v = noise_raw<false>(xh, xl, yh, yl, zh, zl, P.s_hi[o], P.s_lo[o], X, Y, Z, P.s[o], lb, nfb,
-                                           nullptr, nullptr);
-                acc += fmaf(v, P.amp[o] * (1.0f / 103.0f), P.amp[o]);
+                OctP O;
+                O.s1 = P.s1[o]; O.s2 = P.s2[o]; O.s3 = P.s3[o];
+                O.amph = P.amp_hi[o]; O.ampl = P.amp_lo[o]; O.s = P.s[o];
+                float vh, vl;
+                if ((P.norm_mask >> o) & 1u)
+                    noise_pair<true>(x1, x2, x3, y1, y2, y3, z1, z2, z3, O, pow2, lb, nfb, vh, vl);
+                else
+                    noise_pair<false>(x1, x2, x3, y1, y2, y3, z1, z2, z3, O, pow2, lb, nfb, vh, vl);
+                octave_accumulate(vh, vl, O.amph, O.ampl, rh, rl);
             }
-            P.out[i] = acc;
-            mn = fminf(mn, acc);
-            mx = fmaxf(mx, acc);
+            reinterpret_cast<float2 *>(P.out)[i] = make_float2(rh, rl);
+            const unsigned long long k = pair_key(rh, rl);
+            kmn = k < kmn ? k : kmn;
+            kmx = k > kmx ? k : kmx;
         }
         if (P.minmax) {
             for (int o = 16; o > 0; o >>= 1) {
-                mn = fminf(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
-                mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+                const unsigned long long a = __shfl_xor_sync(0xFFFFFFFFu, kmn, o);
+                const unsigned long long b = __shfl_xor_sync(0xFFFFFFFFu, kmx, o);
+                kmn = a < kmn ? a : kmn;
+                kmx = b > kmx ? b : kmx;
             }
             const int w = threadIdx.x >> 5;
-            if ((threadIdx.x & 31) == 0) { s_mm[0][w] = fkey(mn); s_mm[1][w] = fkey(mx); }
+            if ((threadIdx.x & 31) == 0) { s_mm[0][w] = kmn; s_mm[1][w] = kmx; }
             __syncthreads();
             if (threadIdx.x == 0) {
-                uint32_t a0 = s_mm[0][0], a1 = s_mm[1][0];
-                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { a0 = min(a0, s_mm[0][k]); a1 = max(a1, s_mm[1][k]); }
+                unsigned long long a0 = s_mm[0][0], a1 = s_mm[1][0];
+                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+                    a0 = s_mm[0][k] < a0 ? s_mm[0][k] : a0;
+                    a1 = s_mm[1][k] > a1 ? s_mm[1][k] : a1;
+                }
                 atomicMin(&P.minmax[0], a0);
                 atomicMax(&P.minmax[1], a1);
             }
             __syncthreads();
+        }
+    }
+    if (nfb_out) {
+        unsigned tot = __reduce_add_sync(0xFFFFFFFFu, nfb);
+        if ((threadIdx.x & 31) == 0 && tot) atomicAdd(nfb_out, (unsigned long long)tot);
+    }
+}
+
+// Per-octave constants of a single-planet pair launch.
+struct FbmPairParams {
+    int n_oct;
+    int pow2;
+    uint32_t norm_mask;   // bit o: octave o renormalises its displacements
+    float s1[NX_MAX_OCTAVES], s2[NX_MAX_OCTAVES], s3[NX_MAX_OCTAVES];
+    float amph[NX_MAX_OCTAVES], ampl[NX_MAX_OCTAVES];
+    double s[NX_MAX_OCTAVES];
+};
+
+// One planet, the pair path: the octaves of P (any subset of a planet's
+// octaves: the plain path launches one per octave, accumulate = 1 after
+// the first) added to the running pair sums in out2 (float2 per vertex),
+// and/or written as binary64 (out64, = hi + lo exactly; accumulate adds to
+// it).  minmax (optional): ordered keys of the resulting pair sums.
+__global__ void __launch_bounds__(256) fbm_pair_kernel(const double *__restrict__ xyz, int64_t n,
+                                                       const int32_t *__restrict__ perm,
+                                                       const int32_t *__restrict__ pgi, FbmPairParams P,
+                                                       float2 *__restrict__ out2, double *__restrict__ out64,
+                                                       int accumulate, unsigned long long *minmax,
+                                                       unsigned long long *nfb_out)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ unsigned long long s_mm[2][8];
+    build_table_pair(smem, perm, pgi);
+    init_extra_table_pair();
+    init_grad_table();
+    __syncthreads();
+    const uint32_t lb = lane_base(smem);
+    unsigned nfb = 0;
+    unsigned long long kmn = ~0ull, kmx = 0ull;
+    const bool pow2 = P.pow2 != 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double X = xyz[3 * i], Y = xyz[3 * i + 1], Z = xyz[3 * i + 2];
+        float x1, x2, x3, y1, y2, y3, z1, z2, z3;
+        split3_f64(X, x1, x2, x3);
+        split3_f64(Y, y1, y2, y3);
+        split3_f64(Z, z1, z2, z3);
+        float rh = 0.0f, rl = 0.0f;
+        if (accumulate && out2) {
+            const float2 v = out2[i];
+            rh = v.x;
+            rl = v.y;
+        }
+        for (int o = 0; o < P.n_oct; ++o) {
+            OctP O;
+            O.s1 = P.s1[o]; O.s2 = P.s2[o]; O.s3 = P.s3[o];
+            O.amph = P.amph[o]; O.ampl = P.ampl[o]; O.s = P.s[o];
+            float vh, vl;
+            if ((P.norm_mask >> o) & 1u)
+                noise_pair<true>(x1, x2, x3, y1, y2, y3, z1, z2, z3, O, pow2, lb, nfb, vh, vl);
+            else
+                noise_pair<false>(x1, x2, x3, y1, y2, y3, z1, z2, z3, O, pow2, lb, nfb, vh, vl);
+            octave_accumulate(vh, vl, O.amph, O.ampl, rh, rl);
+        }
+        if (out2) out2[i] = make_float2(rh, rl);
+        if (out64) {
+            const double v = (double)rh + (double)rl;
+            out64[i] = (accumulate && !out2) ? out64[i] + v : v;
+        }
+        const unsigned long long k = pair_key(rh, rl);
+        kmn = k < kmn ? k : kmn;
+        kmx = k > kmx ? k : kmx;
+    }
+    if (minmax) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long a = __shfl_xor_sync(0xFFFFFFFFu, kmn, o);
+            const unsigned long long b = __shfl_xor_sync(0xFFFFFFFFu, kmx, o);
+            kmn = a < kmn ? a : kmn;
+            kmx = b > kmx ? b : kmx;
+        }
+        const int w = threadIdx.x >> 5;
+        if ((threadIdx.x & 31) == 0) { s_mm[0][w] = kmn; s_mm[1][w] = kmx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long a0 = s_mm[0][0], a1 = s_mm[1][0];
+            for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+                a0 = s_mm[0][k] < a0 ? s_mm[0][k] : a0;
+                a1 = s_mm[1][k] > a1 ? s_mm[1][k] : a1;
+            }
+            atomicMin(&minmax[0], a0);
+            atomicMax(&minmax[1], a1);
         }
     }
     if (nfb_out) {
@@ -792,6 +1343,7 @@ int configure_smem()
     NX_CHECK_CUDA(cudaFuncSetAttribute(fbm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
     NX_CHECK_CUDA(cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
     NX_CHECK_CUDA(cudaFuncSetAttribute(fbm_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
+    NX_CHECK_CUDA(cudaFuncSetAttribute(fbm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TABLE_BYTES));
     smem_configured = true;
     return NX_OK;
 }
@@ -875,20 +1427,102 @@ NX_EXPORT int nx_noise3d_trace(const double *xyz_dev, int64_t n, const int32_t *
     return NX_OK;
 }
 
+// scale as an exact triple of binary32s and whether it is a power of two
+static void split_scale(double v, float &a, float &b, float &c)
+{
+    a = (float)v;
+    const double r = v - (double)a;      // exact
+    b = (float)r;
+    c = (float)(r - (double)b);          // exact (the few bits left)
+}
+
+static bool is_pow2(double v)
+{
+    int e = 0;
+    return v > 0.0 && std::frexp(v, &e) == 0.5;
+}
+
+// Octaves whose displacements are renormalised (bit o): those with
+// |0.5 strength radius| >= ref / 8, ref = amp_ref if positive, else the
+// largest amplitude among the given octaves.
+static uint32_t norm_mask(int n_octaves, const double *strength, double radius, double amp_ref)
+{
+    double ref = amp_ref;
+    if (!(ref > 0.0))
+        for (int o = 0; o < n_octaves; ++o) ref = std::fmax(ref, std::fabs(0.5 * strength[o] * radius));
+    uint32_t m = 0;
+    for (int o = 0; o < n_octaves; ++o)
+        if (std::fabs(0.5 * strength[o] * radius) >= ref / 8.0) m |= 1u << o;
+    return m;
+}
+
+static int check_octaves(int n_octaves, const double *scale, const double *strength, const char *who)
+{
+    if (n_octaves < 0 || n_octaves > NX_MAX_OCTAVES)
+        return nx::fail(NX_EINVAL, "%s: n_octaves must be in [0, %d]", who, NX_MAX_OCTAVES);
+    if (n_octaves && (!scale || !strength)) return nx::fail(NX_EINVAL, "%s: null scale or strength", who);
+    for (int o = 0; o < n_octaves; ++o)
+        if (!std::isfinite(scale[o]) || !std::isfinite(strength[o]) || std::fabs(scale[o]) > 1e30)
+            return nx::fail(NX_EINVAL, "%s: octave %d: scale and strength must be finite", who, o);
+    return NX_OK;
+}
+
 NX_EXPORT int nx_fbm_planet_fill(nx_fbm_planet *planet, int n_octaves, const double *scale, const double *strength,
                                  double radius)
 {
-    if (!planet || n_octaves < 0 || n_octaves > NX_MAX_OCTAVES || (n_octaves && (!scale || !strength)))
-        return nx::fail(NX_EINVAL, "nx_fbm_planet_fill: bad arguments");
+    if (!planet) return nx::fail(NX_EINVAL, "nx_fbm_planet_fill: null planet");
+    int rc = check_octaves(n_octaves, scale, strength, "nx_fbm_planet_fill");
+    if (rc) return rc;
     planet->n_octaves = n_octaves;
+    bool pow2 = true;
     for (int o = 0; o < NX_MAX_OCTAVES; ++o) {
-        double sc = o < n_octaves ? scale[o] : 0.0;
-        float hi = (float)sc;
-        planet->s_hi[o] = hi;
-        planet->s_lo[o] = (float)(sc - (double)hi);
+        const double sc = o < n_octaves ? scale[o] : 0.0;
+        split_scale(sc, planet->s1[o], planet->s2[o], planet->s3[o]);
         planet->s[o] = sc;
-        planet->amp[o] = o < n_octaves ? (float)(0.5 * strength[o] * radius) : 0.0f;
+        const double amp = o < n_octaves ? 0.5 * strength[o] * radius : 0.0;
+        planet->amp_hi[o] = (float)amp;
+        planet->amp_lo[o] = (float)(amp - (double)planet->amp_hi[o]);
+        if (o < n_octaves && !is_pow2(sc)) pow2 = false;
     }
+    planet->pow2 = pow2 ? 1 : 0;
+    planet->norm_mask = norm_mask(n_octaves, strength, radius, 0.0);
+    return NX_OK;
+}
+
+NX_EXPORT int nx_fbm_pair(const double *xyz_dev, int64_t n, const int32_t *perm_dev, const int32_t *pgi_dev,
+                          int n_octaves, const double *scale, const double *strength, double radius, double amp_ref,
+                          float *pair_dev, double *elev_f64_dev, int accumulate, unsigned long long *minmax_dev,
+                          unsigned long long *n_fallback_dev, void *stream)
+{
+    if (n < 0) return nx::fail(NX_EINVAL, "nx_fbm_pair: n < 0");
+    int rc = check_octaves(n_octaves, scale, strength, "nx_fbm_pair");
+    if (rc) return rc;
+    if (n == 0) return NX_OK;
+    if (!xyz_dev || !perm_dev || !pgi_dev) return nx::fail(NX_EINVAL, "nx_fbm_pair: null pointer");
+    if (!pair_dev && !elev_f64_dev) return nx::fail(NX_EINVAL, "nx_fbm_pair: no output");
+    if (pair_dev && ((uintptr_t)pair_dev & 7u)) return nx::fail(NX_EINVAL, "nx_fbm_pair: pair output must be 8-byte aligned");
+    FbmPairParams P;
+    P.n_oct = n_octaves;
+    bool pow2 = true;
+    for (int o = 0; o < NX_MAX_OCTAVES; ++o) {
+        const double sc = o < n_octaves ? scale[o] : 0.0;
+        split_scale(sc, P.s1[o], P.s2[o], P.s3[o]);
+        P.s[o] = sc;
+        const double amp = o < n_octaves ? 0.5 * strength[o] * radius : 0.0;
+        P.amph[o] = (float)amp;
+        P.ampl[o] = (float)(amp - (double)P.amph[o]);
+        if (o < n_octaves && !is_pow2(sc)) pow2 = false;
+    }
+    P.pow2 = pow2 ? 1 : 0;
+    P.norm_mask = norm_mask(n_octaves, strength, radius, amp_ref);
+    rc = configure_smem();
+    if (rc) return rc;
+    int grid = grid_for(n, 256, (const void *)fbm_pair_kernel, TABLE_BYTES);
+    fbm_pair_kernel<<<grid, 256, TABLE_BYTES, (cudaStream_t)stream>>>(xyz_dev, n, perm_dev, pgi_dev, P,
+                                                                      (float2 *)pair_dev, elev_f64_dev, accumulate,
+                                                                      minmax_dev, n_fallback_dev);
+    NX_CHECK_LAUNCH("fbm_pair_kernel");
+    nx::note_launch(1);
     return NX_OK;
 }
 
@@ -902,6 +1536,7 @@ NX_EXPORT int nx_fbm_batch(const nx_fbm_planet *planets_dev, const nx_fbm_planet
         const nx_fbm_planet &P = planets_host[p];
         if (P.n < 0 || (P.n > 0 && (!P.xyz || !P.perm || !P.pgi || !P.out)))
             return nx::fail(NX_EINVAL, "nx_fbm_batch: planet %d incomplete", p);
+        if ((uintptr_t)P.out & 7u) return nx::fail(NX_EINVAL, "nx_fbm_batch: planet %d: out must be 8-byte aligned", p);
         if (P.n_octaves < 0 || P.n_octaves > NX_MAX_OCTAVES) return nx::fail(NX_EINVAL, "nx_fbm_batch: octaves");
         if (P.chunk0 != total)
             return nx::fail(NX_EINVAL, "nx_fbm_batch: planet %d chunk0 must be %d (chunks of %d vertices)", p, total,

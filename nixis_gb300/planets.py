@@ -5,15 +5,19 @@ Two execution paths over the same kernels:
 * ``PlanetBatch`` -- many planets of uneven size in a handful of launches:
   one persistent fBm launch over all planets (with fused per-planet
   min/max), one launch for the rescale to metres and the initial erosion
-  state, one erosion launch per iteration over the planets still running,
-  one height-extraction launch and one insolation launch per sun schedule.
-  The whole sequence can be captured once as a CUDA graph and replayed.
+  state, one erosion launch per pass (or iteration) over the planets still
+  running, one height-extraction launch and one insolation launch per sun
+  schedule.  The whole sequence can be captured once as a CUDA graph and
+  replayed.
 * ``generate_plain`` -- the plain per-planet GPU path: one planet at a time,
   one launch per octave and per erosion iteration, synchronised per planet.
 
-A planet is fully determined by its request (seed, divisions, octaves,
-iterations, ...), so results are reproducible and a planet gives the same
-bits alone or in any batch.
+The fBm runs in pair precision (nx_fbm_pair), the rescale to metres and
+the erosion state in binary32 pairs, and heights come back in binary64:
+erosion follows binary64's flow choices only from starting heights that
+close to the reference's.  A planet is fully determined by its request
+(seed, divisions, octaves, iterations, ...), so results are reproducible
+and a planet gives the same bits alone or in any batch.
 """
 import ctypes
 import math
@@ -70,9 +74,10 @@ class PlanetRequest:
         return (self.axial_tilt, self.days, self.hours)
 
     def state_bytes(self):
-        """Device bytes a planet needs beyond its mesh (batched path)."""
+        """Device bytes a planet needs beyond its mesh (batched path): raw
+        pair sums, two state rows, binary64 heights, insolation."""
         n = self.n_vertices + ALIGN
-        return n * (4 + 16 + 16 + 4 + (4 if self.insolation else 0))
+        return n * (8 + 32 + 32 + 8 + (4 if self.insolation else 0))
 
 
 def _tiling_shape(divisions, tb):
@@ -101,8 +106,8 @@ def mesh_bytes(divisions, tb=None):
 @dataclass
 class PlanetResult:
     request: PlanetRequest
-    heights: torch.Tensor               # float32 (N,), metres (+-inf beyond binary32's range: the
-                                        # reference's erosion grows without bound over long runs)
+    heights: torch.Tensor               # float64 (N,), metres (finite for every iteration count; the
+                                        # reference's erosion grows heights without bound)
     insolation: torch.Tensor = None     # float32 (N,), mean TOA W/m^2 over the schedule
     scale_exponent: int = 0
 
@@ -142,10 +147,10 @@ class PlanetBatch:
         self.total = off
         N = off
         dev = "cuda"
-        self.raw = torch.empty(N, dtype=torch.float32, device=dev)
+        self.raw = torch.empty((N, 2), dtype=torch.float32, device=dev)     # (hi, lo) pair sums
         self.st = torch.empty((N, 8), dtype=torch.float32, device=dev)
         self.st_tmp = torch.empty((N, 8), dtype=torch.float32, device=dev)
-        self.heights = torch.empty(N, dtype=torch.float32, device=dev)
+        self.heights = torch.empty(N, dtype=torch.float64, device=dev)
         self.any_inso = any(r.insolation for r in requests)
         self.inso = torch.empty(N, dtype=torch.float32, device=dev) if self.any_inso else None
         # per-planet tables (host init, bit-exact) and min/max keys
@@ -153,9 +158,9 @@ class PlanetBatch:
         for j, i in enumerate(self.order):
             tabs[j, 0], tabs[j, 1] = _osx.init(requests[i].seed)
         self.tables = torch.from_numpy(tabs).cuda()
-        mm0 = np.zeros((np_, 2), np.uint32)
-        mm0[:, 0] = 0xFFFFFFFF
-        self.minmax0 = torch.from_numpy(mm0.view(np.int32)).cuda()
+        mm0 = np.zeros((np_, 2), np.uint64)
+        mm0[:, 0] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        self.minmax0 = torch.from_numpy(mm0.view(np.int64)).cuda()       # ordered 64-bit keys
         self.minmax = self.minmax0.clone()
         # descriptors (in packed order)
         chunk = int(lib().nx_fbm_chunk_size())
@@ -172,7 +177,7 @@ class PlanetBatch:
             f.n = m.n
             f.perm = self.tables[j, 0].data_ptr()
             f.pgi = self.tables[j, 1].data_ptr()
-            f.out = self.raw.data_ptr() + 4 * self.vbeg[i]
+            f.out = self.raw.data_ptr() + 8 * self.vbeg[i]
             f.minmax = self.minmax[j].data_ptr()
             f.chunk0 = c0
             c0 += (m.n + chunk - 1) // chunk
@@ -236,8 +241,8 @@ class PlanetBatch:
         self.minmax.copy_(self.minmax0)
         call("nx_fbm_batch", _dev.ptr(self.fb_dev), ctypes.cast(self.fb_host, ctypes.c_void_p), np_, None, s)
         call("nx_erosion_init_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
-             _dev.ptr(self.raw), _dev.ptr(self.minmax), ctypes.c_float(self.requests[0].elev_lo),
-             ctypes.c_float(self.requests[0].elev_hi), ctypes.c_double(self.requests[0].water0), _dev.ptr(self.st),
+             _dev.ptr(self.raw), _dev.ptr(self.minmax), float(self.requests[0].elev_lo),
+             float(self.requests[0].elev_hi), float(self.requests[0].water0), _dev.ptr(self.st),
              _dev.ptr(self.st_tmp), s)
         call("nx_erosion_ctl_init", _dev.ptr(self.ws), self.ws.numel(), np_, s)
         if self.blocked:
@@ -268,15 +273,15 @@ class PlanetBatch:
 
     def run_to_host(self, host_out):
         """One run whose heights are copied into host_out (page-locked
-        float32, at least `total` elements, packed rows as `heights`),
+        float64, at least `total` elements, packed rows as `heights`),
         pipelined for back-to-back calls: the heights alternate between two
         device buffers, the copy of a run's heights goes on a side stream
         while the next call's run proceeds, and a run waits only for the
         copy that last read the buffer it writes.  `wait_host()` blocks until
         the last copy is in host_out.  The first call captures the two CUDA
         graphs (one per buffer; an eager run and a synchronisation each)."""
-        if not host_out.is_pinned() or host_out.dtype != torch.float32 or host_out.numel() < self.total:
-            raise ValueError("host_out must be a page-locked float32 tensor of at least `total` elements")
+        if not host_out.is_pinned() or host_out.dtype != torch.float64 or host_out.numel() < self.total:
+            raise ValueError("host_out must be a page-locked float64 tensor of at least `total` elements")
         if getattr(self, "_pipe", None) is None:
             bufs = [self.heights, self.heights.clone()]      # same padding rows in both
             graphs = []
@@ -365,23 +370,29 @@ class _PlainWork:
 
     def ensure(self, n):
         if n > self.n:
-            self.raw = torch.empty(n, dtype=torch.float32, device="cuda")
+            self.raw = torch.empty((n, 2), dtype=torch.float32, device="cuda")
             self.hm = torch.empty(n, dtype=torch.float64, device="cuda")
             self.st = torch.empty((n, 8), dtype=torch.float32, device="cuda")
             self.st_tmp = torch.empty((n, 8), dtype=torch.float32, device="cuda")
-            self.inso = torch.empty(n, dtype=torch.float32, device="cuda")
             self.ws = torch.zeros(int(lib().nx_erosion_workspace_size(n, 1)), dtype=torch.uint8, device="cuda")
             self.planet = torch.zeros(ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device="cuda")
             self.perm = torch.empty(256, dtype=torch.int32, device="cuda")
             self.pgi = torch.empty(256, dtype=torch.int32, device="cuda")
             self.n = n
+        if not hasattr(self, "minmax"):
+            self.minmax = torch.empty(2, dtype=torch.int64, device="cuda")
+            self.init_desc = torch.zeros(ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device="cuda")
 
 
 _plain = _PlainWork()
 
+# ordered keys of the pair (0, 0): a planet with no octaves
+_ZERO_KEY = (0x80000000 << 32) | 0x80000000
+
 
 def generate_plain(request, meshes=None, sync=True, out=None):
-    """One planet: a launch per octave, per erosion iteration; synchronised."""
+    """One planet: a launch per octave, per erosion iteration; synchronised.
+    Same arithmetic as the batched path, so the same bits."""
     r = request
     meshes = meshes if meshes is not None else _mesh.MeshCache()
     m = meshes.get(r.divisions)
@@ -393,26 +404,31 @@ def generate_plain(request, meshes=None, sync=True, out=None):
     w.perm.copy_(torch.from_numpy(perm))
     w.pgi.copy_(torch.from_numpy(pgi))
     scale, strength = r.octave_args()
+    w.minmax.copy_(torch.tensor([-1, 0], dtype=torch.int64))          # {~0, 0}
+    # the precision choice per octave follows the planet's largest amplitude, as in the batch
+    amp_ref = max([abs(0.5 * a * r.radius) for a in strength], default=0.0)
     for o in range(r.octaves):
         sc = (ctypes.c_double * 1)(scale[o])
         st = (ctypes.c_double * 1)(strength[o])
-        call("nx_fbm", _dev.ptr(m.xyz), n, _dev.ptr(w.perm), _dev.ptr(w.pgi), 1, sc, st, float(r.radius), None,
-             _dev.ptr(w.raw), 1 if o > 0 else 0, None, s)
+        last = o == r.octaves - 1
+        call("nx_fbm_pair", _dev.ptr(m.xyz), n, _dev.ptr(w.perm), _dev.ptr(w.pgi), 1, sc, st, float(r.radius),
+             amp_ref, _dev.ptr(w.raw), None, 1 if o > 0 else 0, _dev.ptr(w.minmax) if last else None, None, s)
     if r.octaves == 0:
         w.raw[:n].zero_()
-    raw = w.raw[:n]
-    mn, mx = torch.aminmax(raw)
-    rng_ = mx - mn
-    sc = torch.tensor(r.elev_hi - r.elev_lo, dtype=torch.float32, device="cuda") / rng_
-    h = (raw - mn) * sc + torch.tensor(r.elev_lo, dtype=torch.float32, device="cuda")
-    hd = w.hm[:n]
-    hd.copy_(h)
-    wat = torch.full((n,), r.water0, dtype=torch.float64, device="cuda")
-    call("nx_erosion_load", _dev.ptr(hd), _dev.ptr(wat), None, n, _dev.ptr(w.st), _dev.ptr(w.ws), w.ws.numel(), s)
+        k = _ZERO_KEY - (1 << 64)
+        w.minmax.copy_(torch.tensor([k, k], dtype=torch.int64))
+    # the rescale to metres and the initial state (buffer 0): the batch's kernel on one planet
+    d = ErosionPlanet()
+    d.vbeg, d.n, d.nbr, d.edge, d.iters, d.slot = 0, n, m.nbr.data_ptr(), m.edge.data_ptr(), 0, 0
+    w.init_desc.copy_(torch.frombuffer(bytearray(bytes(d)), dtype=torch.uint8))
+    call("nx_erosion_init_batch", _dev.ptr(w.init_desc), ctypes.byref(d), 1, _dev.ptr(w.raw), _dev.ptr(w.minmax),
+         float(r.elev_lo), float(r.elev_hi), float(r.water0), _dev.ptr(w.st), _dev.ptr(w.st_tmp), s)
+    call("nx_erosion_ctl_init", _dev.ptr(w.ws), w.ws.numel(), 1, s)
     call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(w.st), _dev.ptr(w.st_tmp),
          r.erosion_iters, ctypes.c_float(r.rain), _dev.ptr(w.planet), None, None, _dev.ptr(w.ws), w.ws.numel(), s)
+    hd = w.hm[:n] if out is None else out
     call("nx_erosion_store", _dev.ptr(w.st), n, _dev.ptr(w.ws), _dev.ptr(hd), None, None, s)
-    heights = hd.float() if out is None else out.copy_(hd)
+    heights = hd.clone() if out is None else hd
     ins = None
     if r.insolation:
         rot, tilts = _climate.annual_schedule(r.axial_tilt, r.days, r.days, r.hours)

@@ -48,7 +48,7 @@ from . import planets as _planets
 from ._lib import ErosionPlanet, FbmPlanet, call, lib
 
 ALIGN = 256
-ROW_BYTES = 32 + 32 + 4 + 4 + 4
+ROW_BYTES = 32 + 32 + 8 + 8 + 4      # state x2, raw pair sum, binary64 height, insolation
 COPY_THREADS = 4           # host threads that move one result array
 COPY_SPLIT = 1 << 20       # elements from which a result array is copied in slices
 HOST_PAGE = 4096           # unit of the page-locked result arena
@@ -103,9 +103,10 @@ class PinnedArena:
                     if self.pages.capacity else None)
         self.lock = threading.Lock()
 
-    def alloc_f32(self, n):
-        """(float32 tensor of n elements, release token), or None when full."""
-        need = (4 * n + HOST_PAGE - 1) // HOST_PAGE
+    def alloc(self, n, dtype):
+        """(tensor of n elements of dtype, release token), or None when full."""
+        size = torch.empty(0, dtype=dtype).element_size()
+        need = (size * n + HOST_PAGE - 1) // HOST_PAGE
         if self.buf is None or need == 0:
             return None
         with self.lock:
@@ -113,7 +114,7 @@ class PinnedArena:
         if start is None:
             return None
         b = start * HOST_PAGE
-        return self.buf[b:b + 4 * n].view(torch.float32), (start, need)
+        return self.buf[b:b + size * n].view(dtype), (start, need)
 
     def release(self, token):
         with self.lock:
@@ -250,8 +251,8 @@ class ServeEngine:
         dev = "cuda"
         self.st = torch.empty((R, 8), dtype=torch.float32, device=dev)
         self.st_tmp = torch.empty((R, 8), dtype=torch.float32, device=dev)
-        self.raw = torch.empty(R, dtype=torch.float32, device=dev)
-        self.heights = torch.empty(R, dtype=torch.float32, device=dev)
+        self.raw = torch.empty((R, 2), dtype=torch.float32, device=dev)     # (hi, lo) fBm pair sums
+        self.heights = torch.empty(R, dtype=torch.float64, device=dev)
         self.inso = torch.empty(R, dtype=torch.float32, device=dev)
         self.nslots = slots
         # block map and partials for R rows, or for the tiles of the planets
@@ -353,9 +354,9 @@ class ServeEngine:
             tabs[j, 0], tabs[j, 1] = _osx.init(t.request.seed)
         with torch.cuda.stream(fs):
             tab_dev = _pinned(tabs).to("cuda", non_blocking=True)
-            mm = torch.tensor([[-1, 0]] * n, dtype=torch.int64).to(torch.int32)
-            mm[:, 0] = -1
-            mm_dev = _pinned(mm.numpy()).to("cuda", non_blocking=True)
+            mm = np.zeros((n, 2), np.int64)
+            mm[:, 0] = -1                        # ordered 64-bit keys: min starts at ~0, max at 0
+            mm_dev = _pinned(mm).to("cuda", non_blocking=True)
             for j, t in enumerate(new):
                 r = t.request
                 f = fb[j]
@@ -363,7 +364,7 @@ class ServeEngine:
                 f.n = t.mesh.n
                 f.perm = tab_dev[j, 0].data_ptr()
                 f.pgi = tab_dev[j, 1].data_ptr()
-                f.out = self.raw.data_ptr() + 4 * t.vbeg
+                f.out = self.raw.data_ptr() + 8 * t.vbeg
                 f.minmax = mm_dev[j].data_ptr()
                 f.chunk0 = c0
                 c0 += (t.mesh.n + self.chunk - 1) // self.chunk
@@ -386,8 +387,8 @@ class ServeEngine:
                 e[0].slot = t.slot
                 e_dev = _descs_tensor(e).to("cuda", non_blocking=True)
                 call("nx_erosion_init_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
-                     ctypes.c_void_p(self.raw.data_ptr() + 4 * t.vbeg), _dev.ptr(mm_dev[j]),
-                     ctypes.c_float(r.elev_lo), ctypes.c_float(r.elev_hi), ctypes.c_double(r.water0),
+                     ctypes.c_void_p(self.raw.data_ptr() + 8 * t.vbeg), _dev.ptr(mm_dev[j]),
+                     float(r.elev_lo), float(r.elev_hi), float(r.water0),
                      ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg),
                      ctypes.c_void_p(self.st_tmp.data_ptr() + 32 * t.vbeg), s)
                 t._e_single = (e, e_dev)
@@ -422,12 +423,12 @@ class ServeEngine:
             ev.record(self.inso_stream)
         t.inso_event = ev
 
-    def _host_buffer(self, t, n):
-        """A page-locked float32 buffer of n elements for t's results: from
-        the arena, else from torch's caching host allocator."""
-        got = self.host.alloc_f32(n)
+    def _host_buffer(self, t, n, dtype=torch.float32):
+        """A page-locked buffer of n elements for t's results: from the
+        arena, else from torch's caching host allocator."""
+        got = self.host.alloc(n, dtype)
         if got is None:
-            return torch.empty(n, dtype=torch.float32, pin_memory=True)
+            return torch.empty(n, dtype=dtype, pin_memory=True)
         buf, token = got
         t.host_tokens.append(token)
         return buf
@@ -446,13 +447,13 @@ class ServeEngine:
                 call("nx_erosion_finish_passes" if self.blocked else "nx_erosion_finish", _dev.ptr(e_dev), 1, ws, s)
             call("nx_erosion_heights_batch", _dev.ptr(e_dev), ctypes.cast(e, ctypes.c_void_p), 1,
                  ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg), ws,
-                 ctypes.c_void_p(self.heights.data_ptr() + 4 * t.vbeg), s)
+                 ctypes.c_void_p(self.heights.data_ptr() + 8 * t.vbeg), s)
         ev = torch.cuda.Event()
         ev.record(stream)
         cs = self.copy_stream
         cs.wait_event(ev)
         n = t.mesh.n
-        t.host_h = self._host_buffer(t, n)
+        t.host_h = self._host_buffer(t, n, torch.float64)
         t.host_i = self._host_buffer(t, n) if r.insolation else None
         with torch.cuda.stream(cs):
             t.host_h.copy_(self.heights[t.vbeg:t.vbeg + n], non_blocking=True)

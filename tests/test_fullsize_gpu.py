@@ -84,13 +84,20 @@ def test_c3_full_size_properties():
         bt = planets.PlanetBatch([req], cache, blocked=blocked)
         bt.run()
         torch.cuda.synchronize()
-        out.append(bt.results()[0].heights.clone())
-        del bt
-    # (binary32 metres: the reference's erosion grows without bound over
-    # long runs, and past ~130 iterations here some heights leave binary32's
-    # range in both paths alike; the binary64 output below stays finite)
+        res = bt.results()[0]
+        out.append(res.heights.clone())
+        K = res.scale_exponent
+        del bt, res
     assert torch.equal(out[0], out[1])
-    del out
+    # binary64 metres through the planet API: finite, although the run
+    # passes binary32's range (the state carries a power-of-two exponent),
+    # and equal to the plain path's heights, which come from the erosion
+    # state's binary64 store (nx_erosion_store, as ErosionRun.store)
+    assert K > 0 and out[0].dtype == torch.float64 and torch.isfinite(out[0]).all()
+    assert float(out[0].abs().max()) > 3.4e38
+    plain = planets.generate_plain(req, cache)
+    assert torch.equal(plain.heights, out[0])
+    del out, plain
     # sum(h + s) is invariant under the update (compensated per-iteration sums)
     hm = torch.from_numpy(O.rescale(hg, -8000.0, 8000.0)).cuda()
     run = erosion.ErosionRun(m.xyz, m.nbr, m.edge)

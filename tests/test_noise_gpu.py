@@ -148,3 +148,72 @@ def test_fbm_float32_output_and_accumulate():
     terrain.fbm(u, perm, pgi, scale, strength, 1.0, out=out32, accumulate=True)
     ref = O.sample_octaves(u, base.double().cpu().numpy(), perm, pgi, 6, 1.0, 1.0, 2.0, 0.5, 1.0)
     assert np.abs(out32.double().cpu().numpy() - ref).max() <= 2e-6 * (ref.max() - ref.min())
+
+
+# Pair-precision fBm (the planet paths): |err| of the raw sum against the
+# binary64 reference, relative to the field's range.  Measured ~1e-14; the
+# erosion needs starting heights within ~1e-11 of binary64's to keep its
+# flow choices (random raw errors of 1e-10 flipped some on 900,002 vertices).
+PAIR_TOL = 2e-13
+
+
+def _fbm_pair(pts, perm, pgi, scale, strength, radius, per_octave=False, f64=False):
+    import ctypes
+    from nixis_gb300 import _dev, _lib
+    xyz = torch.from_numpy(np.ascontiguousarray(pts, np.float64)).cuda()
+    n = len(pts)
+    p = torch.from_numpy(perm).cuda()
+    g = torch.from_numpy(pgi).cuda()
+    pair = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+    mm = torch.tensor([-1, 0], dtype=torch.int64, device="cuda")
+    out64 = torch.zeros(n, dtype=torch.float64, device="cuda") if f64 else None
+    groups = [[o] for o in range(len(scale))] if per_octave else [list(range(len(scale)))]
+    for q, grp in enumerate(groups):
+        sc = (ctypes.c_double * len(grp))(*[scale[o] for o in grp])
+        st = (ctypes.c_double * len(grp))(*[strength[o] for o in grp])
+        last = q == len(groups) - 1
+        _lib.call("nx_fbm_pair", _dev.ptr(xyz), n, _dev.ptr(p), _dev.ptr(g), len(grp), sc, st, float(radius),
+                  max(abs(0.5 * a * radius) for a in strength), _dev.ptr(pair), _dev.ptr(out64) if (f64 and last) else None, 1 if q > 0 else 0,
+                  _dev.ptr(mm) if last else None, None, _dev.stream_handle())
+    torch.cuda.synchronize()
+    return pair.cpu().numpy(), mm.cpu().numpy().view(np.uint64), (out64.cpu().numpy() if f64 else None)
+
+
+def _unkey(k):
+    k = np.uint32(k)
+    b = (k ^ np.uint32(0x80000000)) if (k & np.uint32(0x80000000)) else ~k
+    return np.array([b], np.uint32).view(np.float32)[0]
+
+
+@pytest.mark.parametrize("case", ["unit_pow2", "driver_radius"])
+def test_fbm_pair_against_binary64(case):
+    """The planet paths' fBm: within PAIR_TOL of the reference's binary64
+    sums on a 12-octave field (power-of-two scales: base frequency 1,
+    lacunarity 2, radius 1; and the reference driver's 1.5/6378100-style
+    scales, which take the general coordinate product); one launch over all
+    octaves equals one launch per octave bit for bit; the binary64 output is
+    hi + lo; min/max keys are those of the extreme pair sums."""
+    from nixis_gb300 import terrain
+    rng = np.random.default_rng(5)
+    u = rng.normal(size=(300_000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    if case == "unit_pow2":
+        R, args = 1.0, (12, 1.0, 1.0, 2.0, 0.5, 1.0)
+        pts = u
+    else:
+        R = 6378100.0
+        args = (12, 1.5, 0.4, 2.0, 0.5, R)
+        pts = u * R
+    perm, pgi = O.init(17)
+    scale, strength = terrain._octave_args(*args)
+    ref = O.sample_octaves(pts, None, perm, pgi, *args)
+    one, mm, o64 = _fbm_pair(pts, perm, pgi, scale, strength, R, f64=True)
+    each, _, _ = _fbm_pair(pts, perm, pgi, scale, strength, R, per_octave=True)
+    assert np.array_equal(one, each)
+    got = one[:, 0].astype(np.float64) + one[:, 1].astype(np.float64)
+    assert np.array_equal(o64, got)
+    err = np.abs(got - ref).max() / (ref.max() - ref.min())
+    assert err <= PAIR_TOL, err
+    lo = float(_unkey(mm[0] >> np.uint64(32))) + float(_unkey(mm[0] & np.uint64(0xFFFFFFFF)))
+    hi = float(_unkey(mm[1] >> np.uint64(32))) + float(_unkey(mm[1] & np.uint64(0xFFFFFFFF)))
+    assert lo == got.min() and hi == got.max()

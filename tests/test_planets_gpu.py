@@ -56,7 +56,7 @@ def test_run_to_host_pipelines_copies_of_every_run():
     b.run()
     torch.cuda.synchronize()
     want = b.heights.cpu().numpy().copy()
-    host = torch.empty(b.total, dtype=torch.float32).pin_memory()
+    host = torch.empty(b.total, dtype=torch.float64).pin_memory()
     rows = np.concatenate([np.arange(b.vbeg[i], b.vbeg[i] + r.n_vertices) for i, r in enumerate(reqs)])
     for _ in range(3):
         host.zero_()
@@ -72,7 +72,58 @@ def test_run_to_host_pipelines_copies_of_every_run():
     for r, got in zip(reqs, b.results()):
         assert torch.equal(got.heights, planets.generate_plain(r, cache).heights), r
     with pytest.raises(ValueError):
-        b.run_to_host(torch.empty(b.total, dtype=torch.float32))       # not page-locked
+        b.run_to_host(torch.empty(b.total, dtype=torch.float64))       # not page-locked
+
+
+def c4_requests():
+    """The 64-planet workload: divisions, octaves, iterations drawn with
+    default_rng(7) in that order, seeds 0..63."""
+    from nixis_gb300.planets import PlanetRequest
+    rng = np.random.default_rng(7)
+    d, o, it = rng.integers(100, 801, 64), rng.integers(4, 13, 64), rng.integers(0, 101, 64)
+    return [PlanetRequest(seed=i, divisions=int(d[i]), octaves=int(o[i]), erosion_iters=int(it[i]))
+            for i in range(64)]
+
+
+# max |h - h64| / max |h64| of the heights after the run: the metric's bar
+ELEV_TOL = 1e-5
+
+
+def _oracle_planet(m, r):
+    pts = m.xyz.cpu().numpy()
+    adj = m.nbr.cpu().numpy()
+    perm, pgi = O.init(r.seed)
+    e = O.sample_octaves(pts, None, perm, pgi, r.octaves, 1.0, 1.0, 2.0, 0.5, 1.0)
+    h = O.rescale(e, -8000.0, 8000.0)
+    w = np.full(len(pts), 1e-3)
+    s = np.zeros(len(pts))
+    for _ in range(r.erosion_iters):
+        O.erosion_iteration3(pts, adj, h, w, s)
+    return h
+
+
+def test_batched_planets_from_the_workload_against_binary64():
+    """Whole planets through the batched path -- pair fBm, rescale to
+    +-8000 m, erosion, binary64 heights -- against the binary64 oracle
+    (noise, util.rescale, erosion_iteration3 in the reference's operation
+    order) at the metric's bar: planets 22 (divisions 339, 12 octaves, 85
+    iterations), 9 (310, 7, 97) and 0 (762, 12, 56) of the 64-planet
+    workload, run as one batch."""
+    from nixis_gb300 import mesh, planets
+    reqs = c4_requests()
+    pick = [c4_requests()[i] for i in (22, 9, 0)]
+    assert (pick[0].octaves, pick[1].erosion_iters >= 90, pick[2].divisions >= 300) == (12, True, True)
+    cache = mesh.MeshCache()
+    b = planets.PlanetBatch(pick, cache)
+    b.run()
+    torch.cuda.synchronize()
+    for r, got in zip(pick, b.results()):
+        assert got.heights.dtype == torch.float64
+        h = _oracle_planet(cache.get(r.divisions), r)
+        g = got.heights.cpu().numpy()
+        err = np.abs(g - h).max() / np.abs(h).max()
+        assert err <= ELEV_TOL, (r, err)
+    del reqs
 
 
 def test_pipeline_against_binary64_oracle():
@@ -82,16 +133,9 @@ def test_pipeline_against_binary64_oracle():
     got = planets.generate_batched([r], cache)[0]
     m = cache.get(40)
     pts = m.xyz.cpu().numpy()
-    adj = m.nbr.cpu().numpy()
-    perm, pgi = O.init(5)
-    e = O.sample_octaves(pts, None, perm, pgi, 12, 1.0, 1.0, 2.0, 0.5, 1.0)
-    h = O.rescale(e, -8000.0, 8000.0)
-    w = np.full(len(pts), 1e-3)
-    s = np.zeros(len(pts))
-    for _ in range(30):
-        O.erosion_iteration3(pts, adj, h, w, s)
-    g = got.heights.double().cpu().numpy()
-    assert np.abs(g - h).max() / np.abs(h).max() <= 3e-5
+    h = _oracle_planet(m, r)
+    g = got.heights.cpu().numpy()
+    assert np.abs(g - h).max() / np.abs(h).max() <= ELEV_TOL
     ins = O.annual_insolation(pts, 1.0, axial_tilt=23.44, year_length=30, days=30, hours=24) * 1361.0 / (30 * 24)
     gi = got.insolation.double().cpu().numpy()
     assert np.abs(gi - ins).max() / np.abs(ins).max() <= 1e-5

@@ -63,13 +63,14 @@ def test_admission_waits_for_memory_and_still_matches():
 def test_pinned_arena_hands_out_and_takes_back_ranges():
     from nixis_gb300 import serve
     a = serve.PinnedArena(8 << 20)                 # 8 MB in 1 MB units
-    b1, t1 = a.alloc_f32(1 << 20)                  # 4 MB
-    b2, t2 = a.alloc_f32(1 << 20)
+    b1, t1 = a.alloc(1 << 20, torch.float32)       # 4 MB
+    b2, t2 = a.alloc(1 << 19, torch.float64)       # 4 MB
     assert b1.is_pinned() and b1.dtype == torch.float32 and b1.numel() == 1 << 20
+    assert b2.dtype == torch.float64 and b2.numel() == 1 << 19
     assert b2.data_ptr() == b1.data_ptr() + (4 << 20)
-    assert a.alloc_f32(10) is None                 # full
+    assert a.alloc(10, torch.float32) is None      # full
     a.release(t1)
-    b3, t3 = a.alloc_f32(100)
+    b3, t3 = a.alloc(100, torch.float32)
     assert b3.data_ptr() == b1.data_ptr()
     a.release(t2)
     a.release(t3)
