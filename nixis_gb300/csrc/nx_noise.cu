@@ -95,13 +95,20 @@ __device__ __forceinline__ void build_table_pair(uint32_t *T, const int32_t *__r
     }
 }
 
-// GRADIENTS_3D as binary32 (x, y, z, 0), filled per block.
+// GRADIENTS_3D as binary32 (x, y, z, 0), and as sign masks (bit 31 of each
+// component) with the axis of the +-11 component (every gradient has one
+// +-11 and two +-4 components), filled per block.
 __shared__ float4 s_grad[24];
+__shared__ uint4 s_gsign[24];
 
 __device__ __forceinline__ void init_grad_table()
 {
-    for (int i = threadIdx.x; i < 24; i += blockDim.x)
-        s_grad[i] = make_float4((float)c_grad3[3 * i], (float)c_grad3[3 * i + 1], (float)c_grad3[3 * i + 2], 0.0f);
+    for (int i = threadIdx.x; i < 24; i += blockDim.x) {
+        const int gx = c_grad3[3 * i], gy = c_grad3[3 * i + 1], gz = c_grad3[3 * i + 2];
+        s_grad[i] = make_float4((float)gx, (float)gy, (float)gz, 0.0f);
+        const uint32_t a = (gx == 11 || gx == -11) ? 0u : ((gy == 11 || gy == -11) ? 1u : 2u);
+        s_gsign[i] = make_uint4(gx < 0 ? 0x80000000u : 0u, gy < 0 ? 0x80000000u : 0u, gz < 0 ? 0x80000000u : 0u, a);
+    }
 }
 
 // Hash table load: bits 7-14 of a select the entry; lb = this lane's byte
@@ -838,17 +845,37 @@ __device__ __forceinline__ void contrib2_pair(uint32_t wa, uint32_t wb, float X0
     const float2 h4 = mul2(h2, h2);
     float2 l4 = fma2(h2, h2, f2(-h4.x, -h4.y));
     l4 = fma2(add2(h2, h2), l2, l4);
-    // grad . d
+    // grad . d as a pair (dh, dl), times DSC (see below)
     const float4 ga = s_grad[wa & 31u], gb = s_grad[wb & 31u];
     const float2 gx = f2(ga.x, gb.x), gy = f2(ga.y, gb.y), gz = f2(ga.z, gb.z);
-    const float2 qx = mul2(gx, Xh), qy = mul2(gy, Yh), qz = mul2(gz, Zh);
-    const float2 qxe = fma2(gx, Xh, f2(-qx.x, -qx.y)), qye = fma2(gy, Yh, f2(-qy.x, -qy.y)),
-                 qze = fma2(gz, Zh, f2(-qz.x, -qz.y));
-    float2 s1, t1, dh, t2;
-    two_sum2(qx, qy, s1, t1);
-    two_sum2(s1, qz, dh, t2);
-    const float2 gl = fma2(gx, X2, fma2(gy, Y2, mul2(gz, Z2)));     // 2 (grad . lo)
-    const float2 dl = fma2(f2(0.5f, 0.5f), gl, add2(add2(add2(qxe, qye), qze), add2(t1, t2)));
+    float2 dh, dl;
+    if (NORM) {
+        // products exact as q + qe, summed with two-sums; DSC = 1
+        const float2 qx = mul2(gx, Xh), qy = mul2(gy, Yh), qz = mul2(gz, Zh);
+        const float2 qxe = fma2(gx, Xh, f2(-qx.x, -qx.y)), qye = fma2(gy, Yh, f2(-qy.x, -qy.y)),
+                     qze = fma2(gz, Zh, f2(-qz.x, -qz.y));
+        float2 s1, t1, t2;
+        two_sum2(qx, qy, s1, t1);
+        two_sum2(s1, qz, dh, t2);
+        const float2 gl = fma2(gx, X2, fma2(gy, Y2, mul2(gz, Z2)));     // 2 (grad . lo)
+        dl = fma2(f2(0.5f, 0.5f), gl, add2(add2(add2(qxe, qye), qze), add2(t1, t2)));
+    } else {
+        // hi parts on the 2^-21 grid (|d| < sqrt 2 wherever attn > 0): with
+        // g_i = s_i (4 + 7 [i == a]), grad . hi = 4 (U + V) exactly, U =
+        // sum s_i hi_i + 2 s_a hi_a (|U| < 8 on the grid: exact), V =
+        // -s_a hi_a / 4; the lo parts' product in binary32.  DSC = 1/4.
+        const uint4 sa = s_gsign[wa & 31u], sb = s_gsign[wb & 31u];
+        const float2 sx = f2(__uint_as_float(__float_as_uint(Xh.x) ^ sa.x), __uint_as_float(__float_as_uint(Xh.y) ^ sb.x));
+        const float2 sy = f2(__uint_as_float(__float_as_uint(Yh.x) ^ sa.y), __uint_as_float(__float_as_uint(Yh.y) ^ sb.y));
+        const float2 sz = f2(__uint_as_float(__float_as_uint(Zh.x) ^ sa.z), __uint_as_float(__float_as_uint(Zh.y) ^ sb.z));
+        const float2 s_a = f2(sa.w == 0u ? sx.x : (sa.w == 1u ? sy.x : sz.x), sb.w == 0u ? sx.y : (sb.w == 1u ? sy.y : sz.y));
+        const float2 U = fma2(f2(2.0f, 2.0f), s_a, add2(add2(sx, sy), sz));
+        const float2 V = mul2(f2(-0.25f, -0.25f), s_a);
+        float2 e;
+        two_sum2(U, V, dh, e);
+        const float2 gl = fma2(gx, X2, fma2(gy, Y2, mul2(gz, Z2)));     // 2 (grad . lo)
+        dl = fma2(f2(0.125f, 0.125f), gl, e);
+    }
     // attn^4 * (grad . d)
     const float2 ch = mul2(h4, dh);
     float2 cl = fma2(h4, dh, f2(-ch.x, -ch.y));
@@ -1020,6 +1047,10 @@ __device__ __forceinline__ void noise_pair(float x1, float x2, float x3, float y
     float e;
     two_sum1(AH.x, AH.y, vh, e);
     vl = __fadd_rn(e, __fadd_rn(AL.x, AL.y));
+    if (!NORM) {                      // the dot products carried a factor 1/4 (exact)
+        vh = __fmul_rn(vh, 4.0f);
+        vl = __fmul_rn(vl, 4.0f);
+    }
 }
 
 // The octave's term (v/103 + 1) * amp added to the running pair (rh, rl),
@@ -1042,15 +1073,35 @@ __device__ __forceinline__ void octave_accumulate(float vh, float vl, float amph
     rl = __fsub_rn(sl, __fsub_rn(rh, sh));
 }
 
-// Split a binary64 into three binary32s x1 + x2 + x3 == v exactly (normal
-// range, |v| in [2^-100, 2^100]; others give x1 = (float)v and the rest 0,
-// and such lanes decide in binary64 anyway).
+// Split a binary64 into three binary32s x1 + x2 + x3 == v exactly, with
+// integer operations (GB300's binary64 pipe is narrow): x1 = the top 24
+// significant bits, x2 = the next 23 as an integer times 2^(e-46), x3 = the
+// last 6 times 2^(e-52).  Needs 2^-74 <= |v| < 2^128 (the scales stay
+// normal binary32s); v = 0 gives zeros.  Other magnitudes give x1 =
+// (float)v and zeros: outside what the planet paths use (unit or
+// radius-scaled vertices), and such a coordinate only loses its low bits.
 __device__ __forceinline__ void split3_f64(double v, float &x1, float &x2, float &x3)
 {
-    x1 = __double2float_rz(v);
-    const double r1 = __dsub_rn(v, (double)x1);     // exact: x1 is v truncated to 24 bits
-    x2 = __double2float_rz(r1);
-    x3 = __double2float_rn(__dsub_rn(r1, (double)x2));   // at most 5 bits left: exact
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
+    const int e = (int)((hw >> 20) & 0x7FF) - 1023;
+    const uint32_t sign = hw & 0x80000000u;
+    if (e < -74 || e > 127) {
+        x1 = (float)v;
+        x2 = 0.0f;
+        x3 = 0.0f;
+        return;
+    }
+    // top 24 bits: the implicit one and 23 fraction bits (bits 51-29)
+    x1 = __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+    // next 23 bits (28-6) and last 6 (5-0), as exact integers scaled by 2^(e-46) and 2^(e-52)
+    const uint32_t m2 = (lw >> 6) & 0x7FFFFFu, m3 = lw & 0x3Fu;
+    const float i2 = __fsub_rn(__uint_as_float(0x4B000000u | m2), 8388608.0f);
+    const float i3 = __fsub_rn(__uint_as_float(0x4B000000u | m3), 8388608.0f);
+    const float t2 = __fmul_rn(i2, __uint_as_float((uint32_t)(e + 81) << 23));
+    const float t3 = __fmul_rn(i3, __uint_as_float((uint32_t)(e + 75) << 23));
+    x2 = __uint_as_float(__float_as_uint(t2) | sign);
+    x3 = __uint_as_float(__float_as_uint(t3) | sign);
 }
 
 // Ordered-key transform: unsigned comparisons of keys follow float order.

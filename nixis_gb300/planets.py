@@ -325,6 +325,18 @@ class PlanetBatch:
         extra = (2 if self.max_iters > 0 else 0)       # block map + rebase
         return 3 + self.erosion_launches() + extra + len(self.inso_groups)
 
+    def fields(self, i):
+        """Height, water and sediment of request i after the last run as
+        binary64 true values (the reference's r_buff, wat and sed of
+        erosion_iteration3, erosion.py:197-279): the erosion state's pairs
+        times 2^K, exact."""
+        j = self.order.index(i)
+        K = int(self.ws[:32 * len(self.requests)].view(torch.int32).view(-1, 8)[j, 3].item())
+        b, n = self.vbeg[i], self.requests[i].n_vertices
+        rows = self.st[b:b + n].double()
+        sc = 2.0 ** K
+        return ((rows[:, 0] + rows[:, 1]) * sc, (rows[:, 2] + rows[:, 3]) * sc, (rows[:, 4] + rows[:, 5]) * sc)
+
     def results(self):
         """PlanetResult per request, in request order (views into the batch)."""
         uniform = len({(r.elev_lo, r.elev_hi, r.water0) for r in self.requests}) == 1
@@ -390,8 +402,9 @@ _plain = _PlainWork()
 _ZERO_KEY = (0x80000000 << 32) | 0x80000000
 
 
-def generate_plain(request, meshes=None, sync=True, out=None):
-    """One planet: a launch per octave, per erosion iteration; synchronised.
+def generate_plain(request, meshes=None, sync=True, out=None, blocked=False):
+    """One planet: a launch per octave, per erosion iteration (blocked=True:
+    per temporally blocked pass of the batches' setting); synchronised.
     Same arithmetic as the batched path, so the same bits."""
     r = request
     meshes = meshes if meshes is not None else _mesh.MeshCache()
@@ -417,17 +430,36 @@ def generate_plain(request, meshes=None, sync=True, out=None):
         w.raw[:n].zero_()
         k = _ZERO_KEY - (1 << 64)
         w.minmax.copy_(torch.tensor([k, k], dtype=torch.int64))
-    # the rescale to metres and the initial state (buffer 0): the batch's kernel on one planet
+    # the rescale to metres and the initial state: the batch's kernel on one
+    # planet (state in buffer 0, or in buffer iters & 1 for a blocked run)
+    blocked = blocked and r.erosion_iters > 0
     d = ErosionPlanet()
-    d.vbeg, d.n, d.nbr, d.edge, d.iters, d.slot = 0, n, m.nbr.data_ptr(), m.edge.data_ptr(), 0, 0
+    d.vbeg, d.n, d.nbr, d.edge, d.slot = 0, n, m.nbr.data_ptr(), m.edge.data_ptr(), 0
+    d.iters = r.erosion_iters if blocked else 0
+    d.rain = r.rain
     w.init_desc.copy_(torch.frombuffer(bytearray(bytes(d)), dtype=torch.uint8))
     call("nx_erosion_init_batch", _dev.ptr(w.init_desc), ctypes.byref(d), 1, _dev.ptr(w.raw), _dev.ptr(w.minmax),
          float(r.elev_lo), float(r.elev_hi), float(r.water0), _dev.ptr(w.st), _dev.ptr(w.st_tmp), s)
-    call("nx_erosion_ctl_init", _dev.ptr(w.ws), w.ws.numel(), 1, s)
-    call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(w.st), _dev.ptr(w.st_tmp),
-         r.erosion_iters, ctypes.c_float(r.rain), _dev.ptr(w.planet), None, None, _dev.ptr(w.ws), w.ws.numel(), s)
+    if blocked:
+        tb = _autotune.current()
+        _autotune.apply(tb)
+        tl = m.tiling(tb.tile_side, tb.rings)
+        d.tiling, d.ntiles, d.maxnl, d.maxc = tl.dev.data_ptr(), tl.ntiles, tl.maxnl, tl.maxc
+        w.init_desc.copy_(torch.frombuffer(bytearray(bytes(d)), dtype=torch.uint8))
+        need = int(lib().nx_erosion_workspace_size(max(n, tl.ntiles * ALIGN), 1))
+        if getattr(w, "ws_tb", None) is None or w.ws_tb.numel() < need:
+            w.ws_tb = torch.zeros(need, dtype=torch.uint8, device="cuda")
+        ws = w.ws_tb
+        call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), 1, s)
+        call("nx_erosion_batch", _dev.ptr(w.init_desc), ctypes.byref(d), 1, _dev.ptr(w.st), _dev.ptr(w.st_tmp), None,
+             _dev.ptr(ws), ws.numel(), s)
+    else:
+        ws = w.ws
+        call("nx_erosion_ctl_init", _dev.ptr(ws), ws.numel(), 1, s)
+        call("nx_erosion_steps", _dev.ptr(m.nbr), _dev.ptr(m.edge), n, _dev.ptr(w.st), _dev.ptr(w.st_tmp),
+             r.erosion_iters, ctypes.c_float(r.rain), _dev.ptr(w.planet), None, None, _dev.ptr(ws), ws.numel(), s)
     hd = w.hm[:n] if out is None else out
-    call("nx_erosion_store", _dev.ptr(w.st), n, _dev.ptr(w.ws), _dev.ptr(hd), None, None, s)
+    call("nx_erosion_store", _dev.ptr(w.st), n, _dev.ptr(ws), _dev.ptr(hd), None, None, s)
     heights = hd.clone() if out is None else hd
     ins = None
     if r.insolation:

@@ -33,6 +33,7 @@ def test_batched_equals_plain_bit_exact_and_graph_replay():
     for r, got in zip(reqs, res):
         alone = planets.generate_plain(r, cache)
         assert torch.equal(got.heights, alone.heights), r
+        assert torch.equal(got.heights, planets.generate_plain(r, cache, blocked=True).heights), r
         if r.insolation:
             assert torch.equal(got.insolation, alone.insolation), r
     h0 = [x.heights.clone() for x in res]
@@ -117,12 +118,13 @@ def test_batched_planets_from_the_workload_against_binary64():
     b = planets.PlanetBatch(pick, cache)
     b.run()
     torch.cuda.synchronize()
-    for r, got in zip(pick, b.results()):
+    for q, (r, got) in enumerate(zip(pick, b.results())):
         assert got.heights.dtype == torch.float64
         h = _oracle_planet(cache.get(r.divisions), r)
         g = got.heights.cpu().numpy()
         err = np.abs(g - h).max() / np.abs(h).max()
         assert err <= ELEV_TOL, (r, err)
+        assert np.array_equal(b.fields(q)[0].cpu().numpy(), g)      # the state's heights, exactly
     del reqs
 
 
