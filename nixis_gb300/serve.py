@@ -242,7 +242,7 @@ class ServeEngine:
     """Continuous-batching planet generator over one GPU."""
 
     def __init__(self, hbm_budget=120 * 2**30, arena_fraction=0.4, slots=4096, arena_rows=None, max_ticks=8,
-                 blocked=True, host_bytes=2 * 2**30):
+                 blocked=True, host_bytes=2 * 2**30, result_sink=None):
         _dev.require_cuda()
         self.budget = int(hbm_budget)
         rows = arena_rows if arena_rows is not None else int(self.budget * arena_fraction) // ROW_BYTES
@@ -285,6 +285,10 @@ class ServeEngine:
         self._copy_pool = ThreadPoolExecutor(max_workers=COPY_THREADS, thread_name_prefix="nx-copy")
         self.host = PinnedArena(host_bytes)
         self._delivering = []
+        # called with each finished ticket (results in place) from a delivery
+        # thread: a long stream's caller can store or reduce the results there
+        # and drop them (t.heights = None) instead of holding them all
+        self.result_sink = result_sink
 
     # ------------------------------------------------------------------
     def submit(self, request, arrival, index=0):
@@ -576,6 +580,8 @@ class ServeEngine:
         for tok in tokens:
             self.host.release(tok)
         t.stage = "done"
+        if self.result_sink is not None:
+            self.result_sink(t)
 
     def _collect(self):
         still = []
@@ -657,9 +663,11 @@ class ServeEngine:
         return tickets
 
 
-def serve_plain(stream, meshes=None, realtime=True, t0=None):
+def serve_plain(stream, meshes=None, realtime=True, t0=None, sink=None):
     """The comparator: requests handled one at a time, in arrival order, with
-    the plain per-planet path; returns (arrival, finish) per request."""
+    the plain per-planet path; returns (arrival, finish, heights, insolation)
+    per request, host tensors -- or, with `sink`, (arrival, finish,
+    sink(heights, insolation)) so a long stream need not hold every result."""
     meshes = meshes if meshes is not None else ResidentMeshes(80 * 2**30)
     t0 = time.perf_counter() if t0 is None else t0
     out = []
@@ -675,7 +683,8 @@ def serve_plain(stream, meshes=None, realtime=True, t0=None):
         h = res.heights.cpu()
         i = res.insolation.cpu() if res.insolation is not None else None
         torch.cuda.synchronize()
-        out.append((arrival, time.perf_counter(), h, i))
+        finish = time.perf_counter()
+        out.append((arrival, finish, sink(h, i)) if sink is not None else (arrival, finish, h, i))
     return out
 
 

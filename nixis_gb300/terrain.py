@@ -2,8 +2,10 @@
 
 Arrays may be numpy (copied to the GPU and back, like-for-like with the
 reference) or CUDA tensors (used in place).  The fBm is one fused kernel over
-all octaves (nx_fbm); results are binary32-accurate values returned in the
-reference's float64 dtype.
+all octaves.  Float64 results (the reference's dtype) come from the
+pair-precision kernel (nx_fbm_pair: within ~1e-13 of the binary64 sums,
+close enough that erosion run on them keeps the reference's flow choices);
+float32 results from the binary32 kernel (nx_fbm, ~1e-6 of the range).
 """
 import ctypes
 
@@ -28,7 +30,9 @@ def _octave_args(n_octaves, n_init_roughness, n_init_strength, n_roughness, n_pe
 
 def fbm(verts, perm, pgi, scale, strength, radius, out=None, accumulate=False, out_dtype=torch.float64,
         stream=None, count_fallbacks=False):
-    """Sum over octaves o of (noise3d(v * scale[o]) + 1) * 0.5 * strength[o] * radius.
+    """Sum over octaves o of (noise3d(v * scale[o]) + 1) * 0.5 * strength[o] * radius,
+    in pair precision for a float64 `out` (the default) and in binary32 for a
+    float32 one.
 
     verts: float64 (N,3) CUDA tensor (or numpy).  `out`, if given, is a CUDA
     tensor (float64 or float32) written (or added to, with accumulate=True).
@@ -48,12 +52,15 @@ def fbm(verts, perm, pgi, scale, strength, radius, out=None, accumulate=False, o
     sc = (ctypes.c_double * max(no, 1))(*scale)
     st = (ctypes.c_double * max(no, 1))(*strength)
     nfb = torch.zeros(1, dtype=torch.int64, device="cuda") if count_fallbacks else None
-    o64 = out if out.dtype == torch.float64 else None
-    o32 = out if out.dtype == torch.float32 else None
-    if o64 is None and o32 is None:
+    if out.dtype == torch.float64:
+        # pair precision; the octaves' amplitudes set its per-octave form (amp_ref 0)
+        call("nx_fbm_pair", _dev.ptr(xyz), n, _dev.ptr(p), _dev.ptr(g), no, sc, st, float(radius), 0.0, None,
+             _dev.ptr(out), 1 if accumulate else 0, None, _dev.ptr(nfb), _dev.stream_handle(stream))
+    elif out.dtype == torch.float32:
+        call("nx_fbm", _dev.ptr(xyz), n, _dev.ptr(p), _dev.ptr(g), no, sc, st, float(radius), None,
+             _dev.ptr(out), 1 if accumulate else 0, _dev.ptr(nfb), _dev.stream_handle(stream))
+    else:
         raise ValueError("out must be float64 or float32")
-    call("nx_fbm", _dev.ptr(xyz), n, _dev.ptr(p), _dev.ptr(g), no, sc, st, float(radius), _dev.ptr(o64),
-         _dev.ptr(o32), 1 if accumulate else 0, _dev.ptr(nfb), _dev.stream_handle(stream))
     return out, (int(nfb.item()) if count_fallbacks else None)
 
 
