@@ -288,6 +288,28 @@ def test_temporally_blocked_batch_equals_iteration_at_a_time(rain):
         assert torch.equal(x.heights, planets.generate_plain(r, cache).heights), r
 
 
+@pytest.mark.parametrize("rain", [0.0, 0.3 / 320])
+def test_larger_meshes_blocked_equal_iteration_at_a_time(rain):
+    """Meshes of divisions 160-339 (many tiles per face, tiles away from
+    every face edge), pass counts with a short last pass and both parities:
+    blocked == one launch per iteration, bit for bit, no error flags."""
+    from nixis_gb300 import autotune, mesh, planets
+    from nixis_gb300.planets import PlanetRequest
+    tb = autotune.DEFAULT
+    reqs = [PlanetRequest(seed=s, divisions=k, octaves=7, erosion_iters=it, rain=rain)
+            for s, (k, it) in enumerate([(200, 9), (250, 14), (339, 33), (160, 6), (300, 1)])]
+    cache = mesh.MeshCache()
+    a = planets.PlanetBatch(reqs, cache, blocked=True, tb=tb)
+    a.run()
+    b = planets.PlanetBatch(reqs, cache, blocked=False)
+    b.run()
+    torch.cuda.synchronize()
+    for r, x, y in zip(reqs, a.results(), b.results()):
+        assert torch.equal(x.heights, y.heights), r
+    ctl = a.ws[:32 * len(reqs)].view(torch.int32).view(-1, 8)
+    assert int(ctl[:, 6].abs().sum().item()) == 0
+
+
 def test_temporally_blocked_long_run_rescales_like_iteration_at_a_time():
     """170 and 150 iterations: both paths rescale (at different iterations:
     per pass vs per iteration) and hold the same true values."""
