@@ -395,6 +395,20 @@ def bench_ours(args):
                                       f"{vo} vertex-octaves; peak = 152 SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz (derived)",
                              "note": "evaluated in float-float pairs (~2.4x the binary32 kernel's instructions) to stay "
                                      "within 1e-13 of binary64, which the erosion's flow choices need"}}
+    issue = os.path.join(ROOT, "profiles", "fbm_issue.json")
+    if os.path.exists(issue):
+        # executed instructions against the issue peak (152 SMs x 4
+        # schedulers x 32 lanes per clock): what the pair arithmetic costs
+        try:
+            with open(issue) as f:
+                ipv = float(json.load(f)["thread_instructions_per_vertex_octave"])
+            rate = vo * ipv / (fbm_ms / 1e3)
+            kernels["fbm_batch_kernel"]["executed"] = {
+                "thread_instructions_per_vertex_octave": ipv, "tinst_per_s": rate,
+                "issue_frac": rate / (152 * 4 * 32 * sm_mhz * 1e6),
+                "source": "instruction count from the ncu capture in profiles/fbm_batch_small.md"}
+        except (OSError, KeyError, ValueError):
+            pass
     inso = measure_insolation(sm_mhz)
     if inso:
         kernels["insolation_kernel"] = inso
