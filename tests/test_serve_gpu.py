@@ -47,6 +47,29 @@ def test_served_results_equal_alone(blocked):
     assert eng.arena.used == 0 and len(eng.free_slots) == 64
 
 
+def test_result_sinks_see_every_result_once():
+    """result_sink (engine) and sink (plain path) receive each finished
+    request's arrays -- here reduced to byte strings and dropped, as a long
+    stream's caller does -- and both paths' reductions agree."""
+    from nixis_gb300 import serve
+    stream = small_stream(8, seed=13)
+    seen = {}
+
+    def sink(t):
+        assert t.index not in seen
+        seen[t.index] = (t.heights.tobytes(), None if t.insolation is None else t.insolation.tobytes())
+        t.heights = t.insolation = None
+
+    with serve.ServeEngine(hbm_budget=4 * 2**30, arena_rows=2_000_000, slots=64, result_sink=sink) as eng:
+        tickets = eng.run(stream, realtime=False)
+    assert sorted(seen) == list(range(len(stream)))
+    assert all(t.heights is None for t in tickets)
+    plain = serve.serve_plain(stream, realtime=False,
+                              sink=lambda h, i: (h.numpy().tobytes(), None if i is None else i.numpy().tobytes()))
+    for t, (_, _, red) in zip(tickets, plain):
+        assert seen[t.index] == red, t.request
+
+
 def test_admission_waits_for_memory_and_still_matches():
     from nixis_gb300 import serve
     stream = small_stream(10, seed=9)
