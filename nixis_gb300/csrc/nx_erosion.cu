@@ -132,7 +132,9 @@ __device__ __forceinline__ unsigned erode_accum(float hh, float hl, float4 o, fl
     const float2 d2 = __fadd2_rn(make_float2(o.x, o.y), make_float2(-hh, -hl));
     const float diff = __fadd_rn(d2.x, d2.y);
     const bool up = diff > 0.0f, dn = diff < 0.0f;
-    const float g = up ? 1.0f : (dn ? -1.0f : 0.0f);
+    // +-1 with the sign of diff; 0 where diff is 0 or NaN (no flow, as the
+    // reference's slope tests decide for a NaN slope)
+    const float g = fabsf(diff) > 0.0f ? __int_as_float((__float_as_int(diff) & (int)0x80000000) | 0x3F800000) : 0.0f;
     const float xh = __fmul_rn(g, o.z), xl = __fmul_rn(g, o.w);
     const float p = __fmul_rn(xh, dh);
     float pe = __fmaf_rn(xh, dh, -p);
@@ -709,19 +711,111 @@ __device__ __forceinline__ float unkey(uint32_t k)
     return __uint_as_float((k & 0x80000000u) ? (k ^ 0x80000000u) : ~k);
 }
 
-__device__ __forceinline__ int block_planet(const nx_erosion_planet *P, int np, int64_t row)
+// Rows of the packed planets handed to the init and heights kernels: units
+// of 4 x 256 rows, unit u to block u mod grid (consecutive blocks sweep
+// consecutive rows), thread t of a block the rows base + t + 256 k, k < 4.
+// A thread finds its first row's planet by binary search and then walks to
+// the next planet when its row reaches that planet's vbeg: no per-block
+// search or barrier.  Rows outside every planet (alignment padding) are
+// skipped.
+struct PlanetWalk {
+    int p;
+    int64_t beg, end, next;
+
+    __device__ __forceinline__ void seek(const nx_erosion_planet *P, int np, int64_t row)
+    {
+        p = find_planet(P, np, row);
+        span(P, np);
+    }
+    __device__ __forceinline__ void span(const nx_erosion_planet *P, int np)
+    {
+        beg = P[p].vbeg;
+        end = beg + P[p].n;
+        next = p + 1 < np ? P[p + 1].vbeg : INT64_MAX;
+    }
+    // advance to the planet of `row` (rows increase); true if it changed
+    __device__ __forceinline__ bool to(const nx_erosion_planet *P, int np, int64_t row)
+    {
+        if (row < next) return false;
+        do {
+            ++p;
+            span(P, np);
+        } while (row >= next);
+        return true;
+    }
+    __device__ __forceinline__ bool has(int64_t row) const { return row >= beg && row < end; }
+    // rows row + 256 k, k < WALK_UNROLL, all in this planet
+    __device__ __forceinline__ bool all(int64_t row) const;
+};
+
+constexpr int WALK_UNROLL = 4;
+constexpr int64_t WALK_UNIT = WALK_UNROLL * 256;
+
+__device__ __forceinline__ bool PlanetWalk::all(int64_t row) const
 {
-    return find_planet(P, np, row);
+    return row >= beg && row + (WALK_UNROLL - 1) * 256 < end;
+}
+
+int walk_grid(int64_t total)
+{
+    const int64_t units = (total + WALK_UNIT - 1) / WALK_UNIT;
+    const int64_t cap = (int64_t)nx::sm_count() * 8;
+    return (int)(units < cap ? units : cap);
+}
+
+// Planets whose rescale constants the init kernel stages in shared memory
+// (beyond that each thread forms its planet's constants itself).
+constexpr int INIT_SMEM_PLANETS = 1024;
+
+// A planet's rescale constants: its minimum as a pair, f = (hi - lo) /
+// (max - min) as a pair (formed in binary64).
+__device__ __forceinline__ float4 init_consts(const unsigned long long *minmax, int p, double lo, double hi)
+{
+    const unsigned long long kmn = minmax[2 * p], kmx = minmax[2 * p + 1];
+    const float mnh = unkey((uint32_t)(kmn >> 32)), mnl = unkey((uint32_t)kmn);
+    const float mxh = unkey((uint32_t)(kmx >> 32)), mxl = unkey((uint32_t)kmx);
+    const double mn = (double)mnh + (double)mnl, mx = (double)mxh + (double)mxl;
+    const double f = (hi - lo) / (mx - mn);
+    const float fh = (float)f;
+    return make_float4(mnh, mnl, fh, (float)(f - (double)fh));
+}
+
+// One vertex's starting height pair: (raw - min) * f + lo, renormalised.
+__device__ __forceinline__ float2 init_height(float2 r, float4 c, float loh, float lol)
+{
+    // t = raw - min
+    float th, te;
+    {
+        th = __fsub_rn(r.x, c.x);
+        const float bb = __fsub_rn(th, r.x);
+        te = __fadd_rn(__fsub_rn(r.x, __fsub_rn(th, bb)), __fsub_rn(-c.x, bb));
+    }
+    const float tl = __fadd_rn(te, __fsub_rn(r.y, c.y));
+    // t * f
+    const float ph = __fmul_rn(th, c.z);
+    float pl = __fmaf_rn(th, c.z, -ph);
+    pl = __fmaf_rn(th, c.w, __fmaf_rn(tl, c.z, pl));
+    // + lo, renormalised
+    float sh, se;
+    {
+        sh = __fadd_rn(ph, loh);
+        const float bb = __fsub_rn(sh, ph);
+        se = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bb)), __fsub_rn(loh, bb));
+    }
+    const float sl = __fadd_rn(se, __fadd_rn(pl, lol));
+    const float h = __fadd_rn(sh, sl);
+    return make_float2(h, __fsub_rn(sl, __fsub_rn(h, sh)));
 }
 
 // util.rescale (util.py:110-140) of the raw fBm pair sums to [lo, hi], and
 // the initial state (h as a pair, water0 as a pair | 0, 0, 0, 0) in the
 // buffer the planet's first iteration reads: B[iters & 1].  The reference
 // computes ((x - min) / (max - min)) * (hi - lo) + lo in binary64; here
-// (x - min) * f + lo with f = (hi - lo) / (max - min) formed once per block
-// in binary64 (min and max are exact as binary64) and the per-vertex
+// (x - min) * f + lo with f = (hi - lo) / (max - min) formed once per
+// planet in binary64 (min and max are exact as binary64) and the per-vertex
 // arithmetic in pairs, within ~2^-47 of the value.  A constant field
-// (max == min) gives NaN, as the reference's division does.
+// (max == min) gives NaN, as the reference's division does.  Dynamic shared
+// memory: a float4 per planet when np <= INIT_SMEM_PLANETS, else none.
 __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_planet *__restrict__ P, int np,
                                                            const float2 *__restrict__ raw,
                                                            const unsigned long long *__restrict__ minmax,
@@ -729,73 +823,96 @@ __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_plan
                                                            float4 *__restrict__ st0, float4 *__restrict__ st1,
                                                            int64_t total)
 {
-    __shared__ float s_c[6];
+    extern __shared__ float4 s_ic[];
+    const bool staged = np <= INIT_SMEM_PLANETS;
+    if (staged) {
+        for (int i = threadIdx.x; i < np; i += blockDim.x) s_ic[i] = init_consts(minmax, i, lo, hi);
+        __syncthreads();
+    }
     const float loh = (float)lo, lol = (float)(lo - (double)(float)lo);
-    for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
-        const int p = block_planet(P, np, blk * 256);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const unsigned long long kmn = minmax[2 * p], kmx = minmax[2 * p + 1];
-            const float mnh = unkey((uint32_t)(kmn >> 32)), mnl = unkey((uint32_t)kmn);
-            const float mxh = unkey((uint32_t)(kmx >> 32)), mxl = unkey((uint32_t)kmx);
-            const double mn = (double)mnh + (double)mnl, mx = (double)mxh + (double)mxl;
-            const double f = (hi - lo) / (mx - mn);
-            const float fh = (float)f;
-            s_c[0] = mnh;
-            s_c[1] = mnl;
-            s_c[2] = fh;
-            s_c[3] = (float)(f - (double)fh);
+    int64_t base = (int64_t)blockIdx.x * WALK_UNIT;
+    if (base + threadIdx.x >= total) return;
+    PlanetWalk W;
+    W.seek(P, np, base + threadIdx.x);
+    float4 c = staged ? s_ic[W.p] : init_consts(minmax, W.p, lo, hi);
+    float4 *dst = (P[W.p].iters & 1) ? st1 : st0;
+    for (; base < total; base += (int64_t)gridDim.x * WALK_UNIT) {
+        const int64_t row = base + threadIdx.x;
+        if (W.all(row)) {
+            // the four rows lie in the current planet: loads in flight together
+            float2 r[WALK_UNROLL];
+#pragma unroll
+            for (int u = 0; u < WALK_UNROLL; ++u) r[u] = raw[row + u * 256];
+#pragma unroll
+            for (int u = 0; u < WALK_UNROLL; ++u) {
+                const float2 h = init_height(r[u], c, loh, lol);
+                const int64_t x = row + u * 256;
+                dst[2 * x] = make_float4(h.x, h.y, w0h, w0l);
+                dst[2 * x + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            continue;
         }
-        __syncthreads();
-        const int64_t row = blk * 256 + threadIdx.x;
-        const int64_t i = row - P[p].vbeg;
-        if (i < 0 || i >= P[p].n) continue;
-        const float2 r = raw[row];
-        const float mnh = s_c[0], mnl = s_c[1], fh = s_c[2], fl = s_c[3];
-        // t = raw - min
-        float th, te;
-        {
-            th = __fsub_rn(r.x, mnh);
-            const float bb = __fsub_rn(th, r.x);
-            te = __fadd_rn(__fsub_rn(r.x, __fsub_rn(th, bb)), __fsub_rn(-mnh, bb));
+        for (int u = 0; u < WALK_UNROLL; ++u) {
+            const int64_t x = row + u * 256;
+            if (x >= total) break;
+            if (W.to(P, np, x)) {
+                c = staged ? s_ic[W.p] : init_consts(minmax, W.p, lo, hi);
+                dst = (P[W.p].iters & 1) ? st1 : st0;
+            }
+            if (!W.has(x)) continue;
+            const float2 h = init_height(raw[x], c, loh, lol);
+            dst[2 * x] = make_float4(h.x, h.y, w0h, w0l);
+            dst[2 * x + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
-        const float tl = __fadd_rn(te, __fsub_rn(r.y, mnl));
-        // t * f
-        const float ph = __fmul_rn(th, fh);
-        float pl = __fmaf_rn(th, fh, -ph);
-        pl = __fmaf_rn(th, fl, __fmaf_rn(tl, fh, pl));
-        // + lo, renormalised
-        float sh, se;
-        {
-            sh = __fadd_rn(ph, loh);
-            const float bb = __fsub_rn(sh, ph);
-            se = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bb)), __fsub_rn(loh, bb));
-        }
-        const float sl = __fadd_rn(se, __fadd_rn(pl, lol));
-        const float h = __fadd_rn(sh, sl);
-        const float hl = __fsub_rn(sl, __fsub_rn(h, sh));
-        float4 *dst = (P[p].iters & 1) ? st1 : st0;
-        dst[2 * row] = make_float4(h, hl, w0h, w0l);
-        dst[2 * row + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
-// Heights of every planet after its run: (h_hi + h_lo) * 2^K in binary64.
-// The pair's sum is exact in binary64 and scaling by 2^K is exact, so the
-// value is the state's to the last bit of the pair.
+// v * 2^K as a binary64 (exact) by integer operations when v is a normal
+// binary32 and the result's exponent is in range; otherwise through the
+// binary64 pipe.
+__device__ __forceinline__ double f32_scaled(float v, int K)
+{
+    const uint32_t u = __float_as_uint(v);
+    const int e = (int)((u >> 23) & 0xFFu);
+    const int E = e + (1023 - 127) + K;
+    if (e == 0 || e == 255 || E <= 0 || E >= 2047) return ldexp((double)v, K);
+    return __hiloint2double((int)((u & 0x80000000u) | ((uint32_t)E << 20) | ((u & 0x7FFFFFu) >> 3)), (int)(u << 29));
+}
+
+// Heights of every planet after its run: (h_hi + h_lo) * 2^K in binary64,
+// formed as h_hi 2^K + h_lo 2^K (both exact) with one rounding: the same
+// bits as rounding h_hi + h_lo and then scaling.
 __global__ void __launch_bounds__(256) erosion_heights_kernel(const nx_erosion_planet *__restrict__ P, int np,
                                                               const float4 *__restrict__ st,
                                                               const nx_erosion_ctl *__restrict__ ctl,
                                                               double *__restrict__ out, int64_t total)
 {
-    for (int64_t blk = blockIdx.x; blk * 256 < total; blk += gridDim.x) {
-        const int p = block_planet(P, np, blk * 256);
-        const int64_t row = blk * 256 + threadIdx.x;
-        const int64_t i = row - P[p].vbeg;
-        if (i < 0 || i >= P[p].n) continue;
-        const float4 v = st[2 * row];
-        const int K = ctl[P[p].slot].K[0];
-        out[row] = ldexp((double)v.x + (double)v.y, K);
+    int64_t base = (int64_t)blockIdx.x * WALK_UNIT;
+    if (base + threadIdx.x >= total) return;
+    PlanetWalk W;
+    W.seek(P, np, base + threadIdx.x);
+    int K = ctl[P[W.p].slot].K[0];
+    for (; base < total; base += (int64_t)gridDim.x * WALK_UNIT) {
+        const int64_t row = base + threadIdx.x;
+        if (W.all(row)) {
+            float2 v[WALK_UNROLL];
+#pragma unroll
+            for (int u = 0; u < WALK_UNROLL; ++u) {
+                const float4 s = st[2 * (row + u * 256)];
+                v[u] = make_float2(s.x, s.y);
+            }
+#pragma unroll
+            for (int u = 0; u < WALK_UNROLL; ++u) out[row + u * 256] = f32_scaled(v[u].x, K) + f32_scaled(v[u].y, K);
+            continue;
+        }
+        for (int u = 0; u < WALK_UNROLL; ++u) {
+            const int64_t x = row + u * 256;
+            if (x >= total) break;
+            if (W.to(P, np, x)) K = ctl[P[W.p].slot].K[0];
+            if (!W.has(x)) continue;
+            const float4 s = st[2 * x];
+            out[x] = f32_scaled(s.x, K) + f32_scaled(s.y, K);
+        }
     }
 }
 
@@ -1351,10 +1468,10 @@ NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const 
     if (total == 0) return NX_OK;
     const float w0h = (float)water0, w0l = (float)(water0 - (double)w0h);
     if ((uintptr_t)raw_dev & 7u) return nx::fail(NX_EINVAL, "nx_erosion_init_batch: raw pairs must be 8-byte aligned");
-    erosion_init_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(planets_dev, nplanets, (const float2 *)raw_dev,
-                                                                         minmax_dev,
-                                                                         elev_lo, elev_hi, w0h, w0l, (float4 *)st_dev,
-                                                                         (float4 *)st_tmp_dev, total);
+    const size_t smem = nplanets <= INIT_SMEM_PLANETS ? sizeof(float4) * (size_t)nplanets : 0;
+    erosion_init_kernel<<<walk_grid(total), 256, smem, (cudaStream_t)stream>>>(
+        planets_dev, nplanets, (const float2 *)raw_dev, minmax_dev, elev_lo, elev_hi, w0h, w0l, (float4 *)st_dev,
+        (float4 *)st_tmp_dev, total);
     NX_CHECK_LAUNCH("erosion_init_kernel");
     nx::note_launch(1);
     return NX_OK;
@@ -1371,7 +1488,7 @@ NX_EXPORT int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, con
     int rc = check_packed(planets_host, nplanets, &total);
     if (rc) return rc;
     if (total == 0) return NX_OK;
-    erosion_heights_kernel<<<grid1d(total), 256, 0, (cudaStream_t)stream>>>(
+    erosion_heights_kernel<<<walk_grid(total), 256, 0, (cudaStream_t)stream>>>(
         planets_dev, nplanets, (const float4 *)st_dev, (const nx_erosion_ctl *)workspace, out_dev, total);
     NX_CHECK_LAUNCH("erosion_heights_kernel");
     nx::note_launch(1);
