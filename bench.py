@@ -359,13 +359,15 @@ def bench_ours(args):
     ev[0].record(stream)
     call("nx_fbm_batch", _dev.ptr(batch.fb_dev), ctypes.cast(batch.fb_host, ctypes.c_void_p), np_, None, s)
     ev[1].record(stream)
-    call("nx_erosion_init_batch", _dev.ptr(batch.er_dev), ctypes.cast(batch.er_host, ctypes.c_void_p), np_,
-         _dev.ptr(batch.raw), _dev.ptr(batch.minmax), -8000.0, 8000.0,
-         ctypes.c_double(1e-3), _dev.ptr(batch.st), _dev.ptr(batch.st_tmp), s)
     call("nx_erosion_ctl_init", _dev.ptr(batch.ws), batch.ws.numel(), np_, s)
     ev[2].record(stream)
-    call("nx_erosion_batch", _dev.ptr(batch.er_dev), ctypes.cast(batch.er_host, ctypes.c_void_p), np_,
-         _dev.ptr(batch.st), _dev.ptr(batch.st_tmp), None, _dev.ptr(batch.ws), batch.ws.numel(), s)
+    # the erosion stage as the batch runs it: the blocked passes with the
+    # rescale fused into each planet's first pass and the heights into its last
+    r0 = reqs[0]
+    call("nx_erosion_run_batch", _dev.ptr(batch.er_dev), ctypes.cast(batch.er_host, ctypes.c_void_p), np_,
+         _dev.ptr(batch.raw), _dev.ptr(batch.minmax), float(r0.elev_lo), float(r0.elev_hi), float(r0.water0),
+         _dev.ptr(batch.st), _dev.ptr(batch.st_tmp), _dev.ptr(batch.heights), _dev.ptr(batch.ws),
+         batch.ws.numel(), s)
     ev[3].record(stream)
     torch.cuda.synchronize()
     ero_ms = ev[2].elapsed_time(ev[3])

@@ -393,6 +393,17 @@ int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, const nx_eros
                              int nplanets, const float *st_dev, const void *workspace, double *out_dev,
                              void *stream);
 
+/* nx_erosion_init_batch, nx_erosion_batch and nx_erosion_heights_batch in
+ * one call, with the same results (state in st_dev, heights in
+ * heights_dev).  On the temporally blocked path the rescale runs inside each
+ * eroding planet's first pass (its load phase reads the raw pair sums), so
+ * the starting state is never written to HBM; planets with no iterations get
+ * their state from one rescale launch.  Call nx_erosion_ctl_init first. */
+int nx_erosion_run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int nplanets,
+                         const float *raw_dev, const unsigned long long *minmax_dev, double elev_lo, double elev_hi,
+                         double water0, float *st_dev, float *st_tmp_dev, double *heights_dev, void *workspace,
+                         size_t ws_bytes, void *stream);
+
 /* Latitude-table insolation (climate.py:503-597).  Tables for n_tilts
  * tilts (degrees, device float64[n_tilts]) into tables_dev
  * float[n_tilts * 181]: entry i is latitude i for i <= 90, i - 181 above,

@@ -46,6 +46,7 @@ SIGNATURES = {
     "nx_fbm_pair": (_i32, [_p, _i64, _p, _p, _i32, _p, _p, _d, _d, _p, _p, _i32, _p, _p, _p]),
     "nx_erosion_init_batch": (_i32, [_p, _p, _i32, _p, _p, _d, _d, _d, _p, _p, _p]),
     "nx_erosion_heights_batch": (_i32, [_p, _p, _i32, _p, _p, _p, _p]),
+    "nx_erosion_run_batch": (_i32, [_p, _p, _i32, _p, _p, _d, _d, _d, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "nx_erosion_steps_noalloc": (_i32, [_p, _p, _i64, _p, _i32, ctypes.c_float, _p, _p, _p]),
     "nx_erosion_tick": (_i32, [_p, _p, _i32, _i32, _p, _p, _p, ctypes.c_size_t, _i32, _i32, _p]),
     "nx_erosion_finish": (_i32, [_p, _i32, _p, _p]),

@@ -334,6 +334,72 @@ __global__ void __launch_bounds__(BLOCK, 4) erosion_step_kernel(StepArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// Ordered key -> float (inverse of the fBm kernel's min/max keys).
+__device__ __forceinline__ float unkey(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k ^ 0x80000000u) : ~k);
+}
+
+// A planet's rescale constants: its minimum as a pair, f = (hi - lo) /
+// (max - min) as a pair (formed in binary64).
+__device__ __forceinline__ float4 init_consts(const unsigned long long *minmax, int p, double lo, double hi)
+{
+    const unsigned long long kmn = minmax[2 * p], kmx = minmax[2 * p + 1];
+    const float mnh = unkey((uint32_t)(kmn >> 32)), mnl = unkey((uint32_t)kmn);
+    const float mxh = unkey((uint32_t)(kmx >> 32)), mxl = unkey((uint32_t)kmx);
+    const double mn = (double)mnh + (double)mnl, mx = (double)mxh + (double)mxl;
+    const double f = (hi - lo) / (mx - mn);
+    const float fh = (float)f;
+    return make_float4(mnh, mnl, fh, (float)(f - (double)fh));
+}
+
+// One vertex's starting height pair: (raw - min) * f + lo, renormalised.
+__device__ __forceinline__ float2 init_height(float2 r, float4 c, float loh, float lol)
+{
+    // t = raw - min
+    float th, te;
+    {
+        th = __fsub_rn(r.x, c.x);
+        const float bb = __fsub_rn(th, r.x);
+        te = __fadd_rn(__fsub_rn(r.x, __fsub_rn(th, bb)), __fsub_rn(-c.x, bb));
+    }
+    const float tl = __fadd_rn(te, __fsub_rn(r.y, c.y));
+    // t * f
+    const float ph = __fmul_rn(th, c.z);
+    float pl = __fmaf_rn(th, c.z, -ph);
+    pl = __fmaf_rn(th, c.w, __fmaf_rn(tl, c.z, pl));
+    // + lo, renormalised
+    float sh, se;
+    {
+        sh = __fadd_rn(ph, loh);
+        const float bb = __fsub_rn(sh, ph);
+        se = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bb)), __fsub_rn(loh, bb));
+    }
+    const float sl = __fadd_rn(se, __fadd_rn(pl, lol));
+    const float h = __fadd_rn(sh, sl);
+    return make_float2(h, __fsub_rn(sl, __fsub_rn(h, sh)));
+}
+
+// v * 2^K as a binary64 (exact) for the cases the integer form below leaves
+// out; a call, so that the common path is not if-converted into binary64
+// operations (GB300's binary64 pipe is narrow).
+__device__ __noinline__ double f32_scaled_slow(float v, int K)
+{
+    return ldexp((double)v, K);
+}
+
+// v * 2^K as a binary64 (exact) by integer operations when v is a normal
+// binary32 and the result's exponent is in range; otherwise through the
+// binary64 pipe.
+__device__ __forceinline__ double f32_scaled(float v, int K)
+{
+    const uint32_t u = __float_as_uint(v);
+    const int e = (int)((u >> 23) & 0xFFu);
+    const int E = e + (1023 - 127) + K;
+    if (e == 0 || e == 255 || E <= 0 || E >= 2047) return f32_scaled_slow(v, K);
+    return __hiloint2double((int)((u & 0x80000000u) | ((uint32_t)E << 20) | ((u & 0x7FFFFFu) >> 3)), (int)(u << 29));
+}
+
 // Temporally blocked erosion: one block per (planet, tile) runs a pass of up
 // to R iterations in shared memory.  It loads the tile and its halo rings
 // (state * lambda), then for m = 0..len-1 updates the members and the rings
@@ -375,6 +441,15 @@ struct TbArgs {
     float4 *st0;
     float4 *st1;
     nx_erosion_ctl *ctl;
+    // Optional fusion of the rescale: a planet's first pass reads the raw
+    // fBm pair sums (float2 per row) and rescales them to its starting
+    // heights as erosion_init_kernel does (minimum and maximum keys per
+    // planet index in minmax, target range [elo, ehi], starting water (w0h,
+    // w0l)) instead of reading a state buffer.
+    const float2 *raw = nullptr;
+    const unsigned long long *minmax = nullptr;
+    double elo = 0.0, ehi = 0.0;
+    float w0h = 0.0f, w0l = 0.0f;
 };
 
 // Threads per block of the blocked kernel: 256, 512 or 1024 (autotuned),
@@ -516,6 +591,16 @@ __global__ void __launch_bounds__(THREADS, MINB > 0 ? MINB : (PF ? 768 : 1024) /
         }
         if ((int)threadIdx.x < C0) myrow = tile_row<false>(lnb, led, threadIdx.x);
     }
+    // the planet's first pass of a fused run starts from the raw fBm sums
+    const bool fresh = a.raw != nullptr && q == 0;
+    float4 ic = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float eloh = (float)a.elo, elol = (float)(a.elo - (double)(float)a.elo);
+    if (fresh) {
+        __shared__ float4 s_ic;
+        if (threadIdx.x == 0) s_ic = init_consts(a.minmax, bm.x, a.elo, a.ehi);
+        __syncthreads();
+        ic = s_ic;
+    }
     // two rows per thread per round, both gathers in flight before either
     // is stored (halves the dependent DRAM round trips of the load phase)
     for (int l0 = threadIdx.x; l0 < NL; l0 += 2 * THREADS) {
@@ -523,8 +608,18 @@ __global__ void __launch_bounds__(THREADS, MINB > 0 ? MINB : (PF ? 768 : 1024) /
         const bool two = l1 < NL;
         const int64_t r0 = P.vbeg + ids[l0];
         const int64_t r1 = two ? P.vbeg + ids[l1] : r0;
-        const float4 x0 = ist[2 * r0], y0 = ist[2 * r0 + 1];
-        const float4 x1 = ist[2 * r1], y1 = ist[2 * r1 + 1];
+        float4 x0, y0, x1, y1;
+        if (fresh) {
+            // the state erosion_init_kernel would have written
+            const float2 g0 = a.raw[r0], g1 = a.raw[r1];
+            const float2 h0 = init_height(g0, ic, eloh, elol), h1 = init_height(g1, ic, eloh, elol);
+            x0 = make_float4(h0.x, h0.y, a.w0h, a.w0l);
+            x1 = make_float4(h1.x, h1.y, a.w0h, a.w0l);
+            y0 = y1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            x0 = ist[2 * r0]; y0 = ist[2 * r0 + 1];
+            x1 = ist[2 * r1]; y1 = ist[2 * r1 + 1];
+        }
         const Pair w0 = prain(__fmul_rn(x0.z, lam), __fmul_rn(x0.w, lam), rain);
         buf0[l0] = make_float4(__fmul_rn(x0.x, lam), __fmul_rn(x0.y, lam), w0.h, w0.l);
         sed[l0] = make_float2(__fmul_rn(y0.x, lam), __fmul_rn(y0.y, lam));
@@ -705,12 +800,6 @@ __global__ void erosion_store64_kernel(const float4 *__restrict__ st, int64_t n,
     }
 }
 
-// Ordered key -> float (inverse of the fBm kernel's min/max keys).
-__device__ __forceinline__ float unkey(uint32_t k)
-{
-    return __uint_as_float((k & 0x80000000u) ? (k ^ 0x80000000u) : ~k);
-}
-
 // Rows of the packed planets handed to the init and heights kernels: units
 // of 4 x 256 rows, unit u to block u mod grid (consecutive blocks sweep
 // consecutive rows), thread t of a block the rows base + t + 256 k, k < 4.
@@ -767,46 +856,6 @@ int walk_grid(int64_t total)
 // (beyond that each thread forms its planet's constants itself).
 constexpr int INIT_SMEM_PLANETS = 1024;
 
-// A planet's rescale constants: its minimum as a pair, f = (hi - lo) /
-// (max - min) as a pair (formed in binary64).
-__device__ __forceinline__ float4 init_consts(const unsigned long long *minmax, int p, double lo, double hi)
-{
-    const unsigned long long kmn = minmax[2 * p], kmx = minmax[2 * p + 1];
-    const float mnh = unkey((uint32_t)(kmn >> 32)), mnl = unkey((uint32_t)kmn);
-    const float mxh = unkey((uint32_t)(kmx >> 32)), mxl = unkey((uint32_t)kmx);
-    const double mn = (double)mnh + (double)mnl, mx = (double)mxh + (double)mxl;
-    const double f = (hi - lo) / (mx - mn);
-    const float fh = (float)f;
-    return make_float4(mnh, mnl, fh, (float)(f - (double)fh));
-}
-
-// One vertex's starting height pair: (raw - min) * f + lo, renormalised.
-__device__ __forceinline__ float2 init_height(float2 r, float4 c, float loh, float lol)
-{
-    // t = raw - min
-    float th, te;
-    {
-        th = __fsub_rn(r.x, c.x);
-        const float bb = __fsub_rn(th, r.x);
-        te = __fadd_rn(__fsub_rn(r.x, __fsub_rn(th, bb)), __fsub_rn(-c.x, bb));
-    }
-    const float tl = __fadd_rn(te, __fsub_rn(r.y, c.y));
-    // t * f
-    const float ph = __fmul_rn(th, c.z);
-    float pl = __fmaf_rn(th, c.z, -ph);
-    pl = __fmaf_rn(th, c.w, __fmaf_rn(tl, c.z, pl));
-    // + lo, renormalised
-    float sh, se;
-    {
-        sh = __fadd_rn(ph, loh);
-        const float bb = __fsub_rn(sh, ph);
-        se = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bb)), __fsub_rn(loh, bb));
-    }
-    const float sl = __fadd_rn(se, __fadd_rn(pl, lol));
-    const float h = __fadd_rn(sh, sl);
-    return make_float2(h, __fsub_rn(sl, __fsub_rn(h, sh)));
-}
-
 // util.rescale (util.py:110-140) of the raw fBm pair sums to [lo, hi], and
 // the initial state (h as a pair, water0 as a pair | 0, 0, 0, 0) in the
 // buffer the planet's first iteration reads: B[iters & 1].  The reference
@@ -814,14 +863,15 @@ __device__ __forceinline__ float2 init_height(float2 r, float4 c, float loh, flo
 // (x - min) * f + lo with f = (hi - lo) / (max - min) formed once per
 // planet in binary64 (min and max are exact as binary64) and the per-vertex
 // arithmetic in pairs, within ~2^-47 of the value.  A constant field
-// (max == min) gives NaN, as the reference's division does.  Dynamic shared
-// memory: a float4 per planet when np <= INIT_SMEM_PLANETS, else none.
+// (max == min) gives NaN, as the reference's division does.  Rows from row0
+// (256-aligned) to total.  Dynamic shared memory: a float4 per planet when
+// np <= INIT_SMEM_PLANETS, else none.
 __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_planet *__restrict__ P, int np,
                                                            const float2 *__restrict__ raw,
                                                            const unsigned long long *__restrict__ minmax,
                                                            double lo, double hi, float w0h, float w0l,
                                                            float4 *__restrict__ st0, float4 *__restrict__ st1,
-                                                           int64_t total)
+                                                           int64_t row0, int64_t total)
 {
     extern __shared__ float4 s_ic[];
     const bool staged = np <= INIT_SMEM_PLANETS;
@@ -830,7 +880,7 @@ __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_plan
         __syncthreads();
     }
     const float loh = (float)lo, lol = (float)(lo - (double)(float)lo);
-    int64_t base = (int64_t)blockIdx.x * WALK_UNIT;
+    int64_t base = row0 + (int64_t)blockIdx.x * WALK_UNIT;
     if (base + threadIdx.x >= total) return;
     PlanetWalk W;
     W.seek(P, np, base + threadIdx.x);
@@ -865,18 +915,6 @@ __global__ void __launch_bounds__(256) erosion_init_kernel(const nx_erosion_plan
             dst[2 * x + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
     }
-}
-
-// v * 2^K as a binary64 (exact) by integer operations when v is a normal
-// binary32 and the result's exponent is in range; otherwise through the
-// binary64 pipe.
-__device__ __forceinline__ double f32_scaled(float v, int K)
-{
-    const uint32_t u = __float_as_uint(v);
-    const int e = (int)((u >> 23) & 0xFFu);
-    const int E = e + (1023 - 127) + K;
-    if (e == 0 || e == 255 || E <= 0 || E >= 2047) return ldexp((double)v, K);
-    return __hiloint2double((int)((u & 0x80000000u) | ((uint32_t)E << 20) | ((u & 0x7FFFFFu) >> 3)), (int)(u << 29));
 }
 
 // Heights of every planet after its run: (h_hi + h_lo) * 2^K in binary64,
@@ -1110,15 +1148,18 @@ static int tb_prepare()
 // whether the descriptors' tiling fields may be read at all (the
 // single-planet entry points build descriptors without a tiling and pass 0,
 // so their runs never depend on those fields).
-static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
-                     float *st_dev, float *st_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace,
-                     size_t ws_bytes, cudaStream_t s, bool allow_tb)
+// How a batch runs: validated sizes, and whether it runs temporally blocked
+// (every eroding planet has a tiling and nothing per iteration -- mass
+// sums, flow bits -- is requested).
+struct BatchPlan {
+    bool tb = false;
+    int R = 0, maxnl = 0, maxc = 0, max_it = 0;
+    int64_t total = 0, nblk = 0, ntiles_all = 0;
+};
+
+static int plan_batch(const nx_erosion_planet *planets_host, int np, bool allow_tb, BatchPlan &pl)
 {
-    if (np <= 0) return NX_OK;
-    if (!planets_dev || !planets_host || !st_dev || !st_tmp || !workspace)
-        return nx::fail(NX_EINVAL, "erosion: null pointer");
-    int max_it = 0;
-    int64_t total = 0, nblk = 0;
+    pl = BatchPlan();
     for (int p = 0; p < np; ++p) {
         const nx_erosion_planet &P = planets_host[p];
         if (P.vbeg < 0 || P.n < 0 || P.iters < 0 || P.slot != p || P.t_start != 0)
@@ -1126,19 +1167,15 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         if (P.n > 0 && (!P.nbr || !P.edge)) return nx::fail(NX_EINVAL, "erosion: planet %d has no mesh", p);
         if (p > 0 && P.iters > planets_host[p - 1].iters)
             return nx::fail(NX_EINVAL, "erosion: planets must be ordered by non-increasing iterations");
-        if (P.iters > max_it) max_it = P.iters;
-        if (P.vbeg + P.n > total) total = P.vbeg + P.n;
-        nblk += planet_blocks(P);
+        if (P.iters > pl.max_it) pl.max_it = P.iters;
+        if (P.vbeg + P.n > pl.total) pl.total = P.vbeg + P.n;
+        pl.nblk += planet_blocks(P);
     }
-    // temporally blocked when every planet has a tiling and nothing per
-    // iteration (mass sums, flow bits) is requested
-    bool tb = allow_tb && !mass_dev && !flow_dev && g_tb_enabled;
-    int R = 0, maxnl = 0, maxc = 0;
-    int64_t ntiles_all = 0;
+    bool tb = allow_tb && g_tb_enabled;
     for (int p = 0; p < np && tb; ++p) {
         const nx_erosion_planet &P = planets_host[p];
         if (P.iters == 0) {
-            if (P.tiling && P.ntiles > 0) ntiles_all += P.ntiles;
+            if (P.tiling && P.ntiles > 0) pl.ntiles_all += P.ntiles;
             continue;
         }
         if (!P.tiling || P.ntiles <= 0 || P.maxnl <= 0) { tb = false; break; }
@@ -1148,17 +1185,37 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         if (g_tb_variant == 3 && P.maxc > g_tb_threads)
             return nx::fail(NX_EINVAL, "erosion: planet %d: tiles of %d updatable vertices exceed %d threads (variant 3)",
                             p, P.maxc, g_tb_threads);
-        ntiles_all += P.ntiles;
-        if (P.maxnl > maxnl) maxnl = P.maxnl;
-        if (P.maxc > maxc) maxc = P.maxc;
+        pl.ntiles_all += P.ntiles;
+        if (P.maxnl > pl.maxnl) pl.maxnl = P.maxnl;
+        if (P.maxc > pl.maxc) pl.maxc = P.maxc;
     }
-    if (maxnl == 0) tb = false;
+    if (pl.maxnl == 0) tb = false;
     if (tb) {
-        R = g_tb_rings;
+        pl.R = g_tb_rings;
         int rc = tb_prepare();
         if (rc) return rc;
-        if (tb_launch_smem(maxnl, maxc) > (g_tb_variant == 2 ? TB_SMEM_MAX : 200 * 1024)) tb = false;
+        if (tb_launch_smem(pl.maxnl, pl.maxc) > (g_tb_variant == 2 ? TB_SMEM_MAX : 200 * 1024)) tb = false;
     }
+    pl.tb = tb;
+    return NX_OK;
+}
+
+// fuse (blocked path only): the fusion fields of TbArgs (raw sums and
+// rescale constants for the planets' first passes).
+static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host, int np,
+                     float *st_dev, float *st_tmp, double *mass_dev, uint16_t *flow_dev, void *workspace,
+                     size_t ws_bytes, cudaStream_t s, bool allow_tb, const TbArgs *fuse = nullptr)
+{
+    if (np <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !st_dev || !st_tmp || !workspace)
+        return nx::fail(NX_EINVAL, "erosion: null pointer");
+    BatchPlan pl;
+    int rc = plan_batch(planets_host, np, allow_tb && !mass_dev && !flow_dev, pl);
+    if (rc) return rc;
+    const bool tb = pl.tb;
+    const int R = pl.R, maxnl = pl.maxnl, maxc = pl.maxc, max_it = pl.max_it;
+    const int64_t nblk = pl.nblk, ntiles_all = pl.ntiles_all;
+    if (fuse && !tb) return nx::fail(NX_EINVAL, "erosion: fused steps need the blocked path");
     if (tb) {
         if (ws_bytes < nx_erosion_workspace_size((ntiles_all > nblk ? ntiles_all : nblk) * BLOCK, np))
             return nx::fail(NX_EINVAL, "erosion: workspace too small");
@@ -1180,6 +1237,14 @@ static int run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_plan
         ta.st0 = (float4 *)st_dev;
         ta.st1 = (float4 *)st_tmp;
         ta.ctl = w.ctl;
+        if (fuse) {
+            ta.raw = fuse->raw;
+            ta.minmax = fuse->minmax;
+            ta.elo = fuse->elo;
+            ta.ehi = fuse->ehi;
+            ta.w0h = fuse->w0h;
+            ta.w0l = fuse->w0l;
+        }
         const size_t smem = tb_launch_smem(maxnl, maxc);
         for (int q = 0; q < maxpass; ++q) {
             int64_t grid = 0;
@@ -1471,7 +1536,7 @@ NX_EXPORT int nx_erosion_init_batch(const nx_erosion_planet *planets_dev, const 
     const size_t smem = nplanets <= INIT_SMEM_PLANETS ? sizeof(float4) * (size_t)nplanets : 0;
     erosion_init_kernel<<<walk_grid(total), 256, smem, (cudaStream_t)stream>>>(
         planets_dev, nplanets, (const float2 *)raw_dev, minmax_dev, elev_lo, elev_hi, w0h, w0l, (float4 *)st_dev,
-        (float4 *)st_tmp_dev, total);
+        (float4 *)st_tmp_dev, 0, total);
     NX_CHECK_LAUNCH("erosion_init_kernel");
     nx::note_launch(1);
     return NX_OK;
@@ -1493,6 +1558,64 @@ NX_EXPORT int nx_erosion_heights_batch(const nx_erosion_planet *planets_dev, con
     NX_CHECK_LAUNCH("erosion_heights_kernel");
     nx::note_launch(1);
     return NX_OK;
+}
+
+// The batch after its fBm in one call: rescale, erosion, heights.  On the
+// blocked path the rescale runs in each eroding planet's first pass (its
+// load phase reads the raw sums), so the starting state is never written to
+// HBM; planets without iterations (the last ones of the non-increasing
+// order) get their state from one rescale launch.  Otherwise the rescale
+// runs as its own kernel first.  The heights kernel follows either way.
+NX_EXPORT int nx_erosion_run_batch(const nx_erosion_planet *planets_dev, const nx_erosion_planet *planets_host,
+                                   int nplanets, const float *raw_dev, const unsigned long long *minmax_dev,
+                                   double elev_lo, double elev_hi, double water0, float *st_dev, float *st_tmp_dev,
+                                   double *heights_dev, void *workspace, size_t ws_bytes, void *stream)
+{
+    if (nplanets <= 0) return NX_OK;
+    if (!planets_dev || !planets_host || !raw_dev || !minmax_dev || !st_dev || !st_tmp_dev || !heights_dev ||
+        !workspace)
+        return nx::fail(NX_EINVAL, "nx_erosion_run_batch: null pointer");
+    if ((uintptr_t)raw_dev & 7u) return nx::fail(NX_EINVAL, "nx_erosion_run_batch: raw pairs must be 8-byte aligned");
+    int64_t total = 0;
+    int rc = check_packed(planets_host, nplanets, &total);
+    if (rc) return rc;
+    BatchPlan pl;
+    rc = plan_batch(planets_host, nplanets, true, pl);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!pl.tb) {
+        rc = nx_erosion_init_batch(planets_dev, planets_host, nplanets, raw_dev, minmax_dev, elev_lo, elev_hi, water0,
+                                   st_dev, st_tmp_dev, stream);
+        if (rc) return rc;
+        rc = run_batch(planets_dev, planets_host, nplanets, st_dev, st_tmp_dev, nullptr, nullptr, workspace, ws_bytes, s,
+                       true);
+        if (rc) return rc;
+        return nx_erosion_heights_batch(planets_dev, planets_host, nplanets, st_dev, workspace, heights_dev, stream);
+    }
+    const float w0h = (float)water0, w0l = (float)(water0 - (double)w0h);
+    int dry = nplanets;
+    while (dry > 0 && planets_host[dry - 1].iters == 0) --dry;
+    if (dry < nplanets && total > planets_host[dry].vbeg) {
+        const int nd = nplanets - dry;
+        const int64_t row0 = planets_host[dry].vbeg;
+        const size_t smem = nd <= INIT_SMEM_PLANETS ? sizeof(float4) * (size_t)nd : 0;
+        erosion_init_kernel<<<walk_grid(total - row0), 256, smem, s>>>(
+            planets_dev + dry, nd, (const float2 *)raw_dev, minmax_dev + 2 * dry, elev_lo, elev_hi, w0h, w0l,
+            (float4 *)st_dev, (float4 *)st_tmp_dev, row0, total);
+        NX_CHECK_LAUNCH("erosion_init_kernel");
+        nx::note_launch(1);
+    }
+    TbArgs f;
+    f.raw = (const float2 *)raw_dev;
+    f.minmax = minmax_dev;
+    f.elo = elev_lo;
+    f.ehi = elev_hi;
+    f.w0h = w0h;
+    f.w0l = w0l;
+    rc = run_batch(planets_dev, planets_host, nplanets, st_dev, st_tmp_dev, nullptr, nullptr, workspace, ws_bytes, s,
+                     true, &f);
+    if (rc) return rc;
+    return nx_erosion_heights_batch(planets_dev, planets_host, nplanets, st_dev, workspace, heights_dev, stream);
 }
 
 // ---------------------------------------------------------------------------

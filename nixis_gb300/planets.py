@@ -240,17 +240,14 @@ class PlanetBatch:
         np_ = len(self.requests)
         self.minmax.copy_(self.minmax0)
         call("nx_fbm_batch", _dev.ptr(self.fb_dev), ctypes.cast(self.fb_host, ctypes.c_void_p), np_, None, s)
-        call("nx_erosion_init_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
-             _dev.ptr(self.raw), _dev.ptr(self.minmax), float(self.requests[0].elev_lo),
-             float(self.requests[0].elev_hi), float(self.requests[0].water0), _dev.ptr(self.st),
-             _dev.ptr(self.st_tmp), s)
         call("nx_erosion_ctl_init", _dev.ptr(self.ws), self.ws.numel(), np_, s)
         if self.blocked:
             _autotune.apply(self.tb)
-        call("nx_erosion_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
-             _dev.ptr(self.st), _dev.ptr(self.st_tmp), None, _dev.ptr(self.ws), self.ws.numel(), s)
-        call("nx_erosion_heights_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
-             _dev.ptr(self.st), _dev.ptr(self.ws), _dev.ptr(self.heights), s)
+        # rescale (fused into the planets' first blocked passes), erosion, heights
+        call("nx_erosion_run_batch", _dev.ptr(self.er_dev), ctypes.cast(self.er_host, ctypes.c_void_p), np_,
+             _dev.ptr(self.raw), _dev.ptr(self.minmax), float(self.requests[0].elev_lo),
+             float(self.requests[0].elev_hi), float(self.requests[0].water0), _dev.ptr(self.st),
+             _dev.ptr(self.st_tmp), _dev.ptr(self.heights), _dev.ptr(self.ws), self.ws.numel(), s)
         for g in self.inso_groups:
             call("nx_insolation_batch", _dev.ptr(g["dev"]), ctypes.cast(g["host"], ctypes.c_void_p),
                  len(g["members"]), _dev.ptr(g["table"]), g["nre"], g["pairs"], g["n_tilt"], _dev.ptr(self.inso), s)
@@ -323,6 +320,11 @@ class PlanetBatch:
     def kernels_per_run(self):
         blocked = any(self.er_host[j].tiling for j in range(len(self.requests)))
         extra = (2 if self.max_iters > 0 else 0)       # block map + rebase
+        if blocked:
+            # fBm, the passes (rescale fused into the first), heights, and
+            # one rescale launch for the planets without iterations
+            dry = any(r.erosion_iters == 0 and r.n_vertices > 0 for r in self.requests)
+            return 2 + int(dry) + self.erosion_launches() + extra + len(self.inso_groups)
         return 3 + self.erosion_launches() + extra + len(self.inso_groups)
 
     def fields(self, i):

@@ -49,6 +49,28 @@ def test_batched_equals_plain_bit_exact_and_graph_replay():
     assert torch.equal(one.results()[0].heights, h0[4])
 
 
+def test_fused_and_separate_steps_agree():
+    """The blocked batch rescales inside each planet's first erosion pass and
+    writes the heights from its last one (planets without iterations from
+    one rescale launch); the unblocked batch runs rescale, iterations and
+    heights as separate kernels.  Heights and final state agree bit for
+    bit."""
+    from nixis_gb300 import mesh, planets
+    reqs = small_requests()
+    cache = mesh.MeshCache()
+    fused = planets.PlanetBatch(reqs, cache)
+    fused.heights.fill_(float("nan"))
+    fused.run()
+    sep = planets.PlanetBatch(reqs, cache, blocked=False)
+    sep.run()
+    torch.cuda.synchronize()
+    assert any(r.erosion_iters == 0 for r in reqs) and any(r.erosion_iters > 0 for r in reqs)
+    for i, (x, y) in enumerate(zip(fused.results(), sep.results())):
+        assert torch.equal(x.heights, y.heights), reqs[i]
+        for f, g in zip(fused.fields(i), sep.fields(i)):
+            assert torch.equal(f, g), reqs[i]
+
+
 def test_run_to_host_pipelines_copies_of_every_run():
     from nixis_gb300 import mesh, planets
     reqs = small_requests()
