@@ -29,6 +29,8 @@
 //    with masks per region; hash prefixes of the fixed slots are shared.
 #include "nx_common.cuh"
 
+#include <vector>
+
 #include <cmath>
 
 namespace {
@@ -1206,13 +1208,50 @@ __device__ __forceinline__ int chunk_planet(const nx_fbm_planet *P, int np, int 
     return lo;
 }
 
+// Chunk ranges of a batched launch: block b takes chunks [first[b],
+// first[b + 1]) in order, the ranges cut so that each block gets an equal
+// share of the estimated cost (vertices x octaves, renormalised octaves
+// weighted 9/8).
+constexpr int FBM_SPLIT_MAX = 2048;
+struct FbmSplit {
+    int first[FBM_SPLIT_MAX + 1];
+};
+
+// Fold the ordered keys (kmn, kmx) of the block's sums of planet P into its
+// min/max (a block barrier; the whole block calls it).
+__device__ __forceinline__ void fold_minmax(const nx_fbm_planet &P, unsigned long long kmn, unsigned long long kmx,
+                                            unsigned long long (*s_mm)[8])
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long a = __shfl_xor_sync(0xFFFFFFFFu, kmn, o);
+        const unsigned long long b = __shfl_xor_sync(0xFFFFFFFFu, kmx, o);
+        kmn = a < kmn ? a : kmn;
+        kmx = b > kmx ? b : kmx;
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { s_mm[0][w] = kmn; s_mm[1][w] = kmx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a0 = s_mm[0][0], a1 = s_mm[1][0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            a0 = s_mm[0][k] < a0 ? s_mm[0][k] : a0;
+            a1 = s_mm[1][k] > a1 ? s_mm[1][k] : a1;
+        }
+        atomicMin(&P.minmax[0], a0);
+        atomicMax(&P.minmax[1], a1);
+    }
+    __syncthreads();
+}
+
 // Many planets in one persistent launch: work items are chunks of CHUNK
-// vertices of one planet, handed out round-robin; a block rebuilds its
-// shared table when its next chunk belongs to another planet.  Sums are
-// pairs (pair path above); each chunk also folds the ordered keys of its
-// sums into the planet's min/max (for the rescale to metres that follows).
+// vertices of one planet; each block walks its contiguous range of chunks
+// (so it meets few planets), rebuilding its shared table when the planet
+// changes.  Sums are pairs (pair path above); the ordered keys of a block's
+// sums of a planet are folded into the planet's min/max once, when the
+// block leaves the planet (for the rescale to metres that follows).
 __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__restrict__ planets, int np,
-                                                        int total_chunks, unsigned long long *nfb_out)
+                                                        const __grid_constant__ FbmSplit split,
+                                                        unsigned long long *nfb_out)
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ unsigned long long s_mm[2][8];
@@ -1220,20 +1259,25 @@ __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__r
     init_grad_table();
     __syncthreads();
     const uint32_t lb = lane_base(smem);
+    const int c0 = split.first[blockIdx.x], c1 = split.first[blockIdx.x + 1];
     int cur = -1;
     unsigned nfb = 0;
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        const int p = chunk_planet(planets, np, c);
-        const nx_fbm_planet &P = planets[p];
+    unsigned long long kmn = ~0ull, kmx = 0ull;
+    for (int c = c0; c < c1; ++c) {
+        int p = cur < 0 ? chunk_planet(planets, np, c) : cur;
+        while (p + 1 < np && planets[p + 1].chunk0 <= c) ++p;
         if (p != cur) {
+            if (cur >= 0 && planets[cur].minmax) fold_minmax(planets[cur], kmn, kmx, s_mm);
+            kmn = ~0ull;
+            kmx = 0ull;
             __syncthreads();
-            build_table_pair(smem, P.perm, P.pgi);
+            build_table_pair(smem, planets[p].perm, planets[p].pgi);
             __syncthreads();
             cur = p;
         }
+        const nx_fbm_planet &P = planets[p];
         const int64_t base = (int64_t)(c - P.chunk0) * CHUNK;
         const bool pow2 = P.pow2 != 0;
-        unsigned long long kmn = ~0ull, kmx = 0ull;
         for (int64_t i = base + threadIdx.x; i < base + CHUNK && i < P.n; i += blockDim.x) {
             const double X = P.xyz[3 * i], Y = P.xyz[3 * i + 1], Z = P.xyz[3 * i + 2];
             float x1, x2, x3, y1, y2, y3, z1, z2, z3;
@@ -1257,28 +1301,8 @@ __global__ void __launch_bounds__(256) fbm_batch_kernel(const nx_fbm_planet *__r
             kmn = k < kmn ? k : kmn;
             kmx = k > kmx ? k : kmx;
         }
-        if (P.minmax) {
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long a = __shfl_xor_sync(0xFFFFFFFFu, kmn, o);
-                const unsigned long long b = __shfl_xor_sync(0xFFFFFFFFu, kmx, o);
-                kmn = a < kmn ? a : kmn;
-                kmx = b > kmx ? b : kmx;
-            }
-            const int w = threadIdx.x >> 5;
-            if ((threadIdx.x & 31) == 0) { s_mm[0][w] = kmn; s_mm[1][w] = kmx; }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                unsigned long long a0 = s_mm[0][0], a1 = s_mm[1][0];
-                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-                    a0 = s_mm[0][k] < a0 ? s_mm[0][k] : a0;
-                    a1 = s_mm[1][k] > a1 ? s_mm[1][k] : a1;
-                }
-                atomicMin(&P.minmax[0], a0);
-                atomicMax(&P.minmax[1], a1);
-            }
-            __syncthreads();
-        }
     }
+    if (cur >= 0 && planets[cur].minmax) fold_minmax(planets[cur], kmn, kmx, s_mm);
     if (nfb_out) {
         unsigned tot = __reduce_add_sync(0xFFFFFFFFu, nfb);
         if ((threadIdx.x & 31) == 0 && tot) atomicAdd(nfb_out, (unsigned long long)tot);
@@ -1598,7 +1622,35 @@ NX_EXPORT int nx_fbm_batch(const nx_fbm_planet *planets_dev, const nx_fbm_planet
     int rc = configure_smem();
     if (rc) return rc;
     int grid = grid_for((int64_t)total * 256, 256, (const void *)fbm_batch_kernel, TABLE_BYTES);
-    fbm_batch_kernel<<<grid, 256, TABLE_BYTES, (cudaStream_t)stream>>>(planets_dev, nplanets, total, n_fallback_dev);
+    if (grid > FBM_SPLIT_MAX) grid = FBM_SPLIT_MAX;
+    // cut the chunks into grid ranges of equal estimated cost: a planet's
+    // chunk costs its vertices x (8 per octave + 1 per renormalised octave)
+    std::vector<int64_t> wchunk(nplanets), cum(nplanets + 1, 0);
+    for (int p = 0; p < nplanets; ++p) {
+        const nx_fbm_planet &P = planets_host[p];
+        const uint32_t live = P.n_octaves >= 32 ? ~0u : ((1u << P.n_octaves) - 1u);
+        wchunk[p] = 8 * (int64_t)P.n_octaves + (int64_t)__builtin_popcount(P.norm_mask & live);
+        cum[p + 1] = cum[p] + wchunk[p] * P.n;
+    }
+    FbmSplit split;
+    const int64_t tot = cum[nplanets];
+    int p = 0;
+    split.first[0] = 0;
+    for (int b = 1; b <= grid; ++b) {
+        if (b == grid || tot == 0) { split.first[b] = total; continue; }
+        // first chunk whose cost prefix reaches b * tot / grid
+        const int64_t t = (int64_t)((__int128)tot * b / grid);
+        while (p + 1 < nplanets && cum[p + 1] <= t) ++p;
+        const nx_fbm_planet &P = planets_host[p];
+        const int64_t per = wchunk[p] * CHUNK;
+        int64_t k = per > 0 ? (t - cum[p] + per - 1) / per : 0;
+        const int64_t nch = (P.n + CHUNK - 1) / CHUNK;
+        if (k > nch) k = nch;
+        int c = P.chunk0 + (int)k;
+        if (c < split.first[b - 1]) c = split.first[b - 1];
+        split.first[b] = c;
+    }
+    fbm_batch_kernel<<<grid, 256, TABLE_BYTES, (cudaStream_t)stream>>>(planets_dev, nplanets, split, n_fallback_dev);
     NX_CHECK_LAUNCH("fbm_batch_kernel");
     nx::note_launch(1);
     return NX_OK;
