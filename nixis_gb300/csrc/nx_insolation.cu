@@ -60,18 +60,40 @@ __device__ __forceinline__ float general_term(float x, float y, float z, float i
 // Tilts whose per-day constants a block stages in shared memory (16 B each).
 constexpr int TILT_STAGE_MAX = 2048;
 
-// Per-day constants of the factored pair sum: (|cos tau|, |sin tau| / |cos
-// tau| or -1 when |cos tau| < 2^-20, HP sin tau, sin tau).
+// Per-day constants of the factored pair sum, (|cos tau|, |sin tau| / |cos
+// tau|, HP sin tau, 0); days with |cos tau| < 2^-20 (the direct form) get
+// zeros, which add nothing to the factored sum, and are listed after the
+// days (day indices as ints, their count in entry n_tilt.y); entry n_tilt.x
+// holds the sum of HP sin tau over the factored days (day order, binary64,
+// rounded once), so a vertex adds its days' C terms as one product.
+// Shared memory: tilt_smem(a).
 template <int HP>
 __device__ __forceinline__ void stage_tilts(const InsoArgs &a, float4 *tt)
 {
     for (int d = threadIdx.x; d < a.n_tilt; d += blockDim.x) {
         const float2 t = a.tilt[d];
         const float ak = fabsf(t.x);
-        tt[d] = make_float4(ak, ak >= 0x1p-20f ? __fdiv_rn(fabsf(t.y), ak) : -1.0f, (float)HP * t.y, t.y);
+        tt[d] = ak >= 0x1p-20f ? make_float4(ak, __fdiv_rn(fabsf(t.y), ak), (float)HP * t.y, 0.0f)
+                               : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int *direct = reinterpret_cast<int *>(tt + a.n_tilt + 1);
+        double sc = 0.0;
+        int nd = 0;
+        for (int d = 0; d < a.n_tilt; ++d) {
+            const float4 k = tt[d];
+            if (k.x > 0.0f) sc += (double)k.z;
+            else direct[nd++] = d;
+        }
+        tt[a.n_tilt] = make_float4((float)sc, __int_as_float(nd), 0.0f, 0.0f);
     }
     __syncthreads();
 }
+
+// Days per group of the staged sum: a group's days accumulate in paired
+// lanes (one FFMA2 per day), the groups are added with compensation.
+constexpr int DAY_GROUP = 8;
 
 template <int HP>
 __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double Y, double Z, double r, float inv_r,
@@ -98,34 +120,53 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
         }
         if (tt) {
             // constants staged by the block: per day a shared load, one
-            // multiply for the threshold and the max / add of each pair
+            // multiply for the threshold, the max / add of each pair and one
+            // paired multiply-add into the group's lanes; the days' C terms
+            // come in at the end as z times their staged sum, the (rare)
+            // direct-form days after the others
             const float az = fabsf(z);
-            for (int d = 0; d < a.n_tilt; ++d) {
+            auto day = [&](int d, float2 g) {
                 const float4 k = tt[d];
-                float s;
-                if (k.y >= 0.0f) {
-                    const float c = az * k.y;
-                    float2 acc = make_float2(0.0f, 0.0f);
+                const float c = az * k.y;
+                float2 acc = make_float2(fmaxf(c, au[0]), fmaxf(c, au[1]));
 #pragma unroll
-                    for (int h = 0; h < (HP > 0 ? HP : 2); h += 2)
-                        acc = __fadd2_rn(acc, make_float2(fmaxf(c, au[h]), fmaxf(c, au[h + 1])));
-                    s = fmaf(k.x, acc.x + acc.y, z * k.z);
-                } else {
-                    const float2 t = a.tilt[d];
-                    const float A = x * t.x, B = -(y * t.x), C = z * t.y, aC = fabsf(C);
-                    s = 0.0f;
-#pragma unroll
-                    for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
-                        const float2 q = a.rot[h];
-                        s += fmaxf(aC, fabsf(fmaf(A, q.x, B * q.y)));
-                    }
-                    s = fmaf((float)HP, C, s);
-                }
-                float yk = s - comp;
-                float tk = tot + yk;
+                for (int h = 2; h < (HP > 0 ? HP : 2); h += 2)
+                    acc = __fadd2_rn(acc, make_float2(fmaxf(c, au[h]), fmaxf(c, au[h + 1])));
+                return __ffma2_rn(make_float2(k.x, k.x), acc, g);
+            };
+            auto add = [&](float s) {
+                const float yk = s - comp;
+                const float tk = tot + yk;
                 comp = (tk - tot) - yk;
                 tot = tk;
+            };
+            const int full = a.n_tilt - a.n_tilt % DAY_GROUP;
+            for (int d0 = 0; d0 < full; d0 += DAY_GROUP) {
+                float2 g = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int j = 0; j < DAY_GROUP; ++j) g = day(d0 + j, g);
+                add(g.x + g.y);
             }
+            if (full < a.n_tilt) {
+                float2 g = make_float2(0.0f, 0.0f);
+                for (int d = full; d < a.n_tilt; ++d) g = day(d, g);
+                add(g.x + g.y);
+            }
+            const float4 e = tt[a.n_tilt];
+            const int nd = __float_as_int(e.y);
+            const int *direct = reinterpret_cast<const int *>(tt + a.n_tilt + 1);
+            for (int i = 0; i < nd; ++i) {
+                const float2 t = a.tilt[direct[i]];
+                const float A = x * t.x, B = -(y * t.x), C = z * t.y, aC = fabsf(C);
+                float s = 0.0f;
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
+                    const float2 q = a.rot[h];
+                    s += fmaxf(aC, fabsf(fmaf(A, q.x, B * q.y)));
+                }
+                add(fmaf((float)HP, C, s));
+            }
+            add(z * e.x);
             return tot * inv_r;
         }
         for (int d = 0; d < a.n_tilt; ++d) {
@@ -377,7 +418,8 @@ __global__ void __launch_bounds__(256) surface_temp_kernel(const double *__restr
 // Dynamic shared memory of the 12-pair kernels: the staged tilt constants.
 size_t tilt_smem(const InsoArgs &a)
 {
-    return (a.pairs && a.n_tilt <= TILT_STAGE_MAX) ? sizeof(float4) * (size_t)a.n_tilt : 0;
+    return (a.pairs && a.n_tilt <= TILT_STAGE_MAX) ? sizeof(float4) * ((size_t)a.n_tilt + 1) + sizeof(int) * (size_t)a.n_tilt
+                                                   : 0;
 }
 
 int grid_for(int64_t n)

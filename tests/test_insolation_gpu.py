@@ -79,6 +79,25 @@ def test_annual_sum_random_vertices_and_schedules():
     assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
 
 
+def test_schedule_with_vertical_tilts_takes_the_direct_form():
+    """Days with |cos tilt| < 2^-20 (tilt +-90) leave the factored per-day
+    sum for the direct form; mixed with ordinary days (a full group of 8
+    days and a remainder), against the binary64 sum of the reference's
+    terms."""
+    from nixis_gb300 import climate
+    rng = np.random.default_rng(11)
+    u = rng.normal(size=(20000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    rot, _ = climate.annual_schedule(23.44, 365, 1, 24)
+    tilts = [23.44, 90.0, 10.0, -90.0, 0.0, 45.0, 89.99, -23.44, 90.0, 5.0, -60.0]
+    got = climate.insolation_sum(u, 1.0, rot, tilts).cpu().numpy()
+    ref = np.zeros(len(u), np.float64)
+    for t in tilts:
+        for r in rot:
+            O.sample_insolation(ref, u, 1.0, r, t)
+    assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
+
+
 def test_vertices_off_the_sphere_use_the_general_formula():
     from nixis_gb300 import climate
     rng = np.random.default_rng(10)
