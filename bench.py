@@ -514,6 +514,16 @@ def bench_ours(args):
         torch.cuda.empty_cache()
         serving = run_serving(args.serve_requests)
 
+    # single-planet configurations with per-field errors against binary64
+    # (divisions 250 / 8 octaves; divisions 1000 / 12 octaves + 50 erosion
+    # iterations), outside every timed region
+    singles = None
+    if rank == 0 and world == 1 and not args.no_cpu and not args.no_single:
+        import gc
+        gc.collect()
+        torch.cuda.empty_cache()
+        singles = {c: single_planet(c) for c in ("c1", "c2")}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = run_cpu_baseline(reqs, budget_s=args.cpu_budget)
@@ -530,10 +540,48 @@ def bench_ours(args):
                 "plain_per_planet": plain, "plain_blocked_per_planet": plain_blocked,
                 "ratio_vs_plain": value / (plain["value"] * world),
                 "ratio_vs_plain_blocked": value / (plain_blocked["value"] * world),
-                "errors_vs_fp64": errors}
+                "errors_vs_fp64": errors, "single_planets": singles}
+        # the figures a reader needs first, last on the line and compact
+        line["summary"] = summary(line)
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def summary(line):
+    """Compact digest of the line's comparisons: batch vs the plain paths,
+    serving (p50/p99, planets/s, results equal), errors against binary64,
+    every kernel's roofline fraction."""
+    g = lambda x, n=4: None if x is None else float(f"{x:.{n}g}")
+    out = {"planets_per_s": g(line["value"]), "e2e": g(line["e2e"]["value"]),
+           "plain": g(line["plain_per_planet"]["value"]), "plain_blocked": g(line["plain_blocked_per_planet"]["value"]),
+           "ratio_vs_plain": g(line["ratio_vs_plain"], 3), "ratio_vs_plain_blocked": g(line["ratio_vs_plain_blocked"], 3),
+           "batch_equals_plain": line["plain_per_planet"].get("batch_equals_plain")}
+    rf = line.get("roofline") or {}
+    out["roofline_frac"] = {k: g(v.get("frac"), 3) for k, v in (rf.get("kernels") or {}).items()}
+    sv = line.get("serving")
+    if sv:
+        out["serving"] = {"requests": sv["requests"]}
+        for mode in ("arrivals", "all_at_once"):
+            m = sv[mode]
+            out["serving"][mode] = {p: [g(m[p]["p50_ms"]), g(m[p]["p99_ms"]), g(m[p]["planets_per_s"])]
+                                    for p in ("engine", "plain")}
+            out["serving"][mode]["equal"] = m["results_equal_plain"]
+        out["serving"]["fields"] = "[p50 ms, p99 ms, planets/s]"
+    er = line.get("errors_vs_fp64")
+    if er:
+        out["batch_vs_fp64_max_rel_h"] = g(er["max_rel_h"], 3)
+    sp = line.get("single_planets")
+    if sp:
+        c1, c2 = sp.get("c1") or {}, sp.get("c2") or {}
+        out["c1_elevation_max_err_m"] = g(c1.get("elevation_max_err_m"), 3)
+        e50 = (c2.get("erosion_errors") or {}).get(50)
+        if e50:
+            out["c2_50_iters_vs_fp64"] = {f: [g(e50[f]["max_abs_over_max"], 3), g(e50[f]["rms_over_max"], 3)]
+                                          for f in "hws"}
+            out["c2_50_iters_vs_fp64"]["fields"] = "[max, rms] / max|field|"
+            out["c2_flow_choice_flips"] = e50.get("flow_choice_flips")
+    return out
 
 
 def fp32_peak_tflops(sm_mhz, fma=True):
@@ -751,11 +799,17 @@ def _time(fn, reps=3):
 
 
 def bench_single(name):
+    """Print the single-planet line of `name` (see single_planet)."""
+    print(json.dumps(single_planet(name)))
+
+
+def single_planet(name):
     """c1: divisions 250, 8 octaves, seed 0, metres (float64);
     c2: divisions 1000, 12 octaves, seed 1, then 50 erosion iterations from
         water 1e-3, sediment 0 (errors per field vs binary64 at 1/10/50);
     c3: divisions 2500, 12 octaves, seed 2, 200 erosion iterations, and
-        mean annual insolation over 365 days x 24 hours."""
+        mean annual insolation over 365 days x 24 hours.
+    Returns the configuration's figures as a dict."""
     import torch
     from oracle import oracle as O
     from nixis_gb300 import mesh, terrain, erosion, climate, planets
@@ -788,8 +842,7 @@ def bench_single(name):
     hg = O.rescale(h, -8000.0, 8000.0)
     line["elevation_max_err_m"] = float(np.abs(hg - hm).max())
     if name == "c1":
-        print(json.dumps(line))
-        return
+        return line
     iters = 50 if name == "c2" else 200
     nbr = m.nbr.cpu().numpy()
     hm_t = torch.from_numpy(hm).cuda()
@@ -858,7 +911,7 @@ def bench_single(name):
         ref_i = O.annual_insolation(pts[idx], 1.0)
         line["insolation_max_err_over_max"] = float(np.abs(got - ref_i).max() / np.abs(ref_i).max())
         line["mean_toa_wm2_range"] = [float(1361 * got.min() / 8760), float(1361 * got.max() / 8760)]
-    print(json.dumps(line))
+    return line
 
 
 def bench_mesh_prep(args):
@@ -918,6 +971,8 @@ def main():
                     help="with --profile: one launch per erosion iteration instead of blocked passes")
     ap.add_argument("--serve", type=int, default=0, help="serving comparison on the first N stream requests, exit")
     ap.add_argument("--serve-requests", type=int, default=2000, help="stream requests in the default line's serving leg")
+    ap.add_argument("--no-single", action="store_true",
+                    help="skip the single-planet error block (c1, c2 against binary64) of the default line")
     ap.add_argument("--mesh-prep", action="store_true",
                     help="time the workload's mesh and tiling builds (CUDA events), print one line, exit")
     args = ap.parse_args()

@@ -195,7 +195,9 @@ int nx_edge_lengths(const double *xyz_dev, const int32_t *nbr_dev, int64_t nv, f
                     void *stream);
 
 /* Tiling of a mesh for temporally blocked erosion: every vertex belongs to
- * one tile (a tile_side x tile_side square of its home face's grid); each
+ * one tile of its home face's grid -- for tile > 0 a tile x tile square,
+ * for tile < 0 a hexagon of the grid points within graph distance -tile
+ * (2..64) of a centre (hexagons carry fewer halo vertices per member); each
  * tile lists its members, then `rings` rings of neighbours (local numbering),
  * and, for members and rings 1..rings-1, the six neighbours as local
  * indices and the six edge lengths. */
@@ -210,8 +212,9 @@ typedef struct nx_tiling {
     const float *ledge;        /* ntiles x cmax x 6 edge lengths, (hi, lo) pairs */
 } nx_tiling;
 
-/* Host: sizes of the tiling of divisions k. */
-int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax);
+/* Host: sizes of the tiling of divisions k (tile: square side, or minus
+ * the hexagon radius). */
+int nx_tiling_shape(int k, int tile, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax);
 
 /* Build a tiling from the mesh's neighbour table and edge lengths into
  * caller buffers sized by nx_tiling_shape (counts int32[ntiles*(rings+1)],
@@ -219,7 +222,7 @@ int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *n
  * float[ntiles*cmax*6*2]).  err_dev (device int[3], caller zeroes it):
  * [0] bit 0 = a tile exceeded nmax members, bit 1 = a halo or neighbour
  * problem; [1] largest local vertex count; [2] largest updatable count. */
-int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nbr_dev, const float *edge_dev,
+int nx_tiling_build(int k, int tile, int rings, const int32_t *nbr_dev, const float *edge_dev,
                     int32_t *counts_dev, int32_t *ids_dev, uint16_t *lnbr_dev, float *ledge_dev, int *err_dev,
                     void *stream);
 

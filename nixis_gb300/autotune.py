@@ -1,8 +1,11 @@
 """Autotuner for the temporally blocked erosion kernel.
 
-Four knobs set how the blocked erosion maps onto the GPU: the tile side
-(tiles are side x side squares of a face grid; bigger tiles waste less work
-on halo rings but need more shared memory per block), the rings per pass
+Four knobs set how the blocked erosion maps onto the GPU: the tile shape
+and size (side x side squares of a face grid, or hexagons of the grid
+points within a radius of a centre -- labelled h<radius> and stored as
+tile_side = -radius; bigger tiles waste less work on halo rings but need
+more shared memory per block, and a hexagon has the fewest halo vertices
+for its size), the rings per pass
 (iterations done in shared memory between trips to HBM; more rings mean
 fewer trips but wider halos), the threads per block, and the kernel
 variant: 0 reads the tile tables (neighbour indices, edge lengths) from
@@ -36,6 +39,7 @@ SMEM_LIMIT = 200 * 1024          # dynamic shared memory of variants 0 and 1
 SMEM_LIMIT_TABLES = 226 * 1024   # of variant 2 (the opt-in limit less static shared memory, rounded down)
 ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
 SIDES = (16, 20, 24, 28, 32, 40, 48)
+HEX_RADII = (14, 16, 17, 18, 19, 20, 21, 22)   # hexagonal tiles (tile_side = -radius)
 RINGS = (2, 3, 4, 5)
 THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2), (512, 3), (1024, 3),
            (256, 4), (320, 4), (384, 4), (640, 4), (256, 5))
@@ -60,7 +64,8 @@ class TbConfig:
 
     @property
     def label(self):
-        return f"{self.tile_side}/{self.rings}/{self.threads}" + SUFFIX[self.variant]
+        tile = f"h{-self.tile_side}" if self.tile_side < 0 else str(self.tile_side)
+        return f"{tile}/{self.rings}/{self.threads}" + SUFFIX[self.variant]
 
 
 def smem_bytes(cfg, maxnl, maxc):
@@ -140,13 +145,15 @@ def store(key, cfg, timings=None, path=None):
 
 
 def parse(label):
-    """TbConfig from its label side/rings/threads, 'p' appended for variant
-    1 (prefetch), 's' for variant 2 (tables in shared memory), 'o' for
-    variant 3 (one vertex per thread), 'd' and 'e' for variants 4 and 5
-    (more resident blocks per SM)."""
+    """TbConfig from its label side/rings/threads (side 'h<r>' for
+    hexagons of radius r), 'p' appended for variant 1 (prefetch), 's' for
+    variant 2 (tables in shared memory), 'o' for variant 3 (one vertex per
+    thread), 'd' and 'e' for variants 4 and 5 (more resident blocks per
+    SM)."""
     side, rings, thr = label.split("/")
     v = {"p": 1, "s": 2, "o": 3, "d": 4, "e": 5}.get(thr[-1], 0)
-    return TbConfig(int(side), int(rings), int(thr.rstrip("psode")), v)
+    tile = -int(side[1:]) if side.startswith("h") else int(side)
+    return TbConfig(tile, int(rings), int(thr.rstrip("psode")), v)
 
 
 def current():
@@ -171,10 +178,11 @@ def use(cfg):
 
 
 def candidates(mesh, variants=DEFAULT_VARIANTS):
-    """Every (side, rings, threads, variant) whose tiles may fit the shared
-    memory (checked again against the built tiling's counts)."""
+    """Every (tile, rings, threads, variant) whose tiles may fit the shared
+    memory (checked again against the built tiling's counts): squares of
+    SIDES and hexagons of HEX_RADII."""
     out = []
-    for side in SIDES:
+    for side in SIDES + tuple(-r for r in HEX_RADII):
         for rings in RINGS:
             nt, nm, cm = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
             try:

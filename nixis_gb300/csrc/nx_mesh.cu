@@ -7,6 +7,10 @@
 // the reference's two functions for any consistently wound triangle mesh, so
 // the neighbour table equals what the reference computes from the same
 // triangles.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
 #include "nx_common.cuh"
 
 namespace nx {
@@ -535,6 +539,132 @@ __global__ void tile_assign_kernel(int k, int B, int64_t nv, int R, int nmax, in
     }
 }
 
+}  // namespace
+
+// Hexagonal tiles.  On the face grid's lattice (neighbours (+-1, 0),
+// (0, +-1), (+1, -1), (-1, +1)) the vertices within graph distance rho of a
+// point c, max(|i - ci|, |j - cj|, |i + j - ci - cj|) <= rho, form a hexagon
+// of N = 3 rho^2 + 3 rho + 1 points, and these hexagons tile the lattice
+// exactly with centres c = m a + n b, a = (2 rho + 1, -rho), b = (rho,
+// rho + 1) (det [a b] = N).  A hexagon is the set with the fewest vertices
+// within R of it for its size, so hexagonal tiles carry fewer halo vertices
+// per member than squares.  Per face the tiles are the (m, n) whose hexagon
+// meets the face triangle {i, j >= 0, i + j <= k}; for each m these form one
+// run of n, numbered row by row.
+constexpr int HEX_ROWS_MAX = 1024;
+struct HexRows {
+    int rho, N;
+    int m0, nrows;          // rows m = m0 .. m0 + nrows - 1
+    int per_face;           // tiles per face
+    int nlo[HEX_ROWS_MAX];  // first n of each row
+    int base[HEX_ROWS_MAX + 1];   // local index of each row's first tile; base[nrows] = per_face
+};
+
+static inline int hex_points(int r) { return 3 * r * r + 3 * r + 1; }
+
+// Whether the hexagon of radius rho centred at (ci, cj) holds a point of
+// the face triangle: integer i, j with |i - ci|, |j - cj|, |i + j - ci - cj|
+// <= rho and i, j >= 0, i + j <= k.  Every sum between ilo + jlo and
+// ihi + jhi is reachable, so the box and the sum band must overlap.
+static bool hex_meets_face(long long ci, long long cj, int rho, int k)
+{
+    const long long ilo = std::max(ci - rho, 0LL), ihi = std::min(ci + rho, (long long)k);
+    const long long jlo = std::max(cj - rho, 0LL), jhi = std::min(cj + rho, (long long)k);
+    const long long slo = std::max(ci + cj - rho, 0LL), shi = std::min(ci + cj + rho, (long long)k);
+    return ilo <= ihi && jlo <= jhi && slo <= shi && std::max(slo, ilo + jlo) <= std::min(shi, ihi + jhi);
+}
+
+// Host: the row table of hexagonal tiles of radius rho on divisions k.
+static int hex_rows(int k, int rho, HexRows &H)
+{
+    H.rho = rho;
+    H.N = hex_points(rho);
+    // lattice coordinates of a grid point: (m, n) = [a b]^-1 (i, j) =
+    // ((rho + 1) i - rho j, rho i + (2 rho + 1) j) / N; over the triangle's
+    // corners, widened by one centre on every side
+    const double N = H.N;
+    const double cm[3] = {0.0, (rho + 1.0) * k / N, -(double)rho * k / N};
+    const double cn[3] = {0.0, (double)rho * k / N, (2.0 * rho + 1.0) * k / N};
+    const int mlo = (int)std::floor(std::min(cm[0], std::min(cm[1], cm[2]))) - 2;
+    const int mhi = (int)std::ceil(std::max(cm[0], std::max(cm[1], cm[2]))) + 2;
+    const int nlo = (int)std::floor(std::min(cn[0], std::min(cn[1], cn[2]))) - 2;
+    const int nhi = (int)std::ceil(std::max(cn[0], std::max(cn[1], cn[2]))) + 2;
+    H.nrows = 0;
+    H.m0 = 0;
+    int total = 0;
+    for (int m = mlo; m <= mhi; ++m) {
+        int first = INT_MAX, last = INT_MIN;
+        for (int n = nlo; n <= nhi; ++n) {
+            const long long ci = (long long)m * (2 * rho + 1) + (long long)n * rho;
+            const long long cj = -(long long)m * rho + (long long)n * (rho + 1);
+            if (hex_meets_face(ci, cj, rho, k)) {
+                if (first == INT_MAX) first = n;
+                else if (n != last + 1)
+                    return nx::fail(NX_EINVAL, "hexagonal tiling: row %d of divisions %d is not one run", m, k);
+                last = n;
+            }
+        }
+        if (first == INT_MAX) {
+            if (H.nrows > 0) break;      // past the last row
+            continue;
+        }
+        if (H.nrows == 0) H.m0 = m;
+        else if (m != H.m0 + H.nrows)
+            return nx::fail(NX_EINVAL, "hexagonal tiling: rows of divisions %d are not contiguous", k);
+        if (H.nrows >= HEX_ROWS_MAX)
+            return nx::fail(NX_EINVAL, "hexagonal tiling: more than %d rows (divisions %d, radius %d)", HEX_ROWS_MAX, k, rho);
+        H.nlo[H.nrows] = first;
+        H.base[H.nrows] = total;
+        total += last - first + 1;
+        ++H.nrows;
+    }
+    H.base[H.nrows] = total;
+    H.per_face = total;
+    return total > 0 ? NX_OK : nx::fail(NX_EINVAL, "hexagonal tiling: no tiles");
+}
+
+namespace {
+
+__device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((b - 1 - a) / b); }
+
+// Tile of a grid point: the centre within rho is one of the four lattice
+// points at the floors of its lattice coordinates and their +1 neighbours.
+__device__ __forceinline__ int64_t hex_tile_of(int f, int i, int j, const HexRows &H)
+{
+    const int rho = H.rho;
+    const int m0 = floor_div((rho + 1) * i - rho * j, H.N), n0 = floor_div(rho * i + (2 * rho + 1) * j, H.N);
+    for (int q = 0; q < 4; ++q) {
+        const int m = m0 + (q & 1), n = n0 + (q >> 1);
+        const int di = i - (m * (2 * rho + 1) + n * rho), dj = j - (-m * rho + n * (rho + 1));
+        if (max(abs(di), max(abs(dj), abs(di + dj))) <= rho) {
+            const int r = m - H.m0;
+            if (r < 0 || r >= H.nrows) return -1;
+            const int loc = H.base[r] + n - H.nlo[r];
+            if (n < H.nlo[r] || loc >= H.base[r + 1]) return -1;
+            return (int64_t)f * H.per_face + loc;
+        }
+    }
+    return -1;
+}
+
+__global__ void tile_assign_hex_kernel(int k, int64_t nv, int R, int nmax, int32_t *__restrict__ counts,
+                                       int32_t *__restrict__ ids, int *__restrict__ err,
+                                       const __grid_constant__ HexRows H)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        int f, i, j;
+        home_of(v, k, f, i, j);
+        const int64_t t = hex_tile_of(f, i, j, H);
+        if (t < 0) {
+            atomicOr(err, 2);
+            continue;
+        }
+        const int pos = atomicAdd(&counts[t * (R + 1)], 1);
+        if (pos < nmax) ids[t * nmax + pos] = (int32_t)v;
+        else atomicOr(err, 1);
+    }
+}
+
 // Per-tile hash set of vertex ids in shared memory: 2^bits entries, the
 // smallest power of two with at least twice the tile's local bound (load
 // factor <= 1/2), linear probing.
@@ -749,11 +879,42 @@ __global__ void __launch_bounds__(512) tile_rings_kernel(const int32_t *__restri
 
 static_assert(sizeof(nx_tiling) == 48, "tiling descriptor layout");
 
-NX_EXPORT int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax)
+// Local and updatable capacities of tiles whose members lie within graph
+// distance `reach` of a point or square (see nx_tiling_shape).
+static int tile_caps(int64_t nm, int64_t cm, int32_t *nmax, int32_t *cmax)
 {
-    if (k < 1 || tile_side < 2 || rings < 1 || rings > 8 || !ntiles || !nmax || !cmax)
+    cm = (cm + 3) & ~(int64_t)3;                     // cm*12 B: 16-byte units
+    if (cm > nm) cm = nm & ~(int64_t)3;
+    if (nm > 4096) return nx::fail(NX_EINVAL, "nx_tiling_shape: tile too large (%lld local vertices)", (long long)nm);
+    *nmax = (int32_t)nm;
+    *cmax = (int32_t)cm;
+    return NX_OK;
+}
+
+NX_EXPORT int nx_tiling_shape(int k, int tile, int rings, int32_t *ntiles, int32_t *nmax, int32_t *cmax)
+{
+    if (k < 1 || rings < 1 || rings > 8 || !ntiles || !nmax || !cmax || (tile >= 0 && tile < 2) || tile < -64 ||
+        tile == -1)
         return nx::fail(NX_EINVAL, "nx_tiling_shape: bad arguments");
-    const int M = k / tile_side;
+    if (tile < 0) {
+        // hexagons of radius rho: the vertices within R of a tile lie within
+        // rho + R of its centre (on the flat lattice of a face and across an
+        // edge onto the next face; around the twelve five-neighbour corners
+        // the count only drops), at most hex_points(rho + R); 6(rho + R) of
+        // slack as for squares
+        const int rho = -tile;
+        HexRows H;
+        int rc = hex_rows(k, rho, H);
+        if (rc) return rc;
+        const int64_t nt = (int64_t)20 * H.per_face;
+        if (nt > 0x7FFFFFFF) return nx::fail(NX_EINVAL, "nx_tiling_shape: too many tiles");
+        rc = tile_caps(hex_points(rho + rings) + 6 * (rho + rings), hex_points(rho + rings - 1) + 6 * (rho + rings - 1),
+                       nmax, cmax);
+        if (rc) return rc;
+        *ntiles = (int32_t)nt;
+        return NX_OK;
+    }
+    const int M = k / tile;
     const int64_t nt = (int64_t)20 * (M + 1) * (M + 2) / 2;
     // A tile holds at most B x B members of one face grid.  On the lattice
     // of the face grids (six neighbours: (+-1, 0), (0, +-1), (+1, -1),
@@ -762,24 +923,20 @@ NX_EXPORT int nx_tiling_shape(int k, int tile_side, int rings, int32_t *ntiles, 
     // (B + 2R)^2; at the twelve five-neighbour corners the count only drops.
     // The bounds keep 4(B + 2R) of slack (overflow is still detected and
     // reported by the build); the updatable set (rings below R) uses R - 1.
-    const int64_t B = tile_side, D = B + 2 * (int64_t)rings, Dc = D - 2;
-    int64_t nm = D * D + 4 * D;
-    int64_t cm = (Dc * Dc + 4 * Dc + 3) & ~(int64_t)3;   // cm*12 B: 16-byte units
-    if (cm > nm) cm = nm & ~(int64_t)3;
-    if (nm > 4096) return nx::fail(NX_EINVAL, "nx_tiling_shape: tile too large (%lld local vertices)", (long long)nm);
+    const int64_t B = tile, D = B + 2 * (int64_t)rings, Dc = D - 2;
     if (nt > 0x7FFFFFFF) return nx::fail(NX_EINVAL, "nx_tiling_shape: too many tiles");
+    const int rc = tile_caps(D * D + 4 * D, Dc * Dc + 4 * Dc, nmax, cmax);
+    if (rc) return rc;
     *ntiles = (int32_t)nt;
-    *nmax = (int32_t)nm;
-    *cmax = (int32_t)cm;
     return NX_OK;
 }
 
-NX_EXPORT int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nbr_dev, const float *edge_dev,
+NX_EXPORT int nx_tiling_build(int k, int tile, int rings, const int32_t *nbr_dev, const float *edge_dev,
                               int32_t *counts_dev, int32_t *ids_dev, uint16_t *lnbr_dev, float *ledge_dev, int *err_dev,
                               void *stream)
 {
     int32_t nt = 0, nmax = 0, cmax = 0;
-    int rc = nx_tiling_shape(k, tile_side, rings, &nt, &nmax, &cmax);
+    int rc = nx_tiling_shape(k, tile, rings, &nt, &nmax, &cmax);
     if (rc) return rc;
     if (!nbr_dev || !edge_dev || !counts_dev || !ids_dev || !lnbr_dev || !ledge_dev || !err_dev)
         return nx::fail(NX_EINVAL, "nx_tiling_build: null pointer");
@@ -789,8 +946,16 @@ NX_EXPORT int nx_tiling_build(int k, int tile_side, int rings, const int32_t *nb
     const int64_t nv = (int64_t)10 * k * k + 2;
     cudaStream_t s = (cudaStream_t)stream;
     NX_CHECK_CUDA(cudaMemsetAsync(counts_dev, 0, sizeof(int32_t) * (size_t)nt * (rings + 1), s));
-    tile_assign_kernel<<<grid1d(nv), 256, 0, s>>>(k, tile_side, nv, rings, nmax, counts_dev, ids_dev, err_dev);
-    NX_CHECK_LAUNCH("tile_assign_kernel");
+    if (tile < 0) {
+        HexRows H;
+        rc = hex_rows(k, -tile, H);
+        if (rc) return rc;
+        tile_assign_hex_kernel<<<grid1d(nv), 256, 0, s>>>(k, nv, rings, nmax, counts_dev, ids_dev, err_dev, H);
+        NX_CHECK_LAUNCH("tile_assign_hex_kernel");
+    } else {
+        tile_assign_kernel<<<grid1d(nv), 256, 0, s>>>(k, tile, nv, rings, nmax, counts_dev, ids_dev, err_dev);
+        NX_CHECK_LAUNCH("tile_assign_kernel");
+    }
     int P2 = 1;
     while (P2 < nmax) P2 <<= 1;
     // hash keys + values, the local list (padded for sorting) and a scratch

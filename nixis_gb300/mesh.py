@@ -19,7 +19,8 @@ _tables_done = set()
 _lock = threading.Lock()
 
 # temporally blocked erosion: tiles are TILE_SIDE x TILE_SIDE squares of a
-# face grid with TILE_RINGS halo rings (passes of up to TILE_RINGS iterations)
+# face grid (a negative tile_side: hexagons of radius -tile_side) with
+# TILE_RINGS halo rings (passes of up to TILE_RINGS iterations)
 TILE_SIDE = 40
 TILE_RINGS = 4
 

@@ -18,6 +18,7 @@ def test_cache_round_trip_and_bad_entries(tmp_path):
     assert A.parse("24/4/512s") == A.TbConfig(24, 4, 512, 2) and A.parse("16/3/1024o") == A.TbConfig(16, 3, 1024, 3)
     assert A.parse(A.TbConfig(48, 2, 1024, 0).label) == A.TbConfig(48, 2, 1024, 0)
     assert A.parse("24/4/256d") == A.TbConfig(24, 4, 256, 4) and A.parse("20/5/256e") == A.TbConfig(20, 5, 256, 5)
+    assert A.parse("h19/4/384d") == A.TbConfig(-19, 4, 384, 4) and A.TbConfig(-19, 4, 384, 4).label == "h19/4/384d"
     assert A.parse(A.TbConfig(24, 3, 384, 4).label) == A.TbConfig(24, 3, 384, 4)
     # variants 4 / 5 fit only where their blocks per SM can reside
     assert A.fits(A.TbConfig(24, 4, 256, 4), 1024, 900) and not A.fits(A.TbConfig(40, 4, 256, 4), 2304, 2116)
@@ -62,7 +63,7 @@ def test_candidates_cover_the_default_and_fit_the_limits():
     assert A.DEFAULT in c
     assert {cfg.variant for cfg in c} == set(A.DEFAULT_VARIANTS)
     for cfg in c:
-        assert cfg.tile_side in A.SIDES and cfg.rings in A.RINGS
+        assert (cfg.tile_side in A.SIDES or -cfg.tile_side in A.HEX_RADII) and cfg.rings in A.RINGS
         assert (cfg.threads, cfg.variant) in A.THREADS
     # variants 4 and 5 only where their resident blocks' shared memory fits
     assert not A.fits(A.TbConfig(48, 4, 256, 5), (48 + 8) ** 2, (48 + 6) ** 2)

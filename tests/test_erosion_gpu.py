@@ -242,11 +242,14 @@ def test_bad_neighbour_id_is_reported_not_faulted():
         erosion.erosion_iteration3(pts, bad, g["ero_k6_smooth_h0"].copy(), np.full(len(pts), 1e-3), np.zeros(len(pts)))
 
 
-def test_tiling_covers_every_vertex_once_with_valid_rings():
+@pytest.mark.parametrize("tile", [40, -19, -5])
+def test_tiling_covers_every_vertex_once_with_valid_rings(tile):
+    """Squares of side 40 and hexagons of radius 19 and 5 (many tiles on
+    face edges and around the five-neighbour corners)."""
     from nixis_gb300 import mesh
-    for k in (3, 17, 100):
+    for k in (1, 3, 17, 100):
         m = mesh.PlanetMesh(k)
-        t = m.tiling()
+        t = m.tiling(tile)
         R = t.rings
         cnt = t.counts.view(t.ntiles, R + 1).cpu().numpy()
         ids = t.ids.view(t.ntiles, t.nmax).cpu().numpy()
@@ -288,14 +291,16 @@ def test_temporally_blocked_batch_equals_iteration_at_a_time(rain):
         assert torch.equal(x.heights, planets.generate_plain(r, cache).heights), r
 
 
-@pytest.mark.parametrize("rain", [0.0, 0.3 / 320])
-def test_larger_meshes_blocked_equal_iteration_at_a_time(rain):
+@pytest.mark.parametrize("rain,tile", [(0.0, None), (0.3 / 320, None), (0.3 / 320, -19), (0.0, -6)])
+def test_larger_meshes_blocked_equal_iteration_at_a_time(rain, tile):
     """Meshes of divisions 160-339 (many tiles per face, tiles away from
     every face edge), pass counts with a short last pass and both parities:
-    blocked == one launch per iteration, bit for bit, no error flags."""
+    blocked == one launch per iteration, bit for bit, no error flags; with
+    the default tiles and with hexagons of radius 19 and 6."""
+    from dataclasses import replace
     from nixis_gb300 import autotune, mesh, planets
     from nixis_gb300.planets import PlanetRequest
-    tb = autotune.DEFAULT
+    tb = autotune.DEFAULT if tile is None else replace(autotune.DEFAULT, tile_side=tile)
     reqs = [PlanetRequest(seed=s, divisions=k, octaves=7, erosion_iters=it, rain=rain)
             for s, (k, it) in enumerate([(200, 9), (250, 14), (339, 33), (160, 6), (300, 1)])]
     cache = mesh.MeshCache()

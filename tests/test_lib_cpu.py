@@ -7,6 +7,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 import golden_io
 
@@ -84,3 +85,50 @@ def test_host_only_entry_points_reject_bad_arguments():
     # passes of a blocked run: ceil(iters / 4) made to the parity of iters
     for it, want in ((0, 0), (1, 1), (4, 2), (5, 3), (8, 2), (9, 3), (100, 26), (101, 27)):
         assert L.nx_erosion_npass(it) == want, it
+
+
+def _hex_tiles_of_face(k, rho):
+    """Restatement of the hexagonal tiling's assignment: every grid point
+    (i, j) of a face triangle to the centre m a + n b (a = (2 rho + 1,
+    -rho), b = (rho, rho + 1)) within graph distance rho, searched among the
+    four lattice points at the floors of its lattice coordinates."""
+    N = 3 * rho * rho + 3 * rho + 1
+    I, J = np.meshgrid(np.arange(k + 1), np.arange(k + 1), indexing="ij")
+    keep = I + J <= k
+    I, J = I[keep], J[keep]
+    m0 = np.floor_divide((rho + 1) * I - rho * J, N)
+    n0 = np.floor_divide(rho * I + (2 * rho + 1) * J, N)
+    hits = np.zeros(len(I), int)
+    tile = np.zeros((len(I), 2), int)
+    for dm in (0, 1):
+        for dn in (0, 1):
+            m, n = m0 + dm, n0 + dn
+            di, dj = I - (m * (2 * rho + 1) + n * rho), J - (-m * rho + n * (rho + 1))
+            ok = np.maximum(np.maximum(abs(di), abs(dj)), abs(di + dj)) <= rho
+            hits += ok
+            tile[ok] = np.stack([m[ok], n[ok]], 1)
+    return hits, tile
+
+
+@pytest.mark.parametrize("rho", [2, 5, 14, 19, 22])
+def test_hexagonal_tiles_cover_each_face_point_once_and_are_all_used(rho):
+    """Hexagons of radius rho tile the face grid: each point has exactly one
+    centre among the four candidates the tiling kernel tries, and
+    nx_tiling_shape counts exactly the hexagons that receive points of the
+    face triangle (every tile is a block of the erosion launches; the one
+    or two per face that hold only points of an edge whose home is the
+    other face stay empty)."""
+    import ctypes
+    from nixis_gb300 import _lib
+    L = _lib.lib()
+    for k in (1, 2, 7, 40, 100, 333):
+        hits, tile = _hex_tiles_of_face(k, rho)
+        assert hits.min() == 1 and hits.max() == 1, (k, rho)
+        used = len({(int(a), int(b)) for a, b in tile})
+        nt, nm, cm = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        assert L.nx_tiling_shape(k, -rho, 4, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm)) == 0
+        assert nt.value == 20 * used, (k, rho)
+        R = 4
+        assert nm.value >= 3 * (rho + R) ** 2 + 3 * (rho + R) + 1 and cm.value % 4 == 0
+    for bad in (-1, -65, 0, 1):
+        assert L.nx_tiling_shape(100, bad, 4, ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(cm)) != 0
