@@ -39,7 +39,7 @@ SMEM_LIMIT = 200 * 1024          # dynamic shared memory of variants 0 and 1
 SMEM_LIMIT_TABLES = 226 * 1024   # of variant 2 (the opt-in limit less static shared memory, rounded down)
 ROW_SMEM = 40                    # bytes of shared memory per local vertex (two state rows + sediment)
 SIDES = (16, 20, 24, 28, 32, 40, 48)
-HEX_RADII = (14, 16, 17, 18, 19, 20, 21, 22)   # hexagonal tiles (tile_side = -radius)
+HEX_RADII = (14, 16, 17, 18, 19)   # hexagonal tiles (tile_side = -radius)
 RINGS = (2, 3, 4, 5)
 THREADS = ((256, 0), (512, 0), (1024, 0), (256, 1), (384, 1), (512, 2), (1024, 2), (512, 3), (1024, 3),
            (256, 4), (320, 4), (384, 4), (640, 4), (256, 5))
