@@ -95,9 +95,114 @@ __device__ __forceinline__ void stage_tilts(const InsoArgs &a, float4 *tt)
 // lanes (one FFMA2 per day), the groups are added with compensation.
 constexpr int DAY_GROUP = 8;
 
+// Schedules of up to SORT_MAX days are also summed by breakpoints.  With
+// c_d = |z| tan_d (tan_d = |tan tau_d|, cos_d = |cos tau_d|) and a_h = |U_h|,
+// the factored days' part of the year is
+//   sum_d cos_d sum_h max(c_d, a_h)
+//     = sum_h [ a_h sum_{d: c_d < a_h} cos_d + |z| sum_{d: c_d >= a_h} cos_d tan_d ],
+// exactly (each max picks one side).  With the days sorted by tan_d, both
+// inner sums are a prefix sum P0 and a suffix sum Q1 of the sorted days,
+// read at the count B_h of days with tan_d < a_h / |z|; a vertex then needs
+// twelve searches instead of a max and an add per pair and day.
+// Shared memory after the staged constants (floats): T[SP] the sorted tan_d
+// padded with +inf to a power of two SP > factored days (at least one +inf
+// sentinel), P0[nf + 1] and Q1[nf + 1] (binary64 sums rounded once), the
+// cos_d in sorted order, and a bucket index of SP + 1 ints: with tmax the
+// largest tan_d and NB = SP buckets of width tmax / NB, F[b] = the count of
+// days with tan_d < b tmax / NB (F[NB] = nf).  A search for t > tmax is nf;
+// otherwise it starts at F[b] for b = floor(t NB / tmax) and steps down
+// while the day below is not below t and up while the next day is below t
+// (a step or two: the buckets hold under one day on average), which ends
+// at the exact count whatever the rounding of b.
+constexpr int SORT_MAX = 512;
+
+__host__ __device__ __forceinline__ int sort_pad(int n)
+{
+    int p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+// Builds T, P0, Q1 from the staged constants (after stage_tilts); returns
+// the number of factored days.  Called by the whole block.
+__device__ __forceinline__ int stage_breakpoints(const InsoArgs &a, const float4 *tt, float *T, float *P0, float *Q1,
+                                                 float *CS, int *F, float &scale, float &tmax)
+{
+    const int nd = __float_as_int(tt[a.n_tilt].y);
+    const int nf = a.n_tilt - nd;
+    const int sp = sort_pad(nf + 1);
+    // rank sort of the factored days by (tan, day): position = how many
+    // factored days come before
+    for (int d = threadIdx.x; d < a.n_tilt; d += blockDim.x) {
+        const float4 k = tt[d];
+        if (!(k.x > 0.0f)) continue;
+        int rank = 0;
+        for (int e = 0; e < a.n_tilt; ++e) {
+            const float4 o = tt[e];
+            rank += (o.x > 0.0f && (o.y < k.y || (o.y == k.y && e < d))) ? 1 : 0;
+        }
+        T[rank] = k.y;
+        CS[rank] = k.x;
+    }
+    for (int j = nf + threadIdx.x; j < sp; j += blockDim.x) T[j] = __int_as_float(0x7F800000);
+    __syncthreads();
+    // prefix sums of cos and suffix sums of cos * tan, binary64, one warp:
+    // a lane sums its run of days, the runs are scanned across the warp
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const int per = (nf + 31) / 32;
+        const int j0 = min(nf, lane * per), j1 = min(nf, j0 + per);
+        double s0 = 0.0, s1 = 0.0;
+        for (int j = j0; j < j1; ++j) {
+            s0 += (double)CS[j];
+            s1 += (double)CS[j] * (double)T[j];
+        }
+        double e0 = s0, e1 = s1;                  // inclusive scan over the lanes
+        for (int o = 1; o < 32; o <<= 1) {
+            const double u0 = __shfl_up_sync(0xFFFFFFFFu, e0, o), u1 = __shfl_up_sync(0xFFFFFFFFu, e1, o);
+            if (lane >= o) { e0 += u0; e1 += u1; }
+        }
+        const double tot1 = __shfl_sync(0xFFFFFFFFu, e1, 31);
+        const double tot0 = __shfl_sync(0xFFFFFFFFu, e0, 31);
+        e0 -= s0;                                 // exclusive
+        e1 -= s1;
+        for (int j = j0; j < j1; ++j) {
+            P0[j] = (float)e0;
+            Q1[j] = (float)(tot1 - e1);
+            e0 += (double)CS[j];
+            e1 += (double)CS[j] * (double)T[j];
+        }
+        if (lane == 0) {
+            P0[nf] = (float)tot0;
+            Q1[nf] = 0.0f;
+        }
+    }
+    // the bucket index: F[b] by a binary search per bucket
+    tmax = nf > 0 ? T[nf - 1] : 0.0f;
+    scale = tmax > 0.0f ? (float)sp / tmax : 0.0f;
+    const float width = tmax / (float)sp;
+    for (int b = threadIdx.x; b <= sp; b += blockDim.x) {
+        if (b == sp) { F[b] = nf; continue; }
+        const float edge = (float)b * width;
+        int c = 0;
+        for (int step = sp >> 1; step > 0; step >>= 1) c += T[c + step - 1] < edge ? step : 0;
+        F[b] = c;
+    }
+    __syncthreads();
+    return nf;
+}
+
+// Breakpoint tables of a block (stage_breakpoints), or nf < 0 for none.
+struct Breaks {
+    const float *T = nullptr, *P0 = nullptr, *Q1 = nullptr;
+    const int *F = nullptr;
+    int nf = -1, sp = 0;       // factored days, buckets
+    float scale = 0.0f, tmax = 0.0f;
+};
+
 template <int HP>
 __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double Y, double Z, double r, float inv_r,
-                                             const float4 *tt = nullptr)
+                                             const float4 *tt = nullptr, const Breaks &bk = Breaks())
 {
     const double rho2 = X * X + Y * Y + Z * Z;
     const double r2 = r * r;
@@ -125,6 +230,44 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
             // come in at the end as z times their staged sum, the (rare)
             // direct-form days after the others
             const float az = fabsf(z);
+            auto add = [&](float s) {
+                const float yk = s - comp;
+                const float tk = tot + yk;
+                comp = (tk - tot) - yk;
+                tot = tk;
+            };
+            if (bk.nf >= 0) {
+                // B_h = number of sorted days with tan_d < a_h / |z|
+                // (|z| = 0: every day for a_h > 0, none for a_h = 0)
+                const float iz = 1.0f / az;
+                float th[HP > 0 ? HP : 2];
+                int B[HP > 0 ? HP : 2];
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
+                    th[h] = au[h] > 0.0f ? au[h] * iz : 0.0f;
+                    B[h] = 0;
+                }
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 2); ++h) {
+                    if (th[h] > bk.tmax) {
+                        B[h] = bk.nf;
+                    } else {
+                        const int b = min((int)(th[h] * bk.scale), bk.sp - 1);
+                        int c = bk.F[b];
+                        while (c > 0 && !(bk.T[c - 1] < th[h])) --c;
+                        while (c < bk.nf && bk.T[c] < th[h]) ++c;
+                        B[h] = c;
+                    }
+                }
+                float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+                for (int h = 0; h < (HP > 0 ? HP : 2); h += 2) {
+                    const int b0 = min(B[h], bk.nf), b1 = min(B[h + 1], bk.nf);
+                    s0 = fmaf(au[h], bk.P0[b0], fmaf(az, bk.Q1[b0], s0));
+                    s1 = fmaf(au[h + 1], bk.P0[b1], fmaf(az, bk.Q1[b1], s1));
+                }
+                tot = s0 + s1;
+            } else {
             auto day = [&](int d, float2 g) {
                 const float4 k = tt[d];
                 const float c = az * k.y;
@@ -133,12 +276,6 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
                 for (int h = 2; h < (HP > 0 ? HP : 2); h += 2)
                     acc = __fadd2_rn(acc, make_float2(fmaxf(c, au[h]), fmaxf(c, au[h + 1])));
                 return __ffma2_rn(make_float2(k.x, k.x), acc, g);
-            };
-            auto add = [&](float s) {
-                const float yk = s - comp;
-                const float tk = tot + yk;
-                comp = (tk - tot) - yk;
-                tot = tk;
             };
             const int full = a.n_tilt - a.n_tilt % DAY_GROUP;
             for (int d0 = 0; d0 < full; d0 += DAY_GROUP) {
@@ -152,6 +289,7 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
                 for (int d = full; d < a.n_tilt; ++d) g = day(d, g);
                 add(g.x + g.y);
             }
+            }   // days one by one
             const float4 e = tt[a.n_tilt];
             const int nd = __float_as_int(e.y);
             const int *direct = reinterpret_cast<const int *>(tt + a.n_tilt + 1);
@@ -252,15 +390,37 @@ __device__ __forceinline__ float inso_vertex(const InsoArgs &a, double X, double
     return tot;
 }
 
+// The block's breakpoint tables after the staged constants (see SORT_MAX).
 template <int HP>
-__global__ void __launch_bounds__(256) insolation_kernel(InsoArgs a)
+__device__ __forceinline__ Breaks stage_all(const InsoArgs &a, float4 *s_tilt)
+{
+    Breaks bk;
+    stage_tilts<HP>(a, s_tilt);
+    if (a.n_tilt <= SORT_MAX) {
+        float *base = reinterpret_cast<float *>(reinterpret_cast<int *>(s_tilt + a.n_tilt + 1) + a.n_tilt);
+        const int sp = sort_pad(a.n_tilt + 1);
+        float *T = base, *P0 = T + sp, *Q1 = P0 + a.n_tilt + 1, *CS = Q1 + a.n_tilt + 1;
+        int *F = reinterpret_cast<int *>(CS + a.n_tilt + 1);
+        bk.nf = stage_breakpoints(a, s_tilt, T, P0, Q1, CS, F, bk.scale, bk.tmax);
+        bk.sp = sort_pad(bk.nf + 1);
+        bk.F = F;
+        bk.T = T;
+        bk.P0 = P0;
+        bk.Q1 = Q1;
+    }
+    return bk;
+}
+
+template <int HP>
+__global__ void __launch_bounds__(256, 3) insolation_kernel(InsoArgs a)
 {
     extern __shared__ float4 s_tilt[];
     const bool staged = HP > 0 && a.pairs && a.n_tilt <= TILT_STAGE_MAX;
-    if (staged) stage_tilts<HP>(a, s_tilt);
+    Breaks bk;
+    if (staged) bk = stage_all<HP>(a, s_tilt);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
         float tot = inso_vertex<HP>(a, a.xyz[3 * i], a.xyz[3 * i + 1], a.xyz[3 * i + 2], a.r, a.inv_r,
-                                    staged ? s_tilt : nullptr);
+                                    staged ? s_tilt : nullptr, bk);
         a.out[i] = a.accumulate ? a.out[i] + tot : tot;
     }
 }
@@ -268,12 +428,13 @@ __global__ void __launch_bounds__(256) insolation_kernel(InsoArgs a)
 // Many planets: planet p's vertices fill packed rows [vbeg, vbeg + n)
 // (vbeg a multiple of 256); one block covers 256 rows of one planet.
 template <int HP>
-__global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const nx_inso_planet *__restrict__ P, int np,
+__global__ void __launch_bounds__(256, 3) insolation_batch_kernel(InsoArgs a, const nx_inso_planet *__restrict__ P, int np,
                                                                int64_t total_rows)
 {
     extern __shared__ float4 s_tilt[];
     const bool staged = HP > 0 && a.pairs && a.n_tilt <= TILT_STAGE_MAX;
-    if (staged) stage_tilts<HP>(a, s_tilt);
+    Breaks bk;
+    if (staged) bk = stage_all<HP>(a, s_tilt);
     for (int64_t blk = blockIdx.x; blk * 256 < total_rows; blk += gridDim.x) {
         const int64_t row = blk * 256 + threadIdx.x;
         int lo = 0, hi = np - 1;
@@ -286,7 +447,7 @@ __global__ void __launch_bounds__(256) insolation_batch_kernel(InsoArgs a, const
         if (i < 0 || i >= pl.n) continue;
         const double r = pl.radius;
         float tot = inso_vertex<HP>(a, pl.xyz[3 * i], pl.xyz[3 * i + 1], pl.xyz[3 * i + 2], r, (float)(1.0 / r),
-                                    staged ? s_tilt : nullptr);
+                                    staged ? s_tilt : nullptr, bk);
         a.out[row] = tot;
     }
 }
@@ -418,16 +579,28 @@ __global__ void __launch_bounds__(256) surface_temp_kernel(const double *__restr
 // Dynamic shared memory of the 12-pair kernels: the staged tilt constants.
 size_t tilt_smem(const InsoArgs &a)
 {
-    return (a.pairs && a.n_tilt <= TILT_STAGE_MAX) ? sizeof(float4) * ((size_t)a.n_tilt + 1) + sizeof(int) * (size_t)a.n_tilt
-                                                   : 0;
+    if (!a.pairs || a.n_tilt > TILT_STAGE_MAX) return 0;
+    size_t b = sizeof(float4) * ((size_t)a.n_tilt + 1) + sizeof(int) * (size_t)a.n_tilt;
+    if (a.n_tilt <= SORT_MAX)      // T (padded), P0, Q1, the sorted cosines, the bucket index
+        b += sizeof(float) * ((size_t)sort_pad(a.n_tilt + 1) + 3 * ((size_t)a.n_tilt + 1)) +
+             sizeof(int) * ((size_t)sort_pad(a.n_tilt + 1) + 1);
+    return b;
 }
 
-int grid_for(int64_t n)
+int grid_for(int64_t n, int per_sm = 8)
 {
     int64_t g = (n + 255) / 256;
-    int64_t cap = (int64_t)nx::sm_count() * 8;
+    int64_t cap = (int64_t)nx::sm_count() * per_sm;
     if (g > cap) g = cap;
     return (int)(g < 1 ? 1 : g);
+}
+
+// Blocks of a 12-pair launch: a block that sums by breakpoints sorts the
+// schedule first, so the grid is the resident blocks (3 per SM) and each
+// block takes many vertices.
+int grid_staged(int64_t n, const InsoArgs &a)
+{
+    return grid_for(n, a.pairs && a.n_tilt <= SORT_MAX ? 3 : 8);
 }
 
 }  // namespace
@@ -491,7 +664,7 @@ NX_EXPORT int nx_insolation(const double *xyz_dev, int64_t n, double radius, con
     a.out = out_dev;
     a.accumulate = accumulate;
     if (a.pairs && n_rot_entries == 12)
-        insolation_kernel<12><<<grid_for(n), 256, tilt_smem(a), s>>>(a);
+        insolation_kernel<12><<<grid_staged(n, a), 256, tilt_smem(a), s>>>(a);
     else
         insolation_kernel<0><<<grid_for(n), 256, 0, s>>>(a);
     NX_CHECK_LAUNCH("insolation_kernel");
@@ -526,7 +699,7 @@ NX_EXPORT int nx_insolation_batch(const nx_inso_planet *planets_dev, const nx_in
     a.out = out_dev;
     a.accumulate = 0;
     cudaStream_t s = (cudaStream_t)stream;
-    int grid = grid_for(total);
+    int grid = a.pairs && n_rot_entries == 12 ? grid_staged(total, a) : grid_for(total);
     if (a.pairs && n_rot_entries == 12)
         insolation_batch_kernel<12><<<grid, 256, tilt_smem(a), s>>>(a, planets_dev, nplanets, total);
     else
