@@ -142,6 +142,10 @@ class PlanetMesh:
         self.xyz = xyz
         self.nbr = nbr
         self.edge, eerr = edge_lengths(xyz, nbr, stream=stream)
+        # the whole mesh is ready here (an event of its own, so a later user
+        # need not wait for whatever else its stream has queued since)
+        self.built = torch.cuda.Event()
+        self.built.record(s)
         self._errs = (aerr, eerr)
         self._tilings = {}
         if not defer_checks:

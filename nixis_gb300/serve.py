@@ -336,8 +336,10 @@ class ServeEngine:
                 t.mesh = self.meshes.acquire(r.divisions)
                 t.tiling = (t.mesh.tiling(self.tb.tile_side, self.tb.rings, stream=self.side)
                             if self.blocked and r.erosion_iters > 0 else None)
-                t.mesh_done = torch.cuda.Event()
-                t.mesh_done.record(self.side)
+            # the events of the mesh's and tiling's own builds: a resident mesh
+            # is ready at once, not after the builds queued on the side stream
+            # since (a small planet does not wait for a large one's mesh)
+            t.mesh_done = t.tiling._ready if t.tiling is not None else t.mesh.built
             admitted.append(t)
         return admitted
 
@@ -396,15 +398,16 @@ class ServeEngine:
                      ctypes.c_void_p(self.st.data_ptr() + 32 * t.vbeg),
                      ctypes.c_void_p(self.st_tmp.data_ptr() + 32 * t.vbeg), s)
                 t._e_single = (e, e_dev)
-                # ready: its noise and state (this stream) and its mesh and
-                # tiling (side stream) are done
-                fs.wait_event(t.mesh_done)
+                # its noise and initial state are done at this event; the
+                # planet joins the ticks once this and its mesh and tiling
+                # (t.mesh_done) are done -- the noise stream does not wait for
+                # the mesh, so later planets' noise does not queue behind it
                 ev = torch.cuda.Event()
                 ev.record(fs)
                 t.ready_event = ev
                 t._keep = (tab_dev, mm_dev, fb_dev, fb)
                 if r.insolation:
-                    self._insolation(t, ev)
+                    self._insolation(t, t.mesh.xyz_ready)
                 if r.erosion_iters == 0:
                     t.stage = "output"
                     t.ready = t.eroded = time.perf_counter()
@@ -505,9 +508,10 @@ class ServeEngine:
         # planets whose mesh, noise and initial state are done join the
         # erosion at this tick (checked on the host without waiting)
         for t in self.active:
-            if t.stage == "waiting" and t.ready_event.query():
+            if t.stage == "waiting" and t.ready_event.query() and t.mesh_done.query():
                 t.mesh.check()
                 self.main.wait_event(t.ready_event)
+                self.main.wait_event(t.mesh_done)
                 t.stage = "eroding"
                 t.ready = time.perf_counter()
                 t.t_start = self.tick
