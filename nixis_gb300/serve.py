@@ -51,6 +51,7 @@ ALIGN = 256
 ROW_BYTES = 32 + 32 + 8 + 8 + 4      # state x2, raw pair sum, binary64 height, insolation
 COPY_THREADS = 4           # host threads that move one result array
 COPY_SPLIT = 1 << 20       # elements from which a result array is copied in slices
+SMALL_ROWS = 1 << 21       # planets with fewer vertices (divisions <= 457) set up on the high-priority streams
 HOST_PAGE = 4096           # unit of the page-locked result arena
 
 
@@ -267,6 +268,11 @@ class ServeEngine:
         self.main = torch.cuda.Stream()
         self.side = torch.cuda.Stream()            # meshes and tilings
         self.fbm_stream = torch.cuda.Stream()      # new planets' noise and initial state
+        # the same two for small planets, at a higher priority: their setup
+        # is scheduled ahead of the blocks of a large planet's mesh build or
+        # noise queued before them
+        self.side_small = torch.cuda.Stream(priority=-1)
+        self.fbm_small = torch.cuda.Stream(priority=-1)
         self.copy_stream = torch.cuda.Stream()     # results to the host
         self.inso_stream = torch.cuda.Stream()
         self.desc_dev = torch.empty(slots * ctypes.sizeof(ErosionPlanet), dtype=torch.uint8, device=dev)
@@ -332,9 +338,10 @@ class ServeEngine:
             t.vbeg = vbeg
             t.slot = self.free_slots.pop()
             t.admitted = time.perf_counter()
-            with torch.cuda.stream(self.side):
+            side = self.side_small if r.n_vertices < SMALL_ROWS else self.side
+            with torch.cuda.stream(side):
                 t.mesh = self.meshes.acquire(r.divisions)
-                t.tiling = (t.mesh.tiling(self.tb.tile_side, self.tb.rings, stream=self.side)
+                t.tiling = (t.mesh.tiling(self.tb.tile_side, self.tb.rings, stream=side)
                             if self.blocked and r.erosion_iters > 0 else None)
             # the events of the mesh's and tiling's own builds: a resident mesh
             # is ready at once, not after the builds queued on the side stream
@@ -347,8 +354,16 @@ class ServeEngine:
         """fBm + rescale + initial state of newly admitted planets, on their
         own stream: the noise needs only the vertices, so it starts as soon
         as they exist and overlaps the rest of a new mesh's build (adjacency,
-        edge lengths, tiling) on the side stream."""
-        fs = self.fbm_stream
+        edge lengths, tiling) on the side stream.  Small planets use the
+        higher-priority pair of streams."""
+        small = [t for t in new if t.request.n_vertices < SMALL_ROWS]
+        large = [t for t in new if t.request.n_vertices >= SMALL_ROWS]
+        if small:
+            self._launch_group(small, self.fbm_small)
+        if large:
+            self._launch_group(large, self.fbm_stream)
+
+    def _launch_group(self, new, fs):
         s = _dev.stream_handle(fs)
         n = len(new)
         for t in new:

@@ -98,6 +98,41 @@ def test_schedule_with_vertical_tilts_takes_the_direct_form():
     assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
 
 
+@pytest.mark.parametrize("days", [1, 512, 513, 700])
+def test_schedule_lengths_on_both_staged_paths(days):
+    """Schedules of up to 512 days are summed by breakpoints (days sorted by
+    |tan tilt|, per-vertex bucket lookups), longer ones day by day in groups
+    of 8; a year of 700 days, one of 513 and one of 512 (with ties of
+    |tan tilt| between days of opposite tilt) and a single day, against the
+    binary64 sum of the reference's terms."""
+    from nixis_gb300 import climate
+    rng = np.random.default_rng(days)
+    u = rng.normal(size=(20000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    u[:50, 2] = 0.0                     # on the equator: every threshold |z| |tan| is 0
+    u[:50] /= np.linalg.norm(u[:50], axis=1)[:, None]
+    got = climate.annual_insolation(u, 1.0, days=days, year_length=days, hours=24).cpu().numpy()
+    ref = O.annual_insolation(u, 1.0, axial_tilt=23.44, year_length=days, days=days, hours=24)
+    assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
+
+
+def test_zero_tilt_schedule_by_breakpoints():
+    """Every tilt 0 (all thresholds 0, an empty bucket range): the breakpoint
+    sum against the binary64 sum."""
+    from nixis_gb300 import climate
+    rng = np.random.default_rng(12)
+    u = rng.normal(size=(20000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    rot, _ = climate.annual_schedule(23.44, 365, 1, 24)
+    tilts = [0.0] * 40
+    got = climate.insolation_sum(u, 1.0, rot, tilts).cpu().numpy()
+    ref = np.zeros(len(u), np.float64)
+    for t in tilts:
+        for r in rot:
+            O.sample_insolation(ref, u, 1.0, r, t)
+    assert np.abs(got - ref).max() / np.abs(ref).max() <= INSO_TOL
+
+
 def test_vertices_off_the_sphere_use_the_general_formula():
     from nixis_gb300 import climate
     rng = np.random.default_rng(10)
