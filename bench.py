@@ -630,8 +630,9 @@ def measure_insolation(sm_mhz):
            "hbm": {"bytes_per_vertex": 28, "achieved_gbs": n * 28 / (ms / 1e3) / 1e9},
            "reference_model": {"flop_per_term": 6, "equivalent_tflops": terms * 6 / (ms / 1e3) / 1e12,
                                "fp32_peak_tflops": fp32_peak_tflops(sm_mhz),
-                               "note": "the survey's 6 FLOP per vertex x sun position; the kernel reaches the same "
-                                       "sums without per-term work (exact algebra, within 1e-5 of binary64 in tests)"}}
+                               "note": "6 FLOP per vertex x sun position, the reduced form of the reference's term; "
+                                       "the kernel reaches the same sums without per-term work (exact algebra, within "
+                                       "1e-5 of binary64 in tests)"}}
     peak_issue = 152 * 4 * sm_mhz * 1e6
     issue = os.path.join(ROOT, "profiles", "insolation_issue.json")
     try:

@@ -127,7 +127,7 @@ def gen_octaves(R):
     # (k, seed, n_oct, init_rough, init_strength, rough, persist, radius, with_elev)
     cases.append((5, 0, 8, 1.0, 1.0, 2.0, 0.5, 1.0, False))        # the 8-octave plain method
     cases.append((16, 1, 12, 1.0, 1.0, 2.0, 0.5, 1.0, False))      # 12 octaves
-    cases.append((8, 5, 7, 1.5, 0.4, 2.5, 0.5, 6378100.0, False))  # the driver's defaults, nixis.py:312-320
+    cases.append((8, 5, 7, 1.5, 0.4, 2.5, 0.5, 6378100.0, False))  # nixis.py's defaults, nixis.py:312-320
     cases.append((4, 9, 3, 1.0, 0.2, 2.0, 0.5, 1.0, True))         # accumulate into given elevations
     out = {}
     for ci, (k, seed, n_oct, f0, a0, lac, pers, radius, with_elev) in enumerate(cases):
