@@ -49,7 +49,7 @@ from ._lib import ErosionPlanet, FbmPlanet, call, lib
 
 ALIGN = 256
 ROW_BYTES = 32 + 32 + 8 + 8 + 4      # state x2, raw pair sum, binary64 height, insolation
-COPY_THREADS = 4           # host threads that move one result array
+COPY_THREADS = 8           # host threads that move a planet's result arrays
 COPY_SPLIT = 1 << 20       # elements from which a result array is copied in slices
 SMALL_ROWS = 1 << 21       # planets with fewer vertices (divisions <= 457) set up on the high-priority streams
 HOST_PAGE = 4096           # unit of the page-locked result arena
@@ -574,27 +574,32 @@ class ServeEngine:
                 still.append(f)
         self._delivering = still
 
-    def _copy_out(self, src):
-        """A page-locked tensor's contents as a new numpy array, copied in
-        slices by several host threads (numpy releases the GIL while it
-        copies): one thread does not reach the host's memory bandwidth, and
-        the copy is on the request's latency."""
-        a = src.numpy()
-        out = np.empty_like(a)
-        parts = COPY_THREADS if a.size >= COPY_SPLIT else 1
-        cuts = [a.size * q // parts for q in range(parts + 1)]
-        futs = [self._copy_pool.submit(np.copyto, out[b:e], a[b:e]) for b, e in zip(cuts[:-1], cuts[1:])]
+    def _copy_out(self, *srcs):
+        """Page-locked tensors' contents as new numpy arrays, copied in
+        slices by several host threads at once (numpy releases the GIL while
+        it copies): one thread does not reach the host's memory bandwidth,
+        and the copies are on the request's latency."""
+        outs, futs = [], []
+        for src in srcs:
+            a = src.numpy()
+            out = np.empty_like(a)
+            parts = COPY_THREADS if a.size >= COPY_SPLIT else 1
+            cuts = [a.size * q // parts for q in range(parts + 1)]
+            futs += [self._copy_pool.submit(np.copyto, out[b:e], a[b:e]) for b, e in zip(cuts[:-1], cuts[1:])]
+            outs.append(out)
         for f in futs:
             f.result()
-        return out
+        return outs
 
     def _deliver(self, t, host_h, host_i, tokens):
         """Results to ordinary host memory beside the engine's loop; the
         page-locked buffers then go back to the arena (or the caching
         allocator) for later planets.  The request is finished when its
         arrays are in place."""
-        t.heights = self._copy_out(host_h)
-        t.insolation = self._copy_out(host_i) if host_i is not None else None
+        if host_i is not None:
+            t.heights, t.insolation = self._copy_out(host_h, host_i)
+        else:
+            (t.heights,), t.insolation = self._copy_out(host_h), None
         t.finished = time.perf_counter()
         for tok in tokens:
             self.host.release(tok)
