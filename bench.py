@@ -558,7 +558,14 @@ def summary(line):
            "ratio_vs_plain": g(line["ratio_vs_plain"], 3), "ratio_vs_plain_blocked": g(line["ratio_vs_plain_blocked"], 3),
            "batch_equals_plain": line["plain_per_planet"].get("batch_equals_plain")}
     rf = line.get("roofline") or {}
-    out["roofline_frac"] = {k: g(v.get("frac"), 3) for k, v in (rf.get("kernels") or {}).items()}
+    ks = rf.get("kernels") or {}
+    out["roofline_frac"] = {k: g(v.get("frac"), 3) for k, v in ks.items()}
+    # what the compute-bound kernels issue against the issue peak
+    issue = {k: g((v.get("executed") or {}).get("issue_frac"), 3) for k, v in ks.items()
+             if (v.get("executed") or {}).get("issue_frac") is not None}
+    issue.update({k: g(v.get("frac"), 3) for k, v in ks.items() if v.get("bound") == "issue"})
+    if issue:
+        out["issue_frac"] = issue
     sv = line.get("serving")
     if sv:
         out["serving"] = {"requests": sv["requests"]}
