@@ -98,3 +98,23 @@ def test_pinned_arena_hands_out_and_takes_back_ranges():
     a.release(t2)
     a.release(t3)
     assert a.pages.used == 0
+
+
+def test_small_and_large_planets_set_up_on_their_own_streams():
+    """Planets under serve.SMALL_ROWS vertices build their meshes and run
+    their noise on the higher-priority pair of streams, larger ones on the
+    other; arriving interleaved (a small planet right behind a large one
+    whose mesh is still being built), every result still equals the planet
+    generated alone."""
+    from nixis_gb300 import serve
+    from nixis_gb300.planets import PlanetRequest
+    ks = [470, 24, 510, 36, 16, 480, 52]
+    stream = [(0.002 * i, PlanetRequest(seed=300 + i, divisions=k, octaves=6, erosion_iters=5 + 3 * i,
+                                         insolation=i % 2 == 0, days=5))
+              for i, k in enumerate(ks)]
+    sizes = [r.n_vertices for _, r in stream]
+    assert min(sizes) < serve.SMALL_ROWS <= max(sizes)
+    with serve.ServeEngine(hbm_budget=16 * 2**30, arena_rows=12_000_000, slots=16) as eng:
+        eng.warmup()
+        tickets = eng.run(stream)
+    check_against_alone(tickets)
