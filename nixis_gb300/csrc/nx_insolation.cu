@@ -17,8 +17,17 @@
 // i.e. two operations per sun position.  Vertices off that sphere
 // (| |v|^2 - r^2 | > 1e-12 r^2) take the reference's general formula.
 //
-// Sums per tilt are binary32 (<= 360 terms); the running total over tilts
-// is compensated (Kahan) so the result tracks the binary64 sum.
+// With u = cos(tau) U(theta), U = x cos(theta) - y sin(theta) the same on
+// every day, a day's pairs sum to n C + |cos tau| sum_h max(c, |U_h|),
+// c = |z| |tan tau|.  Schedules of up to SORT_MAX days are then summed by
+// breakpoints: each max picks one side, so over the year the sum is
+// sum_h [ |U_h| (sum of |cos| over days with c < |U_h|) + |z| (sum of
+// |cos| |tan| over the other days) ], both inner sums read from prefix /
+// suffix sums over the days sorted by |tan tau| (built once per block), at
+// a count found through a bucket index: twelve lookups per vertex for a
+// year of hourly positions.  Longer schedules sum day by day (paired lanes,
+// groups of 8 days, Kahan across groups), so the result tracks the binary64
+// sum either way.
 #include "nx_common.cuh"
 
 namespace nx {
